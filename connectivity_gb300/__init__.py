@@ -1,0 +1,406 @@
+"""Python binding of libgbconn, the GB300 Multistep SCC / WCC library.
+
+The compute path is the CUDA library behind the C ABI in include/gbconn.h;
+this module only loads it with ctypes and converts numpy arrays.  There is no
+CPU fallback: if libgbconn.so is missing, importing this module raises, and
+without a GB300 the run functions raise GBError.
+
+Reference surface (HPCGraphAnalysis/Connectivity, multistep/):
+    read_edge      scc_main.cpp:94-125      -> read_edge()
+    create_csr     scc_main.cpp:127-191     -> Graph.from_edges() / from_csr()
+    run_scc        scc_main.cpp:210-317     -> Context.scc()
+    run_cc         cc_main.cpp:184-245      -> Context.wcc() / Context.cc()
+    scc_verify     scc_verify.cpp:47-77     -> scc_verify()
+    cc_verify      cc_verify.cpp:47-74      -> cc_verify()
+    output_scc     scc_main.cpp:193-202     -> output_labels()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgbconn.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with "
+        "`python -c 'import __graft_entry__ as g; g.build()'` or "
+        "`python connectivity_gb300/build.py`")
+
+_lib = C.CDLL(LIB_PATH)
+
+GB_OK = 0
+STATUS_NAMES = {
+    0: "GB_OK", 1: "GB_ERR_INVALID", 2: "GB_ERR_CUDA", 3: "GB_ERR_OOM",
+    4: "GB_ERR_TIMEOUT", 5: "GB_ERR_ITER_LIMIT", 6: "GB_ERR_IO",
+    7: "GB_ERR_NO_DEVICE", 8: "GB_ERR_UNSUPPORTED", 9: "GB_ERR_CAPACITY",
+}
+
+
+class GBError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        detail = _lib.gb_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({detail})")
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("trim_level", C.c_int32), ("canonical", C.c_int32), ("pivot", C.c_int32),
+        ("vert_cutoff", C.c_int32), ("t_block", C.c_int32), ("t_grid", C.c_int32),
+        ("k_pull", C.c_int32), ("alpha", C.c_float), ("beta", C.c_float),
+        ("max_steps", C.c_int32), ("grid_blocks", C.c_int32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("ms_trim", C.c_double), ("ms_reach", C.c_double), ("ms_colour", C.c_double),
+        ("ms_canon", C.c_double), ("ms_total", C.c_double),
+        ("pivot", C.c_int32), ("colour_rounds", C.c_int32),
+        ("n_trim", C.c_int64), ("n_visit_fw", C.c_int64), ("n_fwbw", C.c_int64),
+        ("unassigned", C.c_int64), ("vtx_reads", C.c_int64), ("edge_reads", C.c_int64),
+        ("list_rw", C.c_int64), ("trim_steps", C.c_int64), ("fw_steps", C.c_int64),
+        ("bw_steps", C.c_int64), ("pull_steps", C.c_int64), ("colour_steps", C.c_int64),
+        ("mark_steps", C.c_int64), ("grid_blocks", C.c_int32), ("err_where", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_I64P = C.POINTER(C.c_int64)
+
+
+def _sig(name, res, args):
+    f = getattr(_lib, name)
+    f.restype = res
+    f.argtypes = args
+    return f
+
+
+_sig("gb_status_string", C.c_char_p, [C.c_int32])
+_sig("gb_last_error", C.c_char_p, [])
+_sig("gb_opts_default", None, [C.POINTER(Opts)])
+_sig("gb_ctx_create", C.c_int32, [C.c_int, C.POINTER(_P)])
+_sig("gb_ctx_destroy", C.c_int32, [_P])
+_sig("gb_ctx_set_stream", C.c_int32, [_P, _P])
+_sig("gb_ctx_stream", _P, [_P])
+_sig("gb_ctx_sync", C.c_int32, [_P])
+_sig("gb_graph_from_edges", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, C.POINTER(_P)])
+_sig("gb_graph_from_csr", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, _P, _P, C.POINTER(_P)])
+_sig("gb_graph_from_csr32", C.c_int32, [_P, C.c_int32, C.c_uint32, _P, _P, _P, _P, C.POINTER(_P)])
+_sig("gb_graph_rmat", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                  C.c_double, C.POINTER(_P)])
+_sig("gb_graph_info", C.c_int32, [_P, _I32P, _I64P, _I32P])
+_sig("gb_graph_csr_to_host", C.c_int32, [_P, _P, _P, _P, _P])
+_sig("gb_graph_device_csr", C.c_int32, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+                                        C.POINTER(_P)])
+_sig("gb_graph_pivot", C.c_int32, [_P, _P, C.c_int32, _I32P, C.POINTER(C.c_double)])
+_sig("gb_graph_destroy", C.c_int32, [_P])
+for _n in ("gb_scc", "gb_wcc", "gb_cc"):
+    _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
+for _n in ("gb_scc_async", "gb_wcc_async"):
+    _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
+_sig("gb_run_scc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int])
+_sig("gb_run_cc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, C.c_int, C.c_double])
+_sig("gb_read_edge", C.c_int32, [C.c_char_p, _I32P, _I64P, C.POINTER(_P), C.POINTER(_P)])
+_sig("gb_free_host", None, [_P])
+_sig("gb_output_labels", C.c_int32, [C.c_char_p, C.c_int32, _P])
+_sig("gb_scc_verify", C.c_int32, [C.c_int32, _P, C.c_char_p, C.c_size_t, _I64P])
+_sig("gb_cc_verify", C.c_int32, [C.c_int32, _P, C.c_char_p, C.c_size_t, _I64P])
+_sig("gb_canonicalize", C.c_int32, [C.c_int32, _P])
+_sig("gb_rmat_edges_host", C.c_int32, [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                       C.c_double, _I64P, C.POINTER(_P), C.POINTER(_P)])
+_sig("gb_grid_edges_host", C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _I32P, _I64P,
+                                       C.POINTER(_P), C.POINTER(_P)])
+_sig("gb_batch_sizes", C.c_int32, [C.c_int32, C.c_uint64, C.c_double, C.c_double, C.c_int32,
+                                   C.c_int32, C.c_int32, C.c_int32, _P, _P, _P])
+
+
+def _check(status: int, where: str) -> None:
+    if status != GB_OK:
+        raise GBError(status, where)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _take(p: C.c_void_p, count: int, dtype) -> np.ndarray:
+    """Copies a library-malloc'd array into numpy and frees it."""
+    if count == 0:
+        out = np.zeros(0, dtype=dtype)
+    else:
+        buf = (C.c_byte * (count * np.dtype(dtype).itemsize)).from_address(p.value)
+        out = np.frombuffer(buf, dtype=dtype).copy()
+    _lib.gb_free_host(p)
+    return out
+
+
+def opts(**kw) -> Opts:
+    o = Opts()
+    _lib.gb_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+# ---------------------------------------------------------------------------
+# host utilities
+# ---------------------------------------------------------------------------
+def read_edge(path: str) -> tuple[int, np.ndarray, np.ndarray]:
+    """read_edge (scc_main.cpp:94-125): returns (n, src, dst)."""
+    n, m = C.c_int32(), C.c_int64()
+    s, d = C.c_void_p(), C.c_void_p()
+    _check(_lib.gb_read_edge(path.encode(), C.byref(n), C.byref(m), C.byref(s), C.byref(d)),
+           "read_edge")
+    return n.value, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
+
+
+def output_labels(path: str, labels: np.ndarray) -> None:
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    _check(_lib.gb_output_labels(path.encode(), lab.size, _ptr(lab)), "output_labels")
+
+
+def scc_verify(labels: np.ndarray) -> str:
+    """The exact scc_verify line (scc_verify.cpp:73-74), with newline."""
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    buf = C.create_string_buffer(256)
+    _check(_lib.gb_scc_verify(lab.size, _ptr(lab), buf, 256, None), "scc_verify")
+    return buf.value.decode()
+
+
+def cc_verify(labels: np.ndarray) -> str:
+    """The exact cc_verify line (cc_verify.cpp:70-71), with newline."""
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    buf = C.create_string_buffer(256)
+    _check(_lib.gb_cc_verify(lab.size, _ptr(lab), buf, 256, None), "cc_verify")
+    return buf.value.decode()
+
+
+def canonicalize(labels: np.ndarray) -> np.ndarray:
+    lab = np.array(labels, dtype=np.int32, copy=True)
+    _check(_lib.gb_canonicalize(lab.size, _ptr(lab)), "canonicalize")
+    return lab
+
+
+RMAT_ABC = (0.57, 0.19, 0.19)
+
+
+def rmat_edges(scale: int, edge_factor: int = 16, seed: int = 1,
+               abc: tuple[float, float, float] = RMAT_ABC) -> tuple[int, np.ndarray, np.ndarray]:
+    """Seeded R-MAT edge list (host), without self-loops and duplicates,
+    sorted by (src, dst).  Returns (n, src, dst)."""
+    m = C.c_int64()
+    s, d = C.c_void_p(), C.c_void_p()
+    _check(_lib.gb_rmat_edges_host(scale, edge_factor, seed, abc[0], abc[1], abc[2], C.byref(m),
+                                   C.byref(s), C.byref(d)), "rmat_edges")
+    return 1 << scale, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
+
+
+def grid_edges(side: int, extra: int | None = None, max_chain: int = 64,
+               seed: int = 2) -> tuple[int, np.ndarray, np.ndarray]:
+    """Oriented side x side lattice plus `extra` chain vertices (default
+    side*side // 10).  Returns (n, src, dst)."""
+    if extra is None:
+        extra = side * side // 10
+    n, m = C.c_int32(), C.c_int64()
+    s, d = C.c_void_p(), C.c_void_p()
+    _check(_lib.gb_grid_edges_host(side, extra, max_chain, seed, C.byref(n), C.byref(m),
+                                   C.byref(s), C.byref(d)), "grid_edges")
+    return n.value, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
+
+
+def batch_sizes(count: int, seed: int = 4, median: float = 2000.0, sigma: float = 1.5,
+                n_min: int = 64, n_max: int = 500_000, ef_min: int = 4,
+                ef_max: int = 32) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    ns = np.zeros(count, np.int32)
+    efs = np.zeros(count, np.int32)
+    seeds = np.zeros(count, np.uint64)
+    _check(_lib.gb_batch_sizes(count, seed, median, sigma, n_min, n_max, ef_min, ef_max,
+                               _ptr(ns), _ptr(efs), _ptr(seeds)), "batch_sizes")
+    return ns, efs, seeds
+
+
+def csr_from_edges(n: int, src: np.ndarray, dst: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Host CSR (int64 offsets, int32 adjacency) keyed by src, stable."""
+    order = np.argsort(src, kind="stable")
+    adj = np.ascontiguousarray(dst[order], dtype=np.int32)
+    off = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(src, minlength=n), out=off[1:])
+    return off, adj
+
+
+# ---------------------------------------------------------------------------
+# device objects
+# ---------------------------------------------------------------------------
+class Context:
+    """A CUDA stream plus the device workspace of the runs (gb_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        _check(_lib.gb_ctx_create(device, C.byref(self._h)), "gb_ctx_create")
+
+    def close(self) -> None:
+        if self._h:
+            _lib.gb_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        _check(_lib.gb_ctx_set_stream(self._h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    @property
+    def stream(self) -> int:
+        return _lib.gb_ctx_stream(self._h) or 0
+
+    def sync(self) -> None:
+        _check(_lib.gb_ctx_sync(self._h), "gb_ctx_sync")
+
+    def _run(self, fn, name, g: "Graph", labels, o: Opts | None, want_stats: bool):
+        st = Stats()
+        if labels is None:
+            labels = np.empty(g.n, np.int32)
+        ptr = _ptr(labels) if isinstance(labels, np.ndarray) else C.c_void_p(int(labels))
+        _check(fn(self._h, g._h, ptr, C.byref(o or opts()), C.byref(st)), name)
+        return (labels, st) if want_stats else labels
+
+    def scc(self, g: "Graph", labels=None, o: Opts | None = None, stats: bool = False):
+        """run_scc: canonical SCC labels (numpy int32, or into a device pointer)."""
+        return self._run(_lib.gb_scc, "gb_scc", g, labels, o, stats)
+
+    def wcc(self, g: "Graph", labels=None, o: Opts | None = None, stats: bool = False):
+        """run_cc on the mirrored graph: WCC / CC labels."""
+        return self._run(_lib.gb_wcc, "gb_wcc", g, labels, o, stats)
+
+    cc = wcc
+
+    def scc_async(self, g: "Graph", labels_dev: int, o: Opts | None = None) -> None:
+        _check(_lib.gb_scc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+               "gb_scc_async")
+
+    def wcc_async(self, g: "Graph", labels_dev: int, o: Opts | None = None) -> None:
+        _check(_lib.gb_wcc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+               "gb_wcc_async")
+
+    def pivot(self, g: "Graph", kind: int = 0) -> tuple[int, float]:
+        p, a = C.c_int32(), C.c_double()
+        _check(_lib.gb_graph_pivot(self._h, g._h, kind, C.byref(p), C.byref(a)), "gb_graph_pivot")
+        return p.value, a.value
+
+
+class Graph:
+    """A device-resident graph: out- and in-CSR (gb_graph)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        n, m, sym = C.c_int32(), C.c_int64(), C.c_int32()
+        _check(_lib.gb_graph_info(handle, C.byref(n), C.byref(m), C.byref(sym)), "gb_graph_info")
+        self.n, self.m, self.symmetric = n.value, m.value, bool(sym.value)
+
+    @classmethod
+    def from_edges(cls, ctx: Context, n: int, src, dst) -> "Graph":
+        """create_csr on the device; src/dst numpy int32 arrays or device
+        pointers (ints) with m = len."""
+        h = C.c_void_p()
+        if isinstance(src, np.ndarray):
+            s = np.ascontiguousarray(src, dtype=np.int32)
+            d = np.ascontiguousarray(dst, dtype=np.int32)
+            _check(_lib.gb_graph_from_edges(ctx._h, n, s.size, _ptr(s), _ptr(d), C.byref(h)),
+                   "gb_graph_from_edges")
+        else:
+            raise TypeError("src/dst must be numpy arrays")
+        return cls(h)
+
+    @classmethod
+    def from_csr(cls, ctx: Context, n: int, out_off, out_adj, in_off=None, in_adj=None) -> "Graph":
+        h = C.c_void_p()
+        oo = np.ascontiguousarray(out_off, dtype=np.int64)
+        oa = np.ascontiguousarray(out_adj, dtype=np.int32)
+        io = None if in_off is None else np.ascontiguousarray(in_off, dtype=np.int64)
+        ia = None if in_adj is None else np.ascontiguousarray(in_adj, dtype=np.int32)
+        _check(_lib.gb_graph_from_csr(ctx._h, n, oa.size, _ptr(oo), _ptr(oa), _ptr(io), _ptr(ia),
+                                      C.byref(h)), "gb_graph_from_csr")
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, ctx: Context, scale: int, edge_factor: int = 16, seed: int = 1,
+             abc: tuple[float, float, float] = RMAT_ABC) -> "Graph":
+        h = C.c_void_p()
+        _check(_lib.gb_graph_rmat(ctx._h, scale, edge_factor, seed, abc[0], abc[1], abc[2],
+                                  C.byref(h)), "gb_graph_rmat")
+        return cls(h)
+
+    def to_host(self) -> tuple[np.ndarray, np.ndarray, np.ndarray | None, np.ndarray | None]:
+        oo = np.empty(self.n + 1, np.int64)
+        oa = np.empty(self.m, np.int32)
+        io = None if self.symmetric else np.empty(self.n + 1, np.int64)
+        ia = None if self.symmetric else np.empty(self.m, np.int32)
+        _check(_lib.gb_graph_csr_to_host(self._h, _ptr(oo), _ptr(oa), _ptr(io), _ptr(ia)),
+               "gb_graph_csr_to_host")
+        return oo, oa, io, ia
+
+    def device_csr(self) -> tuple[int, int, int, int]:
+        ps = [C.c_void_p() for _ in range(4)]
+        _check(_lib.gb_graph_device_csr(self._h, *[C.byref(p) for p in ps]), "gb_graph_device_csr")
+        return tuple(p.value or 0 for p in ps)
+
+    def close(self) -> None:
+        if self._h:
+            _lib.gb_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_scc_ref(n: int, out_array, in_array, out_degree_list, in_degree_list,
+                max_deg_vert: int = -1, avg_degree: float = 0.0, vert_cutoff: int = 10000,
+                scc_maps: np.ndarray | None = None) -> np.ndarray:
+    """gb_run_scc: the reference's run_scc signature on host buffers
+    (32-bit offsets as in its graph struct)."""
+    if scc_maps is None:
+        scc_maps = np.empty(n, np.int32)
+    m = int(out_degree_list[n])
+    _check(_lib.gb_run_scc(n, m, _ptr(out_array), _ptr(in_array), _ptr(out_degree_list),
+                           _ptr(in_degree_list), _ptr(scc_maps), max_deg_vert, avg_degree,
+                           vert_cutoff), "gb_run_scc")
+    return scc_maps
+
+
+def run_cc_ref(n: int, out_array, out_degree_list, max_deg_vert: int = -1,
+               avg_degree: float = 0.0, cc_maps: np.ndarray | None = None) -> np.ndarray:
+    """gb_run_cc: the reference's run_cc signature on the mirrored host CSR."""
+    if cc_maps is None:
+        cc_maps = np.empty(n, np.int32)
+    m = int(out_degree_list[n])
+    _check(_lib.gb_run_cc(n, m, _ptr(out_array), _ptr(out_degree_list), _ptr(cc_maps),
+                          max_deg_vert, avg_degree), "gb_run_cc")
+    return cc_maps
+
+
+@dataclass
+class Info:
+    lib_path: str = LIB_PATH
+
+
+__all__ = [
+    "Context", "Graph", "GBError", "Opts", "Stats", "opts", "read_edge", "output_labels",
+    "scc_verify", "cc_verify", "canonicalize", "rmat_edges", "grid_edges", "batch_sizes",
+    "csr_from_edges", "run_scc_ref", "run_cc_ref", "LIB_PATH",
+]

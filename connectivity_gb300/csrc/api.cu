@@ -1,0 +1,667 @@
+// C ABI of libgbconn (include/gbconn.h): contexts, device graphs, runs and
+// the reference-shaped drop-ins.  Host code only; the kernels live in
+// kernels.cu and csr_build.cu.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "../../include/gbconn.h"
+#include "gb_internal.cuh"
+#include "host_internal.h"
+
+struct gb_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  int grid = 0;                 // cooperative grid (all resident blocks)
+  int32_t cap_n = -1;           // workspace capacity in vertices
+  void* ws = nullptr;
+  gb::Work w{};
+  gb::Ctl* d_ctl = nullptr;
+  gb::Ctl* h_ctl = nullptr;     // pinned
+  int* d_sticky = nullptr;      // first error of any run since the last sync
+  int* h_sticky = nullptr;      // pinned
+  cudaEvent_t ev[5] = {};
+};
+
+struct gb_graph {
+  int device = 0;
+  int32_t n = 0;
+  int64_t m = 0;
+  int symmetric = 0;
+  int64_t* out_off = nullptr;
+  int32_t* out_adj = nullptr;
+  int64_t* in_off = nullptr;
+  int32_t* in_adj = nullptr;
+};
+
+namespace {
+
+gb_status cuda_fail(cudaError_t e, const char* where) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  gb_set_error("%s", buf);
+  if (e == cudaErrorMemoryAllocation) return GB_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GB_ERR_NO_DEVICE;
+  return GB_ERR_CUDA;
+}
+#define CK(call, where)                              \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Grows the context workspace to n vertices (never shrinks).
+gb_status ensure_ws(gb_ctx* c, int32_t n) {
+  if (n <= c->cap_n) return GB_OK;
+  if (c->ws) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->ws);
+    c->ws = nullptr;
+    c->cap_n = -1;
+  }
+  const size_t nv = (size_t)(n > 0 ? n : 1) + 32;
+  const size_t nw = nv / 32 + 2;
+  const size_t arr = align256(nv * 4), bm = align256(nw * 4);
+  const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
+  const size_t total = 14 * arr + 4 * bm + align256(G * 4) + align256(G * 8);
+  char* p = nullptr;
+  CK(cudaMalloc(&p, total), "workspace allocation");
+  c->ws = p;
+  gb::Work& w = c->w;
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += bytes;
+    return r;
+  };
+  w.label = (int32_t*)take(arr);
+  w.colour = (int32_t*)take(arr);
+  w.stamp = (int32_t*)take(arr);
+  w.live_in = (int32_t*)take(arr);
+  w.live_out = (int32_t*)take(arr);
+  w.listA = (int32_t*)take(arr);
+  w.listB = (int32_t*)take(arr);
+  w.q = (int32_t*)take(arr);
+  w.x0 = (int32_t*)take(arr);
+  w.x1 = (int32_t*)take(arr);
+  w.candA = (int32_t*)take(arr);
+  w.candB = (int32_t*)take(arr);
+  w.h0 = (int32_t*)take(arr);
+  w.h1 = (int32_t*)take(arr);
+  w.vbits = (uint32_t*)take(bm);
+  w.fvis = (uint32_t*)take(bm);
+  w.bvis = (uint32_t*)take(bm);
+  w.done = (uint32_t*)take(bm);
+  w.blk_i = (int32_t*)take(align256(G * 4));
+  w.blk_l = (long long*)take(align256(G * 8));
+  w.ctl = c->d_ctl;
+  c->cap_n = n;
+  return GB_OK;
+}
+
+void fill_params(const gb_opts* o, gb::RunParams& p) {
+  gb_opts d;
+  gb_opts_default(&d);
+  if (!o) o = &d;
+  p.trim_level = o->trim_level >= 2 ? 2 : 1;
+  p.canonical = o->canonical ? 1 : 0;
+  p.pivot_hint = o->pivot;
+  p.tune.t_block = o->t_block > 32 ? o->t_block : 32;
+  p.tune.t_grid = o->t_grid > p.tune.t_block ? o->t_grid : p.tune.t_block + 1;
+  p.tune.k_pull = o->k_pull > 0 ? o->k_pull : 1;
+  p.tune.alpha = o->alpha > 0 ? o->alpha : 15.0f;
+  p.tune.beta = o->beta > 0 ? o->beta : 25.0f;
+  p.tune.max_steps = o->max_steps > 0 ? o->max_steps : (1 << 30);
+}
+
+gb_status graph_alloc(gb_graph* g, bool with_in) {
+  const size_t offb = (size_t)(g->n + 1) * 8, adjb = (size_t)(g->m > 0 ? g->m : 1) * 4;
+  CK(cudaMalloc(&g->out_off, offb), "graph allocation");
+  CK(cudaMalloc(&g->out_adj, adjb), "graph allocation");
+  if (with_in) {
+    CK(cudaMalloc(&g->in_off, offb), "graph allocation");
+    CK(cudaMalloc(&g->in_adj, adjb), "graph allocation");
+  }
+  return GB_OK;
+}
+
+void graph_free(gb_graph* g) {
+  if (!g) return;
+  cudaFree(g->out_off);
+  cudaFree(g->out_adj);
+  cudaFree(g->in_off);
+  cudaFree(g->in_adj);
+  g->out_off = g->in_off = nullptr;
+  g->out_adj = g->in_adj = nullptr;
+}
+
+gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
+  CK(cudaStreamSynchronize(c->stream), "run");
+  const gb::Ctl& h = *c->h_ctl;
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    float ms[4] = {0, 0, 0, 0}, tot = 0;
+    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
+    cudaEventElapsedTime(&tot, c->ev[0], c->ev[4]);
+    st->ms_trim = ms[0];
+    st->ms_reach = ms[1];
+    st->ms_colour = ms[2];
+    st->ms_canon = ms[3];
+    st->ms_total = tot;
+    st->pivot = h.pivot;
+    st->colour_rounds = h.ncolour_rounds;
+    st->n_trim = h.ntrim;
+    st->n_visit_fw = h.nvisit_fw;
+    st->n_fwbw = h.nscc_fwbw;
+    st->unassigned = h.unassigned;
+    st->vtx_reads = (int64_t)h.stat[gb::kStVtx];
+    st->edge_reads = (int64_t)h.stat[gb::kStEdges];
+    st->list_rw = (int64_t)h.stat[gb::kStList];
+    st->trim_steps = (int64_t)h.stat[gb::kStTrimSteps];
+    st->fw_steps = (int64_t)h.stat[gb::kStFwSteps];
+    st->bw_steps = (int64_t)h.stat[gb::kStBwSteps];
+    st->pull_steps = (int64_t)h.stat[gb::kStPullSteps];
+    st->colour_steps = (int64_t)h.stat[gb::kStColourSteps];
+    st->mark_steps = (int64_t)h.stat[gb::kStMarkSteps];
+    st->grid_blocks = c->grid;
+    st->err_where = h.err_where;
+  }
+  *c->h_sticky = 0;
+  cudaMemsetAsync(c->d_sticky, 0, 2 * sizeof(int), c->stream);
+  if (h.err != 0) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "device error %d at site %d", h.err, h.err_where);
+    gb_set_error("%s", buf);
+    return (gb_status)h.err;
+  }
+  (void)g;
+  return GB_OK;
+}
+
+gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
+              const gb_opts* o, gb_stats* st, bool wait) {
+  if (!c || !g) {
+    gb_set_error("run: null context or graph%s", "");
+    return GB_ERR_INVALID;
+  }
+  if (g->n > 0 && !labels) {
+    gb_set_error("run: null labels%s", "");
+    return GB_ERR_INVALID;
+  }
+  if (g->device != c->device) {
+    gb_set_error("run: graph and context are on different devices%s", "");
+    return GB_ERR_INVALID;
+  }
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (g->n == 0) return GB_OK;
+  gb_status s = ensure_ws(c, g->n);
+  if (s != GB_OK) return s;
+  const bool dev_labels = is_device_ptr(labels);
+  if (!wait && !dev_labels) {
+    gb_set_error("run: the asynchronous form needs device labels%s", "");
+    return GB_ERR_INVALID;
+  }
+  gb::Work w = c->w;
+  w.n = g->n;
+  w.nwords = (g->n + 31) / 32;
+  w.m = g->m;
+  if (dev_labels) w.label = labels;
+  gb::RunParams p;
+  fill_params(o, p);
+  int grid = c->grid;
+  if (o && o->grid_blocks > 0 && o->grid_blocks < grid) grid = o->grid_blocks;
+  gb::GraphView gv;
+  gv.n = g->n;
+  gv.m = g->m;
+  gv.out = {g->out_off, g->out_adj};
+  if (g->symmetric) {
+    // a symmetric graph is its own reverse
+    gv.in = kind == gb::kSCC ? gv.out : gb::Csr{nullptr, nullptr};
+  } else {
+    gv.in = {g->in_off, g->in_adj};
+  }
+  cudaStream_t sm = c->stream;
+  CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
+  CK(cudaMemsetAsync(w.fvis, 0, (size_t)w.nwords * 4, sm), "memset");
+  CK(cudaMemsetAsync(w.bvis, 0, (size_t)w.nwords * 4, sm), "memset");
+  CK(cudaMemsetAsync(w.done, 0, (size_t)w.nwords * 4, sm), "memset");
+  CK(cudaMemsetAsync(w.stamp, 0xff, (size_t)g->n * 4, sm), "memset");
+  CK(gb::launch_run(gv, kind, p, w, grid, sm, c->ev), "kernel launch");
+  CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
+  if (!dev_labels)
+    CK(cudaMemcpyAsync(labels, w.label, (size_t)g->n * 4, cudaMemcpyDeviceToHost, sm), "labels copy");
+  CK(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(gb::Ctl), cudaMemcpyDeviceToHost, sm), "status copy");
+  if (!wait) return GB_OK;
+  return finish_run(c, g, st);
+}
+
+std::mutex g_default_mu;
+gb_ctx* g_default_ctx = nullptr;
+gb_graph* g_stage = nullptr;     // reused device buffers of the drop-ins
+int64_t g_stage_m = -1;
+int32_t g_stage_n = -1;
+
+}  // namespace
+
+extern "C" {
+
+void gb_opts_default(gb_opts* o) {
+  if (!o) return;
+  o->trim_level = 1;
+  o->canonical = 1;
+  o->pivot = -1;
+  o->vert_cutoff = 10000;
+  o->t_block = 512;
+  o->t_grid = 32768;
+  o->k_pull = 8;
+  o->alpha = 15.0f;
+  o->beta = 25.0f;
+  o->max_steps = 1 << 30;
+  o->grid_blocks = 0;
+}
+
+gb_status gb_ctx_create(int device, gb_ctx** out) {
+  if (!out) return GB_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    gb_set_error("gb_ctx_create: %s", e != cudaSuccess ? cudaGetErrorString(e) : "no device");
+    return GB_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return GB_ERR_INVALID;
+  CK(cudaSetDevice(device), "cudaSetDevice");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+  if (prop.major != 10 || prop.minor != 3 || !prop.cooperativeLaunch) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "device %d is sm_%d%d (needs sm_103 with cooperative launch)",
+                  device, prop.major, prop.minor);
+    gb_set_error("gb_ctx_create: %s", buf);
+    return GB_ERR_UNSUPPORTED;
+  }
+  gb_ctx* c = new (std::nothrow) gb_ctx();
+  if (!c) return GB_ERR_OOM;
+  c->device = device;
+  gb_status s = GB_OK;
+  do {
+    cudaError_t r;
+    if ((r = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess) { s = cuda_fail(r, "stream"); break; }
+    c->stream = c->own;
+    if ((r = cudaMalloc(&c->d_ctl, sizeof(gb::Ctl))) != cudaSuccess) { s = cuda_fail(r, "ctl"); break; }
+    if ((r = cudaMallocHost(&c->h_ctl, sizeof(gb::Ctl))) != cudaSuccess) { s = cuda_fail(r, "ctl"); break; }
+    if ((r = cudaMalloc(&c->d_sticky, 2 * sizeof(int))) != cudaSuccess) { s = cuda_fail(r, "sticky"); break; }
+    if ((r = cudaMallocHost(&c->h_sticky, 2 * sizeof(int))) != cudaSuccess) { s = cuda_fail(r, "sticky"); break; }
+    cudaMemset(c->d_sticky, 0, 2 * sizeof(int));
+    std::memset(c->h_ctl, 0, sizeof(gb::Ctl));
+    c->h_sticky[0] = c->h_sticky[1] = 0;
+    for (int i = 0; i < 5 && s == GB_OK; ++i)
+      if ((r = cudaEventCreate(&c->ev[i])) != cudaSuccess) s = cuda_fail(r, "event");
+    if (s != GB_OK) break;
+    c->grid = gb::max_coop_grid(device);
+    if (c->grid <= 0) { gb_set_error("gb_ctx_create: %s", "no cooperative occupancy"); s = GB_ERR_UNSUPPORTED; break; }
+  } while (0);
+  if (s != GB_OK) {
+    gb_ctx_destroy(c);
+    return s;
+  }
+  *out = c;
+  return GB_OK;
+}
+
+gb_status gb_ctx_destroy(gb_ctx* c) {
+  if (!c) return GB_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->ws);
+  cudaFree(c->d_ctl);
+  cudaFree(c->d_sticky);
+  if (c->h_ctl) cudaFreeHost(c->h_ctl);
+  if (c->h_sticky) cudaFreeHost(c->h_sticky);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return GB_OK;
+}
+
+gb_status gb_ctx_set_stream(gb_ctx* c, void* s) {
+  if (!c) return GB_ERR_INVALID;
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return GB_OK;
+}
+
+void* gb_ctx_stream(gb_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+gb_status gb_ctx_sync(gb_ctx* c) {
+  if (!c) return GB_ERR_INVALID;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(c->h_sticky, c->d_sticky, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream), "sync");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  const int err = c->h_sticky[0], where = c->h_sticky[1];
+  CK(cudaMemsetAsync(c->d_sticky, 0, 2 * sizeof(int), c->stream), "sync");
+  if (err) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "device error %d at site %d", err, where);
+    gb_set_error("%s", buf);
+    return (gb_status)err;
+  }
+  return GB_OK;
+}
+
+gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
+                              const int32_t* dst, gb_graph** out) {
+  if (!c || !out || n < 0 || m < 0 || (m > 0 && (!src || !dst))) return GB_ERR_INVALID;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  gb_graph* g = new (std::nothrow) gb_graph();
+  if (!g) return GB_ERR_OOM;
+  g->device = c->device;
+  g->n = n;
+  g->m = m;
+  gb_status s = graph_alloc(g, true);
+  const int32_t *ds = src, *dd = dst;
+  int32_t *ts = nullptr, *tt = nullptr;
+  if (s == GB_OK && m > 0 && !is_device_ptr(src)) {
+    cudaError_t e = cudaMalloc(&ts, (size_t)m * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&tt, (size_t)m * 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ts, src, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tt, dst, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) s = cuda_fail(e, "edge upload");
+    ds = ts;
+    dd = tt;
+  }
+  if (s == GB_OK) {
+    bool ok = true;
+    cudaError_t e = gb::build_csr(n, m, ds, dd, g->out_off, g->out_adj, g->in_off, g->in_adj, c->stream, &ok);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) s = cuda_fail(e, "CSR build");
+    else if (!ok) {
+      gb_set_error("gb_graph_from_edges: %s", "vertex id outside [0, n)");
+      s = GB_ERR_INVALID;
+    }
+  }
+  cudaFree(ts);
+  cudaFree(tt);
+  if (s != GB_OK) {
+    graph_free(g);
+    delete g;
+    return s;
+  }
+  *out = g;
+  return GB_OK;
+}
+
+// Validates CSR arrays already on the device: off[0] == 0, off[n] == m,
+// offsets non-decreasing, ids in [0, n).
+static gb_status validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off, const int32_t* adj) {
+  int bad = 0;
+  cudaError_t e = gb::check_csr(n, m, off, adj, c->stream, &bad);
+  if (e != cudaSuccess) return cuda_fail(e, "CSR check");
+  if (bad) {
+    gb_set_error("CSR check: %s", "offsets not monotone from 0 to m, or an id outside [0, n)");
+    return GB_ERR_INVALID;
+  }
+  return GB_OK;
+}
+
+static gb_status upload(gb_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return GB_OK;
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream), "upload");
+  return GB_OK;
+}
+
+gb_status gb_graph_from_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* out_off,
+                            const int32_t* out_adj, const int64_t* in_off, const int32_t* in_adj,
+                            gb_graph** out) {
+  if (!c || !out || n < 0 || m < 0 || !out_off || (m > 0 && !out_adj)) return GB_ERR_INVALID;
+  if (in_off == nullptr ? in_adj != nullptr : (m > 0 && in_adj == nullptr)) return GB_ERR_INVALID;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  gb_graph* g = new (std::nothrow) gb_graph();
+  if (!g) return GB_ERR_OOM;
+  g->device = c->device;
+  g->n = n;
+  g->m = m;
+  g->symmetric = in_off == nullptr;
+  gb_status s = graph_alloc(g, !g->symmetric);
+  if (s == GB_OK) s = upload(c, g->out_off, out_off, (size_t)(n + 1) * 8);
+  if (s == GB_OK) s = upload(c, g->out_adj, out_adj, (size_t)m * 4);
+  if (s == GB_OK && !g->symmetric) s = upload(c, g->in_off, in_off, (size_t)(n + 1) * 8);
+  if (s == GB_OK && !g->symmetric) s = upload(c, g->in_adj, in_adj, (size_t)m * 4);
+  if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
+  if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
+  if (s != GB_OK) {
+    graph_free(g);
+    delete g;
+    return s;
+  }
+  *out = g;
+  return GB_OK;
+}
+
+// Fills g (whose buffers hold at least n / m) from the reference's CSR layout.
+static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
+                            const uint32_t* odl, const int32_t* in_array, const uint32_t* idl) {
+  uint32_t* tmp = nullptr;
+  CK(cudaMallocAsync(&tmp, (size_t)(n + 1) * 4, c->stream), "offset staging");
+  gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);
+  if (s == GB_OK) CK(gb::widen_offsets(tmp, g->out_off, (int64_t)n + 1, c->stream), "widen");
+  if (s == GB_OK) s = upload(c, g->out_adj, out_array, (size_t)m * 4);
+  if (s == GB_OK && !g->symmetric) {
+    s = upload(c, tmp, idl, (size_t)(n + 1) * 4);
+    if (s == GB_OK) CK(gb::widen_offsets(tmp, g->in_off, (int64_t)n + 1, c->stream), "widen");
+    if (s == GB_OK) s = upload(c, g->in_adj, in_array, (size_t)m * 4);
+  }
+  cudaFreeAsync(tmp, c->stream);
+  if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
+  if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
+  return s;
+}
+
+gb_status gb_graph_from_csr32(gb_ctx* c, int32_t n, uint32_t m, const int32_t* out_array,
+                              const uint32_t* odl, const int32_t* in_array, const uint32_t* idl,
+                              gb_graph** out) {
+  if (!c || !out || n < 0 || !odl || (m > 0 && !out_array) || ((idl == nullptr) != (in_array == nullptr)))
+    return GB_ERR_INVALID;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  gb_graph* g = new (std::nothrow) gb_graph();
+  if (!g) return GB_ERR_OOM;
+  g->device = c->device;
+  g->n = n;
+  g->m = m;
+  g->symmetric = idl == nullptr;
+  gb_status s = graph_alloc(g, !g->symmetric);
+  if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl);
+  if (s != GB_OK) {
+    graph_free(g);
+    delete g;
+    return s;
+  }
+  *out = g;
+  return GB_OK;
+}
+
+gb_status gb_graph_rmat(gb_ctx* c, int32_t scale, int32_t ef, uint64_t seed, double a, double b,
+                        double cc, gb_graph** out) {
+  if (!c || !out || scale < 1 || scale > 30 || ef < 1) return GB_ERR_INVALID;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  int32_t *s = nullptr, *d = nullptr;
+  int64_t m = 0;
+  CK(gb::rmat_edges_device(scale, ef, seed, gb_rmat_thresholds(a, b, cc), &s, &d, &m, c->stream), "R-MAT");
+  gb_status st = gb_graph_from_edges(c, (int32_t)(1 << scale), m, s, d, out);
+  cudaFreeAsync(s, c->stream);
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return st;
+}
+
+gb_status gb_graph_info(const gb_graph* g, int32_t* n, int64_t* m, int32_t* symmetric) {
+  if (!g) return GB_ERR_INVALID;
+  if (n) *n = g->n;
+  if (m) *m = g->m;
+  if (symmetric) *symmetric = g->symmetric;
+  return GB_OK;
+}
+
+gb_status gb_graph_csr_to_host(const gb_graph* g, int64_t* out_off, int32_t* out_adj,
+                               int64_t* in_off, int32_t* in_adj) {
+  if (!g) return GB_ERR_INVALID;
+  CK(cudaSetDevice(g->device), "cudaSetDevice");
+  if (out_off) CK(cudaMemcpy(out_off, g->out_off, (size_t)(g->n + 1) * 8, cudaMemcpyDeviceToHost), "download");
+  if (out_adj && g->m) CK(cudaMemcpy(out_adj, g->out_adj, (size_t)g->m * 4, cudaMemcpyDeviceToHost), "download");
+  if (!g->symmetric) {
+    if (in_off) CK(cudaMemcpy(in_off, g->in_off, (size_t)(g->n + 1) * 8, cudaMemcpyDeviceToHost), "download");
+    if (in_adj && g->m) CK(cudaMemcpy(in_adj, g->in_adj, (size_t)g->m * 4, cudaMemcpyDeviceToHost), "download");
+  }
+  return GB_OK;
+}
+
+gb_status gb_graph_device_csr(const gb_graph* g, const int64_t** out_off, const int32_t** out_adj,
+                              const int64_t** in_off, const int32_t** in_adj) {
+  if (!g) return GB_ERR_INVALID;
+  if (out_off) *out_off = g->out_off;
+  if (out_adj) *out_adj = g->out_adj;
+  if (in_off) *in_off = g->in_off;
+  if (in_adj) *in_adj = g->in_adj;
+  return GB_OK;
+}
+
+gb_status gb_graph_pivot(gb_ctx* c, const gb_graph* g, int32_t kind, int32_t* pivot, double* avg) {
+  if (!c || !g || !pivot) return GB_ERR_INVALID;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const int64_t* in_off = g->symmetric ? (kind == 0 ? g->out_off : nullptr) : g->in_off;
+  int32_t pv = -1;
+  CK(gb::pivot_device(g->n, g->out_off, in_off, kind, c->stream, &pv), "pivot");
+  *pivot = pv;
+  if (avg) {
+    double deg = (double)g->m;
+    if (kind == 1 && !g->symmetric) deg *= 2.0;  // the mirrored graph has 2m arcs
+    *avg = g->n ? deg / (double)g->n : 0.0;
+  }
+  return GB_OK;
+}
+
+gb_status gb_graph_destroy(gb_graph* g) {
+  if (!g) return GB_OK;
+  cudaSetDevice(g->device);
+  graph_free(g);
+  delete g;
+  return GB_OK;
+}
+
+gb_status gb_scc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
+  return run(c, g, gb::kSCC, labels, o, st, true);
+}
+gb_status gb_wcc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
+  return run(c, g, gb::kWCC, labels, o, st, true);
+}
+gb_status gb_cc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
+  return run(c, g, gb::kWCC, labels, o, st, true);
+}
+gb_status gb_scc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o) {
+  return run(c, g, gb::kSCC, labels, o, nullptr, false);
+}
+gb_status gb_wcc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o) {
+  return run(c, g, gb::kWCC, labels, o, nullptr, false);
+}
+
+// Drop-ins with the reference's signatures: a library-owned context on
+// device 0 and reusable device buffers for the graph.
+static gb_status default_ctx(gb_ctx** c) {
+  if (!g_default_ctx) {
+    gb_status s = gb_ctx_create(0, &g_default_ctx);
+    if (s != GB_OK) return s;
+  }
+  *c = g_default_ctx;
+  return GB_OK;
+}
+
+static gb_status stage_graph(gb_ctx* c, int32_t n, int64_t m, bool symmetric, gb_graph** out) {
+  if (!g_stage || n > g_stage_n || m > g_stage_m || (g_stage->symmetric && !symmetric)) {
+    if (g_stage) {
+      graph_free(g_stage);
+      delete g_stage;
+      g_stage = nullptr;
+    }
+    g_stage = new (std::nothrow) gb_graph();
+    if (!g_stage) return GB_ERR_OOM;
+    g_stage->device = c->device;
+    g_stage->n = n;
+    g_stage->m = m;
+    g_stage->symmetric = symmetric;
+    gb_status s = graph_alloc(g_stage, !symmetric);
+    if (s != GB_OK) {
+      graph_free(g_stage);
+      delete g_stage;
+      g_stage = nullptr;
+      return s;
+    }
+    g_stage_n = n;
+    g_stage_m = m;
+  }
+  g_stage->n = n;
+  g_stage->m = m;
+  g_stage->symmetric = symmetric;
+  *out = g_stage;
+  return GB_OK;
+}
+
+gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_array,
+                     const unsigned* out_degree_list, const unsigned* in_degree_list, int* scc_maps,
+                     int max_deg_vert, double avg_degree, int vert_cutoff) {
+  (void)avg_degree;
+  if (n < 0 || !out_degree_list || !in_degree_list || (m > 0 && (!out_array || !in_array)) ||
+      (n > 0 && !scc_maps))
+    return GB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  gb_ctx* c;
+  gb_status s = default_ctx(&c);
+  if (s != GB_OK) return s;
+  gb_graph* g;
+  if ((s = stage_graph(c, n, m, false, &g)) != GB_OK) return s;
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, in_array, in_degree_list);
+  if (s != GB_OK) return s;
+  gb_opts o;
+  gb_opts_default(&o);
+  o.pivot = max_deg_vert;
+  o.vert_cutoff = vert_cutoff;
+  return gb_scc(c, g, scc_maps, &o, nullptr);
+}
+
+gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out_degree_list,
+                    int* cc_maps, int max_deg_vert, double avg_degree) {
+  (void)avg_degree;
+  if (n < 0 || !out_degree_list || (m > 0 && !out_array) || (n > 0 && !cc_maps)) return GB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  gb_ctx* c;
+  gb_status s = default_ctx(&c);
+  if (s != GB_OK) return s;
+  gb_graph* g;
+  if ((s = stage_graph(c, n, m, true, &g)) != GB_OK) return s;
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr);
+  if (s != GB_OK) return s;
+  gb_opts o;
+  gb_opts_default(&o);
+  o.pivot = max_deg_vert;
+  return gb_wcc(c, g, cc_maps, &o, nullptr);
+}
+
+}  // extern "C"

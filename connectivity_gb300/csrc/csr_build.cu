@@ -1,0 +1,270 @@
+// Device CSR construction (create_csr, multistep/scc_main.cpp:127-191) and the
+// device R-MAT generator.
+//
+// The reference builds its CSR with a serial counting sort that keeps the
+// input order of each vertex's edges.  Here the same order comes from a
+// stable LSD radix sort of (key = endpoint, value = other endpoint) pairs
+// (CUB DeviceRadixSort, a library sort: construction is outside the timed
+// region, as in the reference), followed by an offsets kernel that writes
+// off[v] at every boundary of the sorted keys.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
+
+#include "gb_internal.cuh"
+#include "gen_common.h"
+
+#include <cstring>
+
+namespace gb {
+namespace {
+
+__global__ void k_check_ids(const int32_t* a, const int32_t* b, int64_t m, int32_t n, int* bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t x = a[i], y = b[i];
+    if (x < 0 || x >= n || y < 0 || y >= n) {
+      atomicOr(bad, 1);
+      return;
+    }
+  }
+}
+
+// off[v] = first index i with key[i] >= v, for v in [0, n]; keys sorted.
+__global__ void k_offsets(const uint32_t* key, int64_t m, int32_t n, int64_t* off) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t prev = i == 0 ? -1 : (int64_t)key[i - 1];
+    const int64_t cur = i == m ? (int64_t)n : (int64_t)key[i];
+    for (int64_t v = prev + 1; v <= cur; ++v) off[v] = i;
+  }
+}
+
+__global__ void k_widen(const uint32_t* in, int64_t* out, int64_t count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int64_t)in[i];
+}
+
+__global__ void k_rmat_keys(uint64_t seed, int64_t m0, int scale, gb_rmat_thr thr, uint64_t self,
+                            uint64_t* keys) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m0;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t s, d;
+    gb_rmat_edge(seed, (uint64_t)i, scale, thr, &s, &d);
+    keys[i] = s == d ? self : (((uint64_t)s << scale) | d);
+  }
+}
+
+__global__ void k_split(const uint64_t* keys, int64_t m, int scale, int32_t* src, int32_t* dst) {
+  const uint64_t mask = (1ull << scale) - 1ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    src[i] = (int32_t)(k >> scale);
+    dst[i] = (int32_t)(k & mask);
+  }
+}
+
+__global__ void k_check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* adj, int* bad) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t v = t0; v <= n; v += stride) {
+    const int64_t o = off[v];
+    if ((v == 0 && o != 0) || (v == n && o != m) || (v < n && off[v + 1] < o)) atomicOr(bad, 1);
+  }
+  for (int64_t e = t0; e < m; e += stride) {
+    const int32_t x = adj[e];
+    if (x < 0 || x >= n) atomicOr(bad, 1);
+  }
+}
+
+// Pivot keys: out*in (kind 0) or degree (kind 1).
+__device__ __forceinline__ unsigned long long pivot_key(const int64_t* out_off, const int64_t* in_off,
+                                                        int kind, int64_t v) {
+  const unsigned long long o = (unsigned long long)(out_off[v + 1] - out_off[v]);
+  const unsigned long long i = in_off ? (unsigned long long)(in_off[v + 1] - in_off[v]) : 0ull;
+  return kind == 0 ? o * i : o + i;
+}
+__global__ void k_pivot_max(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,
+                            unsigned long long* best) {
+  unsigned long long k = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long x = pivot_key(out_off, in_off, kind, v);
+    if (x > k) k = x;
+  }
+  if (k) atomicMax(best, k);
+}
+__global__ void k_pivot_min(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,
+                            const unsigned long long* best, int* id) {
+  const unsigned long long b = *best;
+  if (b == 0ull) return;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    if (pivot_key(out_off, in_off, kind, v) == b) {
+      atomicMin(id, (int)v);
+      return;
+    }
+  }
+}
+
+__global__ void k_latch(const Ctl* c, int* sticky) {
+  if (c->err != 0 && sticky[0] == 0) {
+    sticky[0] = c->err;
+    sticky[1] = c->err_where;
+  }
+}
+
+int bits_for(int32_t n) {
+  int b = 1;
+  while (b < 32 && (1ll << b) < (long long)n) ++b;
+  return b;
+}
+
+int grid_for(int64_t work) {
+  int64_t g = (work + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// Sort (key, value) pairs by key (stable) and write CSR offsets + adjacency.
+cudaError_t one_side(int32_t n, int64_t m, const int32_t* key, const int32_t* val, int64_t* off,
+                     int32_t* adj, uint32_t* tmp_keys, cudaStream_t s) {
+  size_t bytes = 0;
+  const int bits = bits_for(n);
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(
+      nullptr, bytes, reinterpret_cast<const uint32_t*>(key), tmp_keys, val, adj, m, 0, bits, s);
+  if (e != cudaSuccess) return e;
+  void* temp = nullptr;
+  e = cudaMallocAsync(&temp, bytes ? bytes : 16, s);
+  if (e != cudaSuccess) return e;
+  e = cub::DeviceRadixSort::SortPairs(temp, bytes, reinterpret_cast<const uint32_t*>(key),
+                                      tmp_keys, val, adj, m, 0, bits, s);
+  cudaFreeAsync(temp, s);
+  if (e != cudaSuccess) return e;
+  k_offsets<<<grid_for(m + 1), 256, 0, s>>>(tmp_keys, m, n, off);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t build_csr(int32_t n, int64_t m, const int32_t* d_src, const int32_t* d_dst,
+                      int64_t* out_off, int32_t* out_adj, int64_t* in_off, int32_t* in_adj,
+                      cudaStream_t s, bool* ids_ok) {
+  *ids_ok = true;
+  int* bad = nullptr;
+  cudaError_t e = cudaMallocAsync(&bad, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (m > 0) k_check_ids<<<grid_for(m), 256, 0, s>>>(d_src, d_dst, m, n, bad);
+  int hbad = 0;
+  cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(bad, s);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  if (hbad) {
+    *ids_ok = false;
+    return cudaSuccess;
+  }
+  uint32_t* tmp = nullptr;
+  e = cudaMallocAsync(&tmp, (size_t)(m > 0 ? m : 1) * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  e = one_side(n, m, d_src, d_dst, out_off, out_adj, tmp, s);
+  if (e == cudaSuccess && in_off != nullptr) e = one_side(n, m, d_dst, d_src, in_off, in_adj, tmp, s);
+  cudaFreeAsync(tmp, s);
+  return e;
+}
+
+cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
+                      cudaStream_t s, int* bad) {
+  int* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(d, 0, sizeof(int), s);
+  k_check_csr<<<grid_for((m > n ? m : n) + 1), 256, 0, s>>>(n, m, off, adj, d);
+  cudaMemcpyAsync(bad, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
+}
+
+cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,
+                         cudaStream_t s, int32_t* pivot) {
+  unsigned long long* best = nullptr;
+  cudaError_t e = cudaMallocAsync(&best, 16, s);
+  if (e != cudaSuccess) return e;
+  int* id = reinterpret_cast<int*>(best + 1);
+  cudaMemsetAsync(best, 0, 8, s);
+  cudaMemsetAsync(id, 0x7f, 4, s);
+  if (n > 0) {
+    k_pivot_max<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, kind, best);
+    k_pivot_min<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, kind, best, id);
+  }
+  unsigned long long hb[2] = {0, 0};
+  cudaMemcpyAsync(hb, best, 16, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(best, s);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  int hid;
+  std::memcpy(&hid, &hb[1], sizeof(int));
+  *pivot = hb[0] == 0ull ? -1 : hid;
+  return cudaSuccess;
+}
+
+cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s) {
+  k_latch<<<1, 1, 0, s>>>(ctl, sticky);
+  return cudaGetLastError();
+}
+
+cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s) {
+  if (count > 0) k_widen<<<grid_for(count), 256, 0, s>>>(in, out, count);
+  return cudaGetLastError();
+}
+
+cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat_thr thr,
+                              int32_t** d_src, int32_t** d_dst, int64_t* m_out, cudaStream_t s) {
+  const int64_t m0 = (int64_t)edge_factor << scale;
+  const uint64_t self = (1ull << (2 * scale)) - 1ull;
+  uint64_t *a = nullptr, *b = nullptr;
+  int64_t* nsel = nullptr;
+  cudaError_t e = cudaMallocAsync(&a, (size_t)m0 * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&b, (size_t)m0 * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&nsel, sizeof(int64_t), s);
+  if (e != cudaSuccess) return e;
+  k_rmat_keys<<<grid_for(m0), 256, 0, s>>>(seed, m0, scale, thr, self, a);
+  size_t bytes = 0, bytes2 = 0;
+  cub::DeviceRadixSort::SortKeys(nullptr, bytes, a, b, m0, 0, 2 * scale, s);
+  cub::DeviceSelect::Unique(nullptr, bytes2, b, a, nsel, m0, s);
+  if (bytes2 > bytes) bytes = bytes2;
+  void* temp = nullptr;
+  e = cudaMallocAsync(&temp, bytes ? bytes : 16, s);
+  if (e == cudaSuccess) e = cub::DeviceRadixSort::SortKeys(temp, bytes, a, b, m0, 0, 2 * scale, s);
+  if (e == cudaSuccess) e = cub::DeviceSelect::Unique(temp, bytes, b, a, nsel, m0, s);
+  cudaFreeAsync(temp, s);
+  int64_t k = 0;
+  uint64_t last = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&k, nsel, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && k > 0) {
+    e = cudaMemcpyAsync(&last, a + (k - 1), 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (last == self) --k;  // only the self-loop key can equal `self`
+  }
+  int32_t *src = nullptr, *dst = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&src, (size_t)(k > 0 ? k : 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dst, (size_t)(k > 0 ? k : 1) * 4, s);
+  if (e == cudaSuccess && k > 0) k_split<<<grid_for(k), 256, 0, s>>>(a, k, scale, src, dst);
+  cudaFreeAsync(a, s);
+  cudaFreeAsync(b, s);
+  cudaFreeAsync(nsel, s);
+  if (e != cudaSuccess) return e;
+  *d_src = src;
+  *d_dst = dst;
+  *m_out = k;
+  return cudaGetLastError();
+}
+
+}  // namespace gb

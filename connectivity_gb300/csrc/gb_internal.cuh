@@ -1,0 +1,161 @@
+// Internal declarations shared by the CUDA translation units of libgbconn:
+// the device control block, tuning parameters, kernel argument structs and
+// the host-side launchers.  Nothing here is part of the C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "gen_common.h"
+
+namespace gb {
+
+constexpr int kBlock = 512;               // threads per block, cooperative kernels
+constexpr int kWarps = kBlock / 32;
+constexpr int kBlkList = 128;             // per-block list of large vertices
+constexpr unsigned kFull = 0xffffffffu;
+
+// Error codes written by kernels; equal to the gb_status values of gbconn.h.
+enum : int {
+  kErrNone = 0,
+  kErrTimeout = 4,     // a grid barrier wait hit its time / spin limit
+  kErrIterLimit = 5,   // a fixed-point loop hit its step cap
+  kErrCapacity = 9,    // an append would overflow its array
+};
+
+struct Csr {
+  const int64_t* off;   // n + 1 offsets
+  const int32_t* adj;   // neighbour ids
+};
+
+// Counters filled during one step and read by every block after the
+// barrier that ends it.  Three slots rotate: step s reads slot s%3, appends
+// into slot (s+1)%3 and clears slot (s+2)%3.
+struct Slot {
+  int32_t count;              // vertices appended to the step's output list
+  int32_t huge;               // heavy vertices deferred to the next step
+  int32_t cand;               // candidates kept by a pull step
+  int32_t pad;
+  unsigned long long edges;   // push-degree sum of the appended vertices
+};
+
+// Statistic slots (64-bit counters, summed over the whole run).
+enum Stat : int {
+  kStVtx = 0,        // vertex offset records read (one per vertex per CSR)
+  kStEdges,          // adjacency entries read
+  kStList,           // list entries read or written (frontiers, candidates)
+  kStTrimSteps,
+  kStFwSteps,
+  kStBwSteps,
+  kStPullSteps,
+  kStColourRounds,
+  kStColourSteps,
+  kStMarkSteps,
+  kStNum = 16
+};
+
+struct Ctl {
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int err;
+  int err_where;
+  int step;               // step counter, continued by each kernel of a run
+  int pad0;
+  Slot ring[3];
+  int32_t pivot;          // FW-BW source (-1: none)
+  int32_t nvalid;         // length of the current valid list
+  int32_t nvisit_fw;      // vertices reached forward
+  int32_t nscc_fwbw;      // vertices labelled by FW-BW
+  int32_t ntrim;          // vertices labelled by trim
+  int32_t ncolour_rounds;
+  int32_t unassigned;
+  int32_t pad;
+  unsigned long long m_cand;   // push-degree sum of the valid list after trim
+  unsigned long long stat[kStNum];
+};
+
+struct Tune {
+  int32_t t_block;        // degree from which a whole block expands a vertex
+  int32_t t_grid;         // degree from which every block takes a slice
+  int32_t k_pull;         // in-edges a thread scans before handing a pull
+                          // candidate to a warp
+  float alpha;            // push -> pull when m_f > m_u / alpha
+  float beta;             // pull -> push when n_f < n_cand / beta
+  int32_t max_steps;      // cap on barrier steps per kernel
+};
+
+// Device workspace of one run (all arrays sized for n vertices).
+struct Work {
+  int32_t n;
+  int32_t nwords;         // (n + 31) / 32
+  int64_t m;
+  int32_t* label;
+  int32_t* colour;        // colours; canonicalisation reuses it
+  int32_t* stamp;
+  int32_t* live_in;
+  int32_t* live_out;
+  uint32_t* vbits;        // valid (unassigned) vertices
+  uint32_t* fvis;         // forward reached
+  uint32_t* bvis;         // backward reached
+  uint32_t* done;         // labelled in the current colour round
+  int32_t* listA;         // valid list
+  int32_t* listB;
+  int32_t* q;             // traversal visit queue
+  int32_t* x0;            // push frontiers
+  int32_t* x1;
+  int32_t* candA;         // pull candidate lists
+  int32_t* candB;
+  int32_t* h0;            // heavy-vertex lists
+  int32_t* h1;
+  int32_t* blk_i;         // per-block scratch (grid size)
+  long long* blk_l;
+  Ctl* ctl;
+};
+
+// One graph as the kernels see it.  `in` is null for a symmetric CSR.
+struct GraphView {
+  int32_t n;
+  int64_t m;
+  Csr out;
+  Csr in;
+};
+
+// Kind of run.
+enum RunKind : int { kSCC = 0, kWCC = 1 };
+
+struct RunParams {
+  int32_t trim_level;     // 1: one pass, 2: fixed point
+  int32_t canonical;      // 1: relabel with the minimum member id
+  int32_t pivot_hint;     // >= 0: use as FW-BW source if still valid
+  Tune tune;
+};
+
+// Host launchers (kernels.cu).  All enqueue on `stream`; none synchronise.
+cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p,
+                       const Work& w, int grid, cudaStream_t stream,
+                       cudaEvent_t* ev /* 5 events or null */);
+int max_coop_grid(int device);   // cooperative grid size for the run kernels
+
+// CSR construction (csr_build.cu).  build_csr sorts device edge arrays into
+// out- and (if in_off != null) in-CSR; *ids_ok = false if an id is outside
+// [0, n) (nothing is built then).  Synchronises the stream.
+cudaError_t build_csr(int32_t n, int64_t m, const int32_t* d_src, const int32_t* d_dst,
+                      int64_t* out_off, int32_t* out_adj, int64_t* in_off, int32_t* in_adj,
+                      cudaStream_t s, bool* ids_ok);
+// Sets *bad when off[0] != 0, off[n] != m, offsets decrease or an id is
+// outside [0, n).  Synchronises the stream.
+cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
+                      cudaStream_t s, int* bad);
+// Reference pivot: kind 0 = lowest id maximising out*in (> 0), kind 1 =
+// lowest id maximising out (+ in when in_off != null).  -1 when none.
+// Synchronises the stream.
+cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,
+                         cudaStream_t s, int32_t* pivot);
+// Copies the first device error of a run into sticky[0..1] (code, site)
+// unless an earlier one is already there.
+cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
+cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
+// Seeded R-MAT edge list on the device, sorted by (src, dst), without
+// self-loops and duplicates; *d_src / *d_dst are cudaMallocAsync'd.
+cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat_thr thr,
+                              int32_t** d_src, int32_t** d_dst, int64_t* m_out, cudaStream_t s);
+
+}  // namespace gb

@@ -1,0 +1,1270 @@
+// Multistep SCC / WCC on one GB300: trim, direction-optimising FW-BW
+// reachability from a pivot, max-colour rounds to a fixed point, and
+// relabelling to each component's minimum vertex id.
+//
+// Each phase is one cooperative persistent kernel (all blocks resident) that
+// runs its whole level loop on the device: a "step" is a grid-strided pass
+// over a frontier or candidate list ended by a bounded grid barrier, and the
+// counters that steer the next step (frontier size, frontier edge count,
+// deferred heavy vertices) rotate through three slots of the control block so
+// that no block reads a counter another block is still writing.  The host
+// never waits between levels.
+//
+// Reference phases (HPCGraphAnalysis/Connectivity, multistep/):
+//   k_trim    scc_trim (scc_trim.cpp:89-139), scc_trim_complete (:141-297),
+//             cc_trim (cc_trim.cpp:47-97), pivot rule of create_csr
+//             (scc_main.cpp:169-182, cc_main.cpp:148-160)
+//   k_reach   scc_fwbw_fw / scc_fwbw_bw / update_valid (scc_fwbw.cpp:47-466),
+//             cc_bfs_search / update_valid (cc_bfs.cpp:47-271)
+//   k_colour  scc_color (scc_color.cpp:47-373) run until no vertex is left,
+//             which replaces the serial Tarjan step (scc_serial.cpp:160-258);
+//             cc_color_propagate (cc_color.cpp:47-175)
+//   k_canon   maps every label to its component's minimum id
+#include "gb_internal.cuh"
+
+namespace gb {
+namespace {
+
+// ------------------------------------------------------------------------
+// Small device helpers
+// ------------------------------------------------------------------------
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_vol(const int* p) { return *(volatile const int*)p; }
+
+__device__ __forceinline__ void set_err(Ctl* c, int code, int where) {
+  if (atomicCAS(&c->err, 0, code) == 0) atomicExch(&c->err_where, where);
+}
+
+// Mutable arrays are read through L2 (ld.global.cg) so that a value written
+// by another block in an earlier step is never served stale from L1.
+__device__ __forceinline__ bool bit_get(const uint32_t* bm, int32_t v) {
+  return (__ldcg(bm + (v >> 5)) >> (v & 31)) & 1u;
+}
+__device__ __forceinline__ bool bit_claim(uint32_t* bm, int32_t v) {
+  const uint32_t b = 1u << (v & 31);
+  return (atomicOr(bm + (v >> 5), b) & b) == 0u;
+}
+__device__ __forceinline__ bool bit_release(uint32_t* bm, int32_t v) {
+  const uint32_t b = 1u << (v & 31);
+  return (atomicAnd(bm + (v >> 5), ~b) & b) != 0u;
+}
+
+__device__ __forceinline__ long long shfl64(long long x, int src) {
+  int lo = __shfl_sync(kFull, (int)(x & 0xffffffffll), src);
+  int hi = __shfl_sync(kFull, (int)(x >> 32), src);
+  return ((long long)hi << 32) | (unsigned)lo;
+}
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long x) {
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+  return x;
+}
+// Exclusive warp prefix sum; `total` receives the warp sum.
+__device__ __forceinline__ int warp_excl(int x, int& total) {
+  int inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, inc, o);
+    if ((int)lane_id() >= o) inc += y;
+  }
+  total = __shfl_sync(kFull, inc, 31);
+  return inc - x;
+}
+
+// Block-wide exclusive prefix sum over kBlock threads; returns the block
+// total in `total`.  Contains __syncthreads.
+__device__ int block_excl(int x, int& total, int* sm_warp /* kWarps + 1 */) {
+  int wt;
+  int ex = warp_excl(x, wt);
+  const int warp = threadIdx.x >> 5;
+  if (lane_id() == 31) sm_warp[warp] = wt;
+  __syncthreads();
+  if (warp == 0) {
+    int v = (int)lane_id() < kWarps ? sm_warp[lane_id()] : 0;
+    int t;
+    int e = warp_excl(v, t);
+    if ((int)lane_id() < kWarps) sm_warp[lane_id()] = e;
+    if (lane_id() == 0) sm_warp[kWarps] = t;
+  }
+  __syncthreads();
+  int r = ex + sm_warp[warp];
+  total = sm_warp[kWarps];
+  __syncthreads();
+  return r;
+}
+
+constexpr unsigned long long kBarrierTimeoutNs = 20ull * 1000ull * 1000ull * 1000ull;
+constexpr unsigned kBarrierMaxSpins = 1u << 28;
+
+// Grid-wide barrier for a cooperative launch.  Every wait is bounded by
+// time and by spin count; on expiry it sets the error flag, and any block
+// that sees the flag leaves its wait.  Returns false when the kernel must
+// stop.
+__device__ bool grid_barrier(Ctl* c, int where) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned gen = ld_acquire(&c->bar_gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&c->bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      st_release(&c->bar_gen, gen + 1u);
+    } else {
+      const uint64_t t0 = gtimer();
+      unsigned spins = 0;
+      while (ld_acquire(&c->bar_gen) == gen) {
+        if (ld_vol(&c->err) != 0) break;
+        __nanosleep(64);
+        ++spins;
+        if (spins >= kBarrierMaxSpins ||
+            ((spins & 1023u) == 0u && gtimer() - t0 > kBarrierTimeoutNs)) {
+          set_err(c, kErrTimeout, where);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ld_vol(&c->err) == 0;
+}
+
+// Step bookkeeping: step s reads ring[s%3], appends into ring[(s+1)%3] and
+// clears ring[(s+2)%3] (read two steps ago, written next step).  The step
+// number persists in the control block across the kernels of one run, so
+// the rotation continues over kernel boundaries.
+struct StepIn {
+  int32_t count, huge, cand;
+  unsigned long long edges;
+};
+__device__ __forceinline__ StepIn step_read(Ctl* c, int step) {
+  const Slot& s = c->ring[step % 3];
+  StepIn r;
+  r.count = __ldcg(&s.count);
+  r.huge = __ldcg(&s.huge);
+  r.cand = __ldcg(&s.cand);
+  r.edges = __ldcg(&s.edges);
+  return r;
+}
+__device__ __forceinline__ void step_begin(Ctl* c, int step) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Slot& s = c->ring[(step + 2) % 3];
+    s.count = 0;
+    s.huge = 0;
+    s.cand = 0;
+    s.edges = 0ull;
+  }
+}
+__device__ __forceinline__ Slot* step_out(Ctl* c, int step) { return &c->ring[(step + 1) % 3]; }
+
+constexpr unsigned long long kKernelTimeLimitNs = 120ull * 1000ull * 1000ull * 1000ull;
+
+// Per-kernel step state: the step counter and the kernel's start time.  A
+// kernel that runs past kKernelTimeLimitNs stops with kErrTimeout.
+struct Steps {
+  int s;
+  int s0;
+  uint64_t t0;
+};
+__device__ __forceinline__ Steps steps_open(Ctl* c) {
+  Steps st;
+  st.s = __ldcg(&c->step);
+  st.s0 = st.s;
+  st.t0 = gtimer();
+  step_begin(c, st.s);
+  return st;
+}
+// End the current step: barrier, next step number, clear the slot ahead.
+__device__ __forceinline__ bool step_sync(Ctl* c, Steps& st, int where) {
+  if (threadIdx.x == 0 && gtimer() - st.t0 > kKernelTimeLimitNs) set_err(c, kErrTimeout, 1000 + where);
+  if (!grid_barrier(c, where)) return false;
+  ++st.s;
+  step_begin(c, st.s);
+  return true;
+}
+__device__ __forceinline__ void steps_close(Ctl* c, const Steps& st) {
+  if (st.s != st.s0 && blockIdx.x == 0 && threadIdx.x == 0) c->step = st.s;
+}
+
+// Per-thread counters of algorithmic traffic, flushed once per kernel.
+struct Tally {
+  unsigned long long vtx = 0, edges = 0, list = 0;
+};
+__device__ void tally_flush(const Tally& t, Ctl* c) {
+  const unsigned long long a = warp_sum64(t.vtx), b = warp_sum64(t.edges), d = warp_sum64(t.list);
+  if (lane_id() == 0) {
+    if (a) atomicAdd(&c->stat[kStVtx], a);
+    if (b) atomicAdd(&c->stat[kStEdges], b);
+    if (d) atomicAdd(&c->stat[kStList], d);
+  }
+}
+__device__ __forceinline__ void stat_inc(Ctl* c, int slot) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->stat[slot], 1ull);
+}
+
+// Exclusive warp prefix sum in 64 bits.
+__device__ __forceinline__ long long warp_excl64(long long x, long long& total) {
+  long long inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = (long long)__shfl_up_sync(kFull, (unsigned long long)inc, o);
+    if ((int)lane_id() >= o) inc += y;
+  }
+  total = (long long)__shfl_sync(kFull, (unsigned long long)inc, 31);
+  return inc - x;
+}
+
+// ------------------------------------------------------------------------
+// Adjacency of a vertex over one or two CSRs (two: the union of out- and
+// in-edges, which is the mirrored graph that cc builds, cc_main.cpp:102-118).
+// ------------------------------------------------------------------------
+struct Adj {
+  Csr c[2];
+  int n;
+};
+__device__ __forceinline__ void rec_load(const Adj& a, int32_t v, long long& s0, long long& d0,
+                                         long long& s1, long long& d1) {
+  s0 = a.c[0].off[v];
+  d0 = a.c[0].off[v + 1] - s0;
+  s1 = 0;
+  d1 = 0;
+  if (a.n > 1) {
+    s1 = a.c[1].off[v];
+    d1 = a.c[1].off[v + 1] - s1;
+  }
+}
+__device__ __forceinline__ int32_t adj_at(const Adj& a, long long s0, long long d0, long long s1,
+                                          long long e, int& k) {
+  if (e < d0) {
+    k = 0;
+    return a.c[0].adj[s0 + e];
+  }
+  k = 1;
+  return a.c[1].adj[s1 + (e - d0)];
+}
+__device__ __forceinline__ unsigned long long adj_degree(const Adj& a, int32_t v) {
+  long long d = a.c[0].off[v + 1] - a.c[0].off[v];
+  if (a.n > 1) d += a.c[1].off[v + 1] - a.c[1].off[v];
+  return (unsigned long long)d;
+}
+__device__ __forceinline__ Adj adj1(Csr x) {
+  Adj a;
+  a.c[0] = x;
+  a.c[1] = x;
+  a.n = 1;
+  return a;
+}
+__device__ __forceinline__ Adj adj2(Csr x, Csr y) {
+  Adj a;
+  a.c[0] = x;
+  a.c[1] = y;
+  a.n = 2;
+  return a;
+}
+// Undirected view: the union of both CSRs of a directed graph, or the single
+// CSR of a symmetric one.
+__device__ __forceinline__ Adj adj_undirected(const GraphView& g) {
+  return g.in.off != nullptr ? adj2(g.out, g.in) : adj1(g.out);
+}
+
+// Output of one expansion step.
+struct Sink {
+  int32_t* arr;               // receives appended vertices at base + slot
+  long long base;
+  long long cap;              // bound on base + slot
+  int32_t* counter;           // Slot::count of the step
+  unsigned long long* edges;  // Slot::edges, or null
+  int32_t* harr;              // heavy list for the next step, or null
+  int32_t hcap;
+  int32_t* hcounter;          // Slot::huge
+};
+__device__ __forceinline__ Sink sink_make(int32_t* arr, long long base, long long cap, Slot* o,
+                                          bool weighted, int32_t* harr, int32_t hcap) {
+  Sink k;
+  k.arr = arr;
+  k.base = base;
+  k.cap = cap;
+  k.counter = &o->count;
+  k.edges = weighted ? &o->edges : nullptr;
+  k.harr = harr;
+  k.hcap = hcap;
+  k.hcounter = &o->huge;
+  return k;
+}
+
+// Warp-aggregated append: one atomic per warp and call.  All 32 lanes call.
+template <class V>
+__device__ __forceinline__ void sink_append(bool app, int32_t w, const Sink& sk, const V& vis,
+                                            Ctl* c) {
+  const unsigned mask = __ballot_sync(kFull, app);
+  if (mask == 0u) return;
+  const int leader = __ffs(mask) - 1;
+  int pos = 0;
+  if ((int)lane_id() == leader) pos = atomicAdd(sk.counter, __popc(mask));
+  pos = __shfl_sync(kFull, pos, leader) + __popc(mask & lanemask_lt());
+  if (app) {
+    const long long at = sk.base + pos;
+    if (at < sk.cap) sk.arr[at] = w;
+    else set_err(c, kErrCapacity, 101);
+  }
+  if (V::kWeighted && sk.edges != nullptr) {
+    unsigned long long wt = app ? vis.weight(w) : 0ull;
+    wt = warp_sum64(wt);
+    if ((int)lane_id() == leader && wt) atomicAdd(sk.edges, wt);
+  }
+}
+
+__device__ __forceinline__ void heavy_append(bool app, int32_t v, const Sink& sk, Ctl* c) {
+  const unsigned mask = __ballot_sync(kFull, app);
+  if (mask == 0u) return;
+  const int leader = __ffs(mask) - 1;
+  int pos = 0;
+  if ((int)lane_id() == leader) pos = atomicAdd(sk.hcounter, __popc(mask));
+  pos = __shfl_sync(kFull, pos, leader) + __popc(mask & lanemask_lt());
+  if (app) {
+    if (pos < sk.hcap) sk.harr[pos] = v;
+    else set_err(c, kErrCapacity, 102);
+  }
+}
+
+// Plain warp-aggregated append into a list with a slot counter.
+__device__ __forceinline__ void list_append(bool app, int32_t v, int32_t* arr, int32_t* counter,
+                                            long long cap, Ctl* c, int where) {
+  const unsigned mask = __ballot_sync(kFull, app);
+  if (mask == 0u) return;
+  const int leader = __ffs(mask) - 1;
+  int pos = 0;
+  if ((int)lane_id() == leader) pos = atomicAdd(counter, __popc(mask));
+  pos = __shfl_sync(kFull, pos, leader) + __popc(mask & lanemask_lt());
+  if (app) {
+    if (pos < cap) arr[pos] = v;
+    else set_err(c, kErrCapacity, where);
+  }
+}
+
+struct BlockList {
+  int cnt;
+  int32_t v[kBlkList];
+  int32_t sval[kBlkList];
+  long long s0[kBlkList];
+  long long d0[kBlkList];
+  long long s1[kBlkList];
+  long long d1[kBlkList];
+};
+
+struct Smem {
+  BlockList bl;
+  int warp_tmp[kWarps + 1];
+  long long red_l[kWarps];
+  int red_i[kWarps];
+};
+
+// ------------------------------------------------------------------------
+// Frontier expansion (push).  Three tiers by degree:
+//   d >= t_grid : deferred to the next step, where every block takes a
+//                 1/grid slice of the vertex's edges;
+//   d >= t_block: the whole block walks the edges (per-block list);
+//   otherwise   : a warp takes 32 vertices, scans their degrees and walks
+//                 the concatenated edge lists 32 edges at a time.
+// The visitor decides per edge whether the far end is appended.
+// ------------------------------------------------------------------------
+template <class V>
+__device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heavy, int32_t nheavy,
+                       const Adj& a, const V& vis, const Sink& sk, const Tune& tn, Smem& sm,
+                       Ctl* c, Tally& ty) {
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  // (1) heavy vertices deferred by the previous step: block b takes slice b
+  for (int j = 0; j < nheavy; ++j) {
+    const int32_t v = __ldcg(heavy + j);
+    long long s0, d0, s1, d1;
+    rec_load(a, v, s0, d0, s1, d1);
+    const long long d = d0 + d1;
+    const long long lo = d * b / G, hi = d * (b + 1) / G;
+    const int32_t sv = vis.source(v);
+    if (t == 0) ty.vtx += a.n;
+    for (long long e0 = lo; e0 < hi; e0 += T) {
+      const long long e = e0 + t;
+      const bool act = e < hi;
+      int32_t w = 0;
+      int k = 0;
+      if (act) {
+        w = adj_at(a, s0, d0, s1, e, k);
+        ty.edges++;
+      }
+      const bool app = vis.edge(sv, w, k, act);
+      sink_append(app, w, sk, vis, c);
+    }
+  }
+  // (2) regular frontier, warp-gathered
+  if (t == 0) sm.bl.cnt = 0;
+  __syncthreads();
+  const int warp = t >> 5, lane = t & 31;
+  const long long nw = (long long)G * (T >> 5);
+  for (long long base = ((long long)b * (T >> 5) + warp) * 32; base < nfront; base += nw * 32) {
+    const long long i = base + lane;
+    int32_t v = -1;
+    long long s0 = 0, d0 = 0, s1 = 0, d1 = 0;
+    if (i < nfront) {
+      v = __ldcg(front + i);
+      rec_load(a, v, s0, d0, s1, d1);
+      ty.list++;
+      ty.vtx += a.n;
+    }
+    const long long d = d0 + d1;
+    const bool to_grid = v >= 0 && d >= tn.t_grid && sk.harr != nullptr;
+    heavy_append(to_grid, v, sk, c);
+    bool to_block = false;
+    if (v >= 0 && !to_grid && d >= tn.t_block) {
+      const int slot = atomicAdd(&sm.bl.cnt, 1);
+      if (slot < kBlkList) {
+        sm.bl.v[slot] = v;
+        sm.bl.sval[slot] = vis.source(v);
+        sm.bl.s0[slot] = s0;
+        sm.bl.d0[slot] = d0;
+        sm.bl.s1[slot] = s1;
+        sm.bl.d1[slot] = d1;
+        to_block = true;
+      }
+    }
+    const long long mine = (v < 0 || to_grid || to_block) ? 0 : d;
+    const int32_t sv = mine ? vis.source(v) : 0;
+    long long tot;
+    const long long ex = warp_excl64(mine, tot);
+    for (long long eb = 0; eb < tot; eb += 32) {
+      const long long e = eb + lane;
+      const bool act = e < tot;
+      int j = 0;
+#pragma unroll
+      for (int st = 16; st; st >>= 1) {
+        const int cnd = j + st;
+        const long long exc = shfl64(ex, cnd);
+        if (exc <= e) j = cnd;
+      }
+      const long long ej = shfl64(ex, j);
+      const int32_t svj = __shfl_sync(kFull, sv, j);
+      const long long s0j = shfl64(s0, j), d0j = shfl64(d0, j), s1j = shfl64(s1, j);
+      int32_t w = 0;
+      int k = 0;
+      if (act) {
+        w = adj_at(a, s0j, d0j, s1j, e - ej, k);
+        ty.edges++;
+      }
+      const bool app = vis.edge(svj, w, k, act);
+      sink_append(app, w, sk, vis, c);
+    }
+  }
+  __syncthreads();
+  // (3) block-expanded vertices
+  const int nb = sm.bl.cnt < kBlkList ? sm.bl.cnt : kBlkList;
+  for (int j = 0; j < nb; ++j) {
+    const int32_t sv = sm.bl.sval[j];
+    const long long s0 = sm.bl.s0[j], d0 = sm.bl.d0[j], s1 = sm.bl.s1[j];
+    const long long d = d0 + sm.bl.d1[j];
+    for (long long e0 = 0; e0 < d; e0 += T) {
+      const long long e = e0 + t;
+      const bool act = e < d;
+      int32_t w = 0;
+      int k = 0;
+      if (act) {
+        w = adj_at(a, s0, d0, s1, e, k);
+        ty.edges++;
+      }
+      const bool app = vis.edge(sv, w, k, act);
+      sink_append(app, w, sk, vis, c);
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------
+// Visitors: edge(source value, far end, which CSR, active) -> append?
+// ------------------------------------------------------------------------
+// Reachability: the far end is taken if allowed and not yet reached.
+struct ReachVisit {
+  static constexpr bool kWeighted = true;
+  const uint32_t* allow;
+  uint32_t* vis;
+  Adj push;
+  __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
+  __device__ __forceinline__ bool edge(int32_t, int32_t w, int, bool act) const {
+    if (!act) return false;
+    if (bit_get(vis, w)) return false;
+    if (!bit_get(allow, w)) return false;
+    return bit_claim(vis, w);
+  }
+  __device__ __forceinline__ unsigned long long weight(int32_t w) const { return adj_degree(push, w); }
+};
+
+// Max-colour push: colour[w] = max(colour[w], colour[v]) over valid w
+// (scc_color.cpp:89-113); a vertex whose colour rose is queued once per step
+// (iteration stamp).
+struct ColourVisit {
+  static constexpr bool kWeighted = false;
+  const uint32_t* valid;
+  int32_t* colour;
+  int32_t* stamp;
+  int32_t iter;
+  __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
+  __device__ __forceinline__ bool edge(int32_t cv, int32_t w, int, bool act) const {
+    if (!act) return false;
+    if (!bit_get(valid, w)) return false;
+    if (__ldcg(colour + w) >= cv) return false;
+    if (atomicMax(colour + w, cv) >= cv) return false;
+    return atomicExch(stamp + w, iter) != iter;
+  }
+  __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
+};
+
+// Backward search inside one colour (scc_color_find_sccs,
+// scc_color.cpp:243-252): a valid in-neighbour with the same colour joins the
+// root's SCC and is labelled with the colour.
+struct MarkVisit {
+  static constexpr bool kWeighted = false;
+  const uint32_t* valid;
+  uint32_t* done;
+  const int32_t* colour;
+  int32_t* label;
+  __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
+  __device__ __forceinline__ bool edge(int32_t cv, int32_t u, int, bool act) const {
+    if (!act) return false;
+    if (!bit_get(valid, u)) return false;
+    if (__ldcg(colour + u) != cv) return false;
+    if (bit_get(done, u)) return false;
+    if (!bit_claim(done, u)) return false;
+    label[u] = cv;
+    return true;
+  }
+  __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
+};
+
+// Fixed-point trim: removing r takes one edge from each neighbour's live
+// count (out-edge r->w: w loses an in-edge; in-edge u->r: u loses an
+// out-edge).  A valid vertex whose count reaches zero is removed and labelled
+// with itself (scc_trim_complete, scc_trim.cpp:205-263).
+struct TrimVisit {
+  static constexpr bool kWeighted = false;
+  uint32_t* valid;
+  int32_t* live_in;
+  int32_t* live_out;
+  int32_t* label;
+  __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
+  __device__ __forceinline__ bool edge(int32_t, int32_t w, int k, bool act) const {
+    if (!act) return false;
+    if (!bit_get(valid, w)) return false;
+    int32_t* ctr = k == 0 ? live_in : live_out;
+    if (atomicSub(ctr + w, 1) != 1) return false;
+    if (!bit_release(valid, w)) return false;
+    label[w] = w;
+    return true;
+  }
+  __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
+};
+
+// ------------------------------------------------------------------------
+// Kernel arguments
+// ------------------------------------------------------------------------
+struct Args {
+  GraphView g;
+  RunParams p;
+  Work w;
+  int kind;
+};
+
+// Ordered compaction: in[0, nin) -> out, keeping the entries whose bit is
+// clear in `drop`, in list order.  Block b owns a contiguous chunk; one
+// barrier between counting and writing.  The survivor count goes to *total.
+__device__ bool compact_ordered(const int32_t* in, int32_t nin, int32_t* out, const uint32_t* drop,
+                                Work& w, Smem& sm, Steps& st, int where, int32_t* total,
+                                Tally& ty) {
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const long long chunk = ((long long)nin + G - 1) / G;
+  const long long lo = chunk * b < nin ? chunk * b : nin;
+  const long long hi = lo + chunk < nin ? lo + chunk : nin;
+  int cnt = 0;
+  for (long long i = lo + t; i < hi; i += T) {
+    if (!bit_get(drop, __ldcg(in + i))) ++cnt;
+    ty.list++;
+  }
+  int tot;
+  block_excl(cnt, tot, sm.warp_tmp);
+  if (t == 0) w.blk_i[b] = tot;
+  if (!step_sync(w.ctl, st, where)) return false;
+  int pre = 0;
+  for (int j = t; j < b; j += T) pre += __ldcg(w.blk_i + j);
+  int boff;
+  block_excl(pre, boff, sm.warp_tmp);
+  if (b == G - 1 && t == 0) *total = boff + tot;
+  int run = boff;
+  for (long long i0 = lo; i0 < hi; i0 += T) {
+    const long long i = i0 + t;
+    int32_t v = -1;
+    bool k = false;
+    if (i < hi) {
+      v = __ldcg(in + i);
+      k = !bit_get(drop, v);
+    }
+    int bt;
+    const int pos = block_excl(k ? 1 : 0, bt, sm.warp_tmp);
+    if (k) {
+      out[run + pos] = v;
+      ty.list++;
+    }
+    run += bt;
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------------
+// k_trim: labels, valid bitmap, valid list (ordered), pivot, m_cand.
+// SCC: a vertex with no out- or no in-edge is its own component
+// (scc_trim, scc_trim.cpp:101-126); level 2 iterates to the fixed point with
+// live degree counters.  WCC: a vertex with no edge at all (cc_trim.cpp:59-
+// 84).  Pivot: SCC lowest id maximising out*in (> 0) (scc_main.cpp:169-182);
+// WCC lowest id of maximum degree in the mirrored graph (cc_main.cpp:148-160).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsigned long long k,
+                                       int32_t v) {
+  return k2 > k || (k2 == k && v2 >= 0 && (v < 0 || v2 < v));
+}
+
+__global__ void __launch_bounds__(kBlock) k_trim(Args A) {
+  __shared__ Smem sm;
+  Work& w = A.w;
+  Ctl* c = w.ctl;
+  const GraphView& g = A.g;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  const bool scc = A.kind == kSCC;
+  const bool level2 = scc && A.p.trim_level >= 2;
+  Tally ty;
+  if (ld_vol(&c->err)) return;
+  Steps st = steps_open(c);
+
+  // Pass 1: warp k of the grid takes the 32-vertex word k.
+  unsigned long long best_key = 0ull;  // out*in (SCC) or degree (WCC)
+  int32_t best_v = -1;
+  unsigned long long mc = 0ull;
+  int removed = 0;
+  TrimVisit tv{w.vbits, w.live_in, w.live_out, w.label};
+  const Sink rsink = sink_make(w.x0, 0, g.n, step_out(c, st.s), false, nullptr, 0);
+  const long long nwarps = (long long)G * (T >> 5);
+  for (long long wd = (long long)b * (T >> 5) + warp; wd < w.nwords; wd += nwarps) {
+    const long long vv = wd * 32 + lane;
+    bool keep = false, gone = false;
+    if (vv < g.n) {
+      const int32_t v = (int32_t)vv;
+      const long long dout = g.out.off[v + 1] - g.out.off[v];
+      long long din = 0;
+      if (g.in.off != nullptr) din = g.in.off[v + 1] - g.in.off[v];
+      ty.vtx += g.in.off != nullptr ? 2 : 1;
+      if (scc) {
+        keep = dout > 0 && din > 0;
+        if (keep) {
+          const unsigned long long prod = (unsigned long long)dout * (unsigned long long)din;
+          if (prod > best_key) { best_key = prod; best_v = v; }
+          mc += (unsigned long long)dout;
+        }
+      } else {
+        const long long deg = dout + din;
+        keep = deg > 0;
+        if (keep) {
+          if ((unsigned long long)deg > best_key) { best_key = (unsigned long long)deg; best_v = v; }
+          mc += (unsigned long long)deg;
+        }
+      }
+      gone = !keep;
+      w.label[v] = keep ? -1 : v;
+      if (level2) {
+        w.live_out[v] = (int32_t)(dout < 0x7fffffffll ? dout : 0x7fffffffll);
+        w.live_in[v] = (int32_t)(din < 0x7fffffffll ? din : 0x7fffffffll);
+      }
+      if (gone) ++removed;
+    }
+    const unsigned bits = __ballot_sync(kFull, keep);
+    if (lane == 0) w.vbits[wd] = bits;
+    if (level2) sink_append(gone, (int32_t)vv, rsink, tv, c);
+  }
+  {
+    unsigned long long k = best_key;
+    int32_t v = best_v;
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long k2 = __shfl_xor_sync(kFull, k, o);
+      const int32_t v2 = __shfl_xor_sync(kFull, v, o);
+      if (better(k2, v2, k, v)) { k = k2; v = v2; }
+    }
+    if (lane == 0) { sm.red_l[warp] = (long long)k; sm.red_i[warp] = v; }
+    const unsigned long long msum = warp_sum64(mc);
+    int rsum = removed;
+    for (int o = 16; o; o >>= 1) rsum += __shfl_xor_sync(kFull, rsum, o);
+    if (lane == 0) {
+      if (msum) atomicAdd(&c->m_cand, msum);
+      if (rsum) atomicAdd(&c->ntrim, rsum);
+    }
+    __syncthreads();
+    if (t == 0) {
+      unsigned long long bk = 0ull;
+      int32_t bv = -1;
+      for (int i = 0; i < kWarps; ++i) {
+        if (better((unsigned long long)sm.red_l[i], sm.red_i[i], bk, bv)) {
+          bk = (unsigned long long)sm.red_l[i];
+          bv = sm.red_i[i];
+        }
+      }
+      w.blk_l[b] = (long long)bk;
+      w.blk_i[b] = bv;
+    }
+  }
+  if (!step_sync(c, st, 1)) return;
+  if (b == 0 && t == 0) {
+    unsigned long long bk = 0ull;
+    int32_t bv = -1;
+    for (int i = 0; i < G; ++i) {
+      const unsigned long long k2 = (unsigned long long)__ldcg(w.blk_l + i);
+      const int32_t v2 = __ldcg(w.blk_i + i);
+      if (better(k2, v2, bk, bv)) { bk = k2; bv = v2; }
+    }
+    c->pivot = bk > 0ull ? bv : -1;
+  }
+
+  // Level 2: propagate removals to the fixed point.
+  if (level2) {
+    const Adj both = adj2(g.out, g.in);
+    int32_t* bufs[2] = {w.x0, w.x1};
+    int cur = 0;
+    for (;;) {
+      if (st.s - st.s0 >= A.p.tune.max_steps) { set_err(c, kErrIterLimit, 2); return; }
+      const StepIn in = step_read(c, st.s);
+      if (in.count == 0) break;
+      const Sink sk = sink_make(bufs[cur ^ 1], 0, g.n, step_out(c, st.s), false, nullptr, 0);
+      expand(bufs[cur], in.count, nullptr, 0, both, tv, sk, A.p.tune, sm, c, ty);
+      stat_inc(c, kStTrimSteps);
+      if (!step_sync(c, st, 3)) return;
+      cur ^= 1;
+    }
+  }
+
+  // Ordered valid list from the bitmap: block b owns a contiguous word range.
+  {
+    const long long chunk = ((long long)w.nwords + G - 1) / G;
+    const long long lo = chunk * b < w.nwords ? chunk * b : w.nwords;
+    const long long hi = lo + chunk < w.nwords ? lo + chunk : w.nwords;
+    int cnt = 0;
+    for (long long wd = lo + t; wd < hi; wd += T) cnt += __popc(__ldcg(w.vbits + wd));
+    int tot;
+    block_excl(cnt, tot, sm.warp_tmp);
+    if (t == 0) w.blk_i[b] = tot;
+    if (!step_sync(c, st, 4)) return;
+    int pre = 0;
+    for (int j = t; j < b; j += T) pre += __ldcg(w.blk_i + j);
+    int boff;
+    block_excl(pre, boff, sm.warp_tmp);
+    if (b == G - 1 && t == 0) {
+      c->nvalid = boff + tot;
+      if (level2) c->ntrim = g.n - (boff + tot);
+    }
+    int run = boff;
+    for (long long wd0 = lo; wd0 < hi; wd0 += T) {
+      const long long wd = wd0 + t;
+      const unsigned bits = wd < hi ? __ldcg(w.vbits + wd) : 0u;
+      int bt;
+      const int pos = block_excl(__popc(bits), bt, sm.warp_tmp);
+      unsigned x = bits;
+      int o = run + pos;
+      while (x) {
+        const int bit = __ffs(x) - 1;
+        x &= x - 1;
+        w.listA[o++] = (int32_t)(wd * 32 + bit);
+      }
+      ty.list += __popc(bits);
+      run += bt;
+    }
+  }
+  if (!step_sync(c, st, 5)) return;
+  // A hint replaces the pivot; level 2 may have trimmed the pivot, in which
+  // case FW-BW is skipped and the colour rounds label what is left.
+  if (b == 0 && t == 0) {
+    int32_t pv = c->pivot;
+    if (A.p.pivot_hint >= 0 && A.p.pivot_hint < g.n) pv = A.p.pivot_hint;
+    if (pv >= 0 && !bit_get(w.vbits, pv)) pv = -1;
+    c->pivot = pv;
+  }
+  tally_flush(ty, c);
+  steps_close(c, st);
+}
+
+// ------------------------------------------------------------------------
+// Direction-optimising reachability from `root`, run by the whole grid.
+// Push steps expand the frontier (the vertices appended by the previous
+// step) with ReachVisit; pull steps let every unreached candidate scan its
+// pull adjacency for a reached vertex and stop at the first
+// (scc_fwbw.cpp:116-149).  Push -> pull when the frontier's edge count times
+// alpha exceeds the unvisited edge estimate; pull -> push when the frontier
+// has fewer than ncand / beta vertices.  q receives every reached vertex
+// exactly once, so q[0, result) is the reached set.  Returns -1 on error.
+// ------------------------------------------------------------------------
+struct ReachSpec {
+  Adj push, pull;
+  const uint32_t* allow;
+  uint32_t* vis;
+  const int32_t* cand;
+  int32_t ncand;
+  unsigned long long m_cand;
+  int32_t root;
+  int32_t* q;
+  int stat_slot;
+};
+
+__device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps& st, Tally& ty) {
+  Ctl* c = w.ctl;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  const Tune& tn = A.p.tune;
+  const ReachVisit rv{R.allow, R.vis, R.push};
+  if (b == 0 && t == 0) {
+    if (bit_claim(R.vis, R.root)) {
+      R.q[0] = R.root;
+      Slot* o = step_out(c, st.s);
+      o->count = 1;
+      o->edges = adj_degree(R.push, R.root);
+    }
+  }
+  if (!step_sync(c, st, 20)) return -1;
+  long long qlo = 0, qhi = 0;
+  bool pull = false, prev_pull = false;
+  unsigned long long edges_seen = 0ull;
+  const int32_t* cand_cur = R.cand;
+  int32_t ncur = R.ncand;
+  int32_t* cand_next = w.candA;
+  int hsel = 0;
+  int32_t* hl[2] = {w.h0, w.h1};
+  const int s_start = st.s;
+  for (;;) {
+    if (st.s - s_start >= tn.max_steps) { set_err(c, kErrIterLimit, 21); return -1; }
+    const StepIn in = step_read(c, st.s);
+    qlo = qhi;
+    qhi = qlo + in.count;
+    edges_seen += in.edges;
+    if (prev_pull) {
+      cand_cur = cand_next;
+      ncur = in.cand;
+      cand_next = (cand_next == w.candA) ? w.candB : w.candA;
+    }
+    if (!pull) {
+      const unsigned long long mu = R.m_cand > edges_seen ? R.m_cand - edges_seen : 0ull;
+      if ((double)in.edges * (double)tn.alpha > (double)mu) pull = true;
+    } else if ((double)in.count * (double)tn.beta < (double)R.ncand) {
+      pull = false;
+    }
+    if (in.count == 0 && (pull || in.huge == 0)) break;
+    Slot* o = step_out(c, st.s);
+    const Sink sk = sink_make(R.q, qhi, w.n, o, true, hl[hsel ^ 1], w.n);
+    if (!pull) {
+      expand(R.q + qlo, (int32_t)(qhi - qlo), hl[hsel], in.huge, R.push, rv, sk, tn, sm, c, ty);
+      prev_pull = false;
+    } else {
+      // every unreached candidate looks for a reached pull-neighbour; the
+      // still-unreached ones are kept (any order) for the next pull step
+      if (t == 0) sm.bl.cnt = 0;
+      __syncthreads();
+      const long long nw = (long long)G * (T >> 5);
+      for (long long base = ((long long)b * (T >> 5) + warp) * 32; base < ncur; base += nw * 32) {
+        const long long i = base + lane;
+        int32_t v = -1;
+        bool found = false, keep = false;
+        if (i < ncur) {
+          v = __ldcg(cand_cur + i);
+          ty.list++;
+          if (!bit_get(R.vis, v)) {
+            long long s0, d0, s1, d1;
+            rec_load(R.pull, v, s0, d0, s1, d1);
+            ty.vtx += R.pull.n;
+            const long long d = d0 + d1;
+            const long long lim = d < tn.k_pull ? d : tn.k_pull;
+            for (long long e = 0; e < lim; ++e) {
+              int k;
+              const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
+              ty.edges++;
+              if (bit_get(R.vis, u)) { found = true; break; }
+            }
+            if (!found && d > lim) {
+              const int slot = atomicAdd(&sm.bl.cnt, 1);
+              if (slot < kBlkList) {
+                sm.bl.v[slot] = v;
+                sm.bl.s0[slot] = s0;
+                sm.bl.d0[slot] = d0;
+                sm.bl.s1[slot] = s1;
+                sm.bl.d1[slot] = d1;
+              } else {
+                for (long long e = lim; e < d; ++e) {
+                  int k;
+                  const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
+                  ty.edges++;
+                  if (bit_get(R.vis, u)) { found = true; break; }
+                }
+                keep = !found;
+              }
+            } else if (!found) {
+              keep = true;
+            }
+          }
+        }
+        if (found) found = bit_claim(R.vis, v);
+        sink_append(found, v, sk, rv, c);
+        list_append(keep, v, cand_next, &o->cand, w.n, c, 22);
+        if (keep) ty.list++;
+      }
+      __syncthreads();
+      // candidates with long pull lists: one warp each, 32 edges at a time
+      const int nb = sm.bl.cnt < kBlkList ? sm.bl.cnt : kBlkList;
+      for (int j = warp; j < nb; j += kWarps) {
+        const int32_t v = sm.bl.v[j];
+        const long long s0 = sm.bl.s0[j], d0 = sm.bl.d0[j], s1 = sm.bl.s1[j];
+        const long long d = d0 + sm.bl.d1[j];
+        bool found = false;
+        for (long long e0 = tn.k_pull; e0 < d; e0 += 32) {
+          const long long e = e0 + lane;
+          bool hit = false;
+          if (e < d) {
+            int k;
+            const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
+            ty.edges++;
+            hit = bit_get(R.vis, u);
+          }
+          if (__any_sync(kFull, hit)) { found = true; break; }
+        }
+        const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
+        sink_append(f, v, sk, rv, c);
+        list_append(!found && lane == 0, v, cand_next, &o->cand, w.n, c, 23);
+      }
+      __syncthreads();
+      prev_pull = true;
+      stat_inc(c, kStPullSteps);
+    }
+    stat_inc(c, R.stat_slot);
+    if (!step_sync(c, st, 24)) return -1;
+    hsel ^= 1;
+  }
+  return (int)qhi;
+}
+
+// ------------------------------------------------------------------------
+// k_reach: SCC -> forward and backward reachability from the pivot; the SCC
+// (reached both ways) takes the pivot as label and leaves the valid list
+// (scc_fwbw, scc_fwbw.cpp:469-513).  WCC -> one search over the union
+// adjacency (cc_bfs, cc_bfs.cpp:273-291).
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_reach(Args A) {
+  __shared__ Smem sm;
+  Work& w = A.w;
+  Ctl* c = w.ctl;
+  const GraphView& g = A.g;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  Tally ty;
+  if (ld_vol(&c->err)) return;
+  const int32_t pivot = __ldcg(&c->pivot);
+  const int32_t nvalid = __ldcg(&c->nvalid);
+  if (pivot < 0 || nvalid == 0) return;
+  Steps st = steps_open(c);
+  const bool scc = A.kind == kSCC;
+  const uint32_t* hit;
+  ReachSpec F;
+  F.push = scc ? adj1(g.out) : adj_undirected(g);
+  F.pull = scc ? adj1(g.in) : F.push;
+  F.allow = w.vbits;
+  F.vis = w.fvis;
+  F.cand = w.listA;
+  F.ncand = nvalid;
+  F.m_cand = __ldcg(&c->m_cand);
+  F.root = pivot;
+  F.q = w.q;
+  F.stat_slot = kStFwSteps;
+  const int nf = reach(F, A, w, sm, st, ty);
+  if (nf < 0) return;
+  if (b == 0 && t == 0) c->nvisit_fw = nf;
+  if (scc) {
+    // backward inside the forward set; its candidates are the forward set
+    ReachSpec B;
+    B.push = adj1(g.in);
+    B.pull = adj1(g.out);
+    B.allow = w.fvis;
+    B.vis = w.bvis;
+    B.cand = w.q;
+    B.ncand = nf;
+    B.m_cand = F.m_cand;
+    B.root = pivot;
+    B.q = w.x0;
+    B.stat_slot = kStBwSteps;
+    const int nb = reach(B, A, w, sm, st, ty);
+    if (nb < 0) return;
+    if (b == 0 && t == 0) c->nscc_fwbw = nb;
+    hit = w.bvis;
+  } else {
+    if (b == 0 && t == 0) c->nscc_fwbw = nf;
+    hit = w.fvis;
+  }
+  // label the component and take it out of the valid set (update_valid,
+  // scc_fwbw.cpp:425-433)
+  for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
+    const uint32_t h = __ldcg(hit + wd);
+    if (h) {
+      w.vbits[wd] = __ldcg(w.vbits + wd) & ~h;
+      unsigned x = h;
+      while (x) {
+        const int bit = __ffs(x) - 1;
+        x &= x - 1;
+        w.label[wd * 32 + bit] = pivot;
+      }
+    }
+  }
+  if (!compact_ordered(w.listA, nvalid, w.listB, hit, w, sm, st, 26, &c->nvalid, ty)) return;
+  if (!step_sync(c, st, 27)) return;
+  const int32_t nv = __ldcg(&c->nvalid);
+  for (long long i = (long long)b * T + t; i < nv; i += (long long)G * T) w.listA[i] = __ldcg(w.listB + i);
+  tally_flush(ty, c);
+  steps_close(c, st);
+}
+
+// ------------------------------------------------------------------------
+// k_colour: rounds of max-colour propagation until no vertex is left.
+// SCC: each round propagates colours along out-edges to the fixed point;
+// every vertex whose colour is its own id is a root; a backward search over
+// same-colour vertices labels the root's SCC with the colour; the rest stay
+// for the next round (scc_color, scc_color.cpp:340-373).  The reference
+// hands the last <= vert_cutoff vertices to serial Tarjan; here the rounds
+// simply continue to the end.  WCC: one propagation over the union
+// adjacency; every vertex takes its colour (its component's largest id) as
+// label (cc_color_propagate, cc_color.cpp:47-175).
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_colour(Args A) {
+  __shared__ Smem sm;
+  Work& w = A.w;
+  Ctl* c = w.ctl;
+  const GraphView& g = A.g;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const long long gt = (long long)b * T + t, gstride = (long long)G * T;
+  Tally ty;
+  if (ld_vol(&c->err)) return;
+  int32_t nl = __ldcg(&c->nvalid);
+  if (nl == 0) return;
+  Steps st = steps_open(c);
+  const bool scc = A.kind == kSCC;
+  const Adj prop = scc ? adj1(g.out) : adj_undirected(g);
+  const Adj back = adj1(g.in);
+  int32_t* L = w.listA;
+  int32_t* L2 = w.listB;
+  int32_t iter = 0;
+  int rounds = 0;
+  int32_t* bufs[2] = {w.x0, w.x1};
+  int32_t* hl[2] = {w.h0, w.h1};
+  const Tune& tn = A.p.tune;
+  while (nl > 0) {
+    if (rounds > g.n || st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 30); return; }
+    for (long long i = gt; i < nl; i += gstride) {
+      const int32_t v = __ldcg(L + i);
+      w.colour[v] = v;
+      ty.list++;
+    }
+    if (!step_sync(c, st, 31)) return;
+    // propagation; the first step pushes from every vertex of L
+    {
+      const int32_t* front = L;
+      int32_t nfront = nl, nheavy = 0;
+      int cur = 0, hs = 0;
+      for (;;) {
+        if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 32); return; }
+        const ColourVisit cv{w.vbits, w.colour, w.stamp, iter++};
+        const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, hl[hs ^ 1], w.n);
+        expand(front, nfront, hl[hs], nheavy, prop, cv, sk, tn, sm, c, ty);
+        stat_inc(c, kStColourSteps);
+        if (!step_sync(c, st, 33)) return;
+        const StepIn in = step_read(c, st.s);
+        if (in.count == 0 && in.huge == 0) break;
+        front = bufs[cur];
+        nfront = in.count;
+        nheavy = in.huge;
+        cur ^= 1;
+        hs ^= 1;
+      }
+    }
+    if (!scc) {
+      for (long long i = gt; i < nl; i += gstride) {
+        const int32_t v = __ldcg(L + i);
+        w.label[v] = __ldcg(w.colour + v);
+      }
+      nl = 0;
+      ++rounds;
+      break;
+    }
+    // roots: colour == own id (scc_color_get_roots, scc_color.cpp:179-201)
+    const MarkVisit mv{w.vbits, w.done, w.colour, w.label};
+    {
+      const Sink sk = sink_make(bufs[0], 0, w.n, step_out(c, st.s), false, nullptr, 0);
+      for (long long base = gt - (t & 31); base < nl; base += gstride) {
+        const long long i = base + (t & 31);
+        bool root = false;
+        int32_t v = 0;
+        if (i < nl) {
+          v = __ldcg(L + i);
+          if (__ldcg(w.colour + v) == v && bit_claim(w.done, v)) {
+            w.label[v] = v;
+            root = true;
+          }
+        }
+        sink_append(root, v, sk, mv, c);
+      }
+      if (!step_sync(c, st, 34)) return;
+    }
+    // backward same-colour search from the roots
+    {
+      int cur = 0, hs = 0;
+      for (;;) {
+        if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 35); return; }
+        const StepIn in = step_read(c, st.s);
+        if (in.count == 0 && in.huge == 0) break;
+        const Sink sk = sink_make(bufs[cur ^ 1], 0, w.n, step_out(c, st.s), false, hl[hs ^ 1], w.n);
+        expand(bufs[cur], in.count, hl[hs], in.huge, back, mv, sk, tn, sm, c, ty);
+        stat_inc(c, kStMarkSteps);
+        if (!step_sync(c, st, 36)) return;
+        cur ^= 1;
+        hs ^= 1;
+      }
+    }
+    // the labelled vertices leave the valid set; L is compacted into L2
+    for (long long i = gt; i < nl; i += gstride) {
+      const int32_t v = __ldcg(L + i);
+      if (bit_get(w.done, v)) bit_release(w.vbits, v);
+    }
+    if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 37, &c->nvalid, ty)) return;
+    if (!step_sync(c, st, 38)) return;
+    nl = __ldcg(&c->nvalid);
+    int32_t* tmp = L;
+    L = L2;
+    L2 = tmp;
+    ++rounds;
+    stat_inc(c, kStColourRounds);
+  }
+  if (b == 0 && t == 0) c->ncolour_rounds = rounds;
+  tally_flush(ty, c);
+  steps_close(c, st);
+}
+
+// ------------------------------------------------------------------------
+// k_canon: label[v] <- min { u : label[u] == label[v] }.  rep[r] starts at r
+// (every representative is a member of its own component) and takes an
+// atomicMin from each member.  Also counts unassigned vertices.
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_canon(Args A) {
+  Work& w = A.w;
+  Ctl* c = w.ctl;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const long long gt = (long long)b * T + t, gs = (long long)G * T;
+  const int32_t n = A.g.n;
+  if (ld_vol(&c->err)) return;
+  Steps st = steps_open(c);
+  int32_t* rep = w.colour;
+  for (long long v = gt; v < n; v += gs) rep[v] = (int32_t)v;
+  if (!step_sync(c, st, 40)) return;
+  int un = 0;
+  for (long long v = gt; v < n; v += gs) {
+    const int32_t l = __ldcg(w.label + v);
+    if (l >= 0 && l < n) {
+      if (l != v) atomicMin(rep + l, (int32_t)v);
+    } else {
+      ++un;
+    }
+  }
+  for (int o = 16; o; o >>= 1) un += __shfl_xor_sync(kFull, un, o);
+  if (lane_id() == 0 && un) atomicAdd(&c->unassigned, un);
+  if (!step_sync(c, st, 41)) return;
+  for (long long v = gt; v < n; v += gs) {
+    const int32_t l = __ldcg(w.label + v);
+    if (l >= 0 && l < n) w.label[v] = __ldcg(rep + l);
+  }
+  steps_close(c, st);
+}
+
+// Unassigned count only (labels kept as produced).
+__global__ void k_count_unassigned(Args A) {
+  Work& w = A.w;
+  const int32_t n = A.g.n;
+  int un = 0;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int32_t l = w.label[v];
+    if (l < 0 || l >= n) ++un;
+  }
+  for (int o = 16; o; o >>= 1) un += __shfl_xor_sync(kFull, un, o);
+  if (lane_id() == 0 && un) atomicAdd(&w.ctl->unassigned, un);
+}
+
+template <class K>
+cudaError_t coop(K kern, int grid, const Args& a, cudaStream_t s) {
+  void* params[] = {const_cast<Args*>(&a)};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kBlock), params, 0, s);
+}
+
+}  // namespace
+
+int max_coop_grid(int device) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+  int best = 1 << 30;
+  const void* ks[] = {(const void*)k_trim, (const void*)k_reach, (const void*)k_colour,
+                      (const void*)k_canon};
+  for (const void* k : ks) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, 0) != cudaSuccess) return 0;
+    if (per < best) best = per;
+  }
+  if (best < 1) return 0;
+  return best * sms;
+}
+
+cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p, const Work& w,
+                       int grid, cudaStream_t stream, cudaEvent_t* ev) {
+  Args a;
+  a.g = g;
+  a.p = p;
+  a.w = w;
+  a.kind = kind;
+  cudaError_t e;
+  if (ev) cudaEventRecord(ev[0], stream);
+  e = coop(k_trim, grid, a, stream);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[1], stream);
+  e = coop(k_reach, grid, a, stream);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[2], stream);
+  e = coop(k_colour, grid, a, stream);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[3], stream);
+  if (p.canonical) {
+    e = coop(k_canon, grid, a, stream);
+  } else {
+    k_count_unassigned<<<grid, kBlock, 0, stream>>>(a);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[4], stream);
+  return cudaSuccess;
+}
+
+}  // namespace gb

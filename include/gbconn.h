@@ -1,0 +1,229 @@
+/*
+ * gbconn.h -- C ABI of libgbconn, a GB300 (sm_103a) implementation of the
+ * Multistep connectivity pipeline (trim, forward/backward reachability from a
+ * max in-degree x out-degree pivot, colour propagation, cleanup) for strongly,
+ * weakly and plain connected components.
+ *
+ * It is a drop-in for the OpenMP Multistep code of HPCGraphAnalysis/
+ * Connectivity (multistep/).  That code has no library API: its surface is
+ * the two executables and the functions inside their translation units.  Each
+ * entry point below names the reference function it replaces (path:line in
+ * that project).
+ *
+ * Conventions
+ *   - Every function returns a gb_status; nothing calls exit().  The reference
+ *     has no error reporting (bad ids, missing files and zero-edge graphs are
+ *     undefined behaviour there); here they are GB_ERR_INVALID / GB_ERR_IO.
+ *   - Vertex ids are int32 in [0, n); edge counts and offsets are int64.
+ *   - Label arrays hold n int32 and are owned by the caller.  They may be host
+ *     or device (cudaMalloc) memory; the library detects which.
+ *   - Labels come back in canonical form by default: every vertex is labelled
+ *     with the smallest vertex id of its component.  The reference labels a
+ *     component with whichever member the phase that found it used (trim: the
+ *     vertex; FW-BW: the pivot; colour: the largest id; Tarjan: the DFS root,
+ *     which depends on thread timing); the partition is the same, and the
+ *     verify lines, which only count, are byte-identical.
+ *   - A gb_ctx owns one CUDA stream and the device workspace; calls on one
+ *     context are serialised by the caller, calls on different contexts may
+ *     run concurrently.  No CPU fallback exists: without a usable GB300 the
+ *     compute calls return GB_ERR_NO_DEVICE or GB_ERR_CUDA.
+ */
+#ifndef GBCONN_H
+#define GBCONN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t gb_status;
+#define GB_OK 0
+#define GB_ERR_INVALID 1     /* bad argument: null pointer, negative size, id out of range */
+#define GB_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define GB_ERR_OOM 3         /* a device or pinned allocation failed */
+#define GB_ERR_TIMEOUT 4     /* a device-side wait or a kernel hit its time limit */
+#define GB_ERR_ITER_LIMIT 5  /* a fixed-point loop hit its step cap */
+#define GB_ERR_IO 6          /* a file could not be opened, read, parsed or written */
+#define GB_ERR_NO_DEVICE 7   /* no CUDA device */
+#define GB_ERR_UNSUPPORTED 8 /* device is not sm_103 or lacks cooperative launch */
+#define GB_ERR_CAPACITY 9    /* a size exceeds a fixed maximum */
+
+/* Human-readable name of a status, and the detail of the last failure on
+ * the calling thread. */
+const char* gb_status_string(gb_status s);
+const char* gb_last_error(void);
+
+typedef struct gb_ctx gb_ctx;     /* stream + device workspace */
+typedef struct gb_graph gb_graph; /* device-resident out- and in-CSR */
+
+/* Run options.  gb_opts_default fills the defaults noted per field. */
+typedef struct gb_opts {
+  int32_t trim_level;  /* 1: one pass (reference default, TRIM_LEVEL 1 at
+                          multistep/scc_main.cpp:61, scc_trim.cpp:89-139);
+                          2: iterate to the fixed point (scc_trim_complete,
+                          scc_trim.cpp:141-297).  Default 1. SCC only. */
+  int32_t canonical;   /* 1: minimum-member labels (default); 0: labels as
+                          the phases produce them */
+  int32_t pivot;       /* -1 (default): the reference rule, lowest id of
+                          maximum out*in (SCC) or degree (WCC); >= 0: that
+                          vertex, if it survives trim */
+  int32_t vert_cutoff; /* accepted for run_scc parity (scc_main.cpp:336);
+                          the device colours every remaining vertex */
+  int32_t t_block;     /* degree from which a block expands one vertex (512) */
+  int32_t t_grid;      /* degree from which all blocks share one vertex (32768) */
+  int32_t k_pull;      /* in-edges one thread scans in a pull step (8) */
+  float alpha;         /* push -> pull when frontier edges * alpha > unvisited
+                          edges (15, the reference's ALPHA scc_main.cpp:64) */
+  float beta;          /* pull -> push when frontier * beta < candidates
+                          (25, the reference's BETA scc_main.cpp:65) */
+  int32_t max_steps;   /* cap on device steps per phase (1 << 30) */
+  int32_t grid_blocks; /* 0: all resident blocks; else a smaller grid */
+} gb_opts;
+
+void gb_opts_default(gb_opts* o);
+
+/* Per-run results.  Times are device times between CUDA events on the
+ * context stream, in milliseconds. */
+typedef struct gb_stats {
+  double ms_trim, ms_reach, ms_colour, ms_canon, ms_total;
+  int32_t pivot;          /* FW-BW source, -1 if none */
+  int32_t colour_rounds;
+  int64_t n_trim;         /* vertices labelled by trim */
+  int64_t n_visit_fw;     /* vertices reached forward from the pivot */
+  int64_t n_fwbw;         /* vertices labelled by FW-BW */
+  int64_t unassigned;     /* labels < 0 after the run (0 when correct) */
+  int64_t vtx_reads;      /* vertex offset records read (8 B x 2 each) */
+  int64_t edge_reads;     /* adjacency entries read (4 B each) */
+  int64_t list_rw;        /* list entries read or written (4 B each) */
+  int64_t trim_steps, fw_steps, bw_steps, pull_steps, colour_steps, mark_steps;
+  int32_t grid_blocks;
+  int32_t err_where;      /* device location code of a failure, 0 if none */
+} gb_stats;
+
+/* ---- contexts --------------------------------------------------------- */
+gb_status gb_ctx_create(int device, gb_ctx** ctx);
+gb_status gb_ctx_destroy(gb_ctx* ctx);
+/* Use an existing cudaStream_t (e.g. a framework's current stream) for all
+ * work of this context; NULL restores the context's own stream. */
+gb_status gb_ctx_set_stream(gb_ctx* ctx, void* cuda_stream);
+void* gb_ctx_stream(gb_ctx* ctx);
+/* Wait for all work queued on the context; returns the first device error
+ * raised by any run since the last wait. */
+gb_status gb_ctx_sync(gb_ctx* ctx);
+
+/* ---- graphs: create_csr (multistep/scc_main.cpp:127-191) --------------- */
+/* Device CSR build from an edge list (host or device arrays, m entries
+ * each): out- and in-CSR by stable radix sort on the device, adjacency in
+ * input order within a vertex as in the reference's counting sort. */
+gb_status gb_graph_from_edges(gb_ctx* ctx, int32_t n, int64_t m, const int32_t* src,
+                              const int32_t* dst, gb_graph** g);
+/* From CSR arrays (host or device).  in_off/in_adj may be NULL for a
+ * symmetric graph (the mirrored CSR that cc builds, cc_main.cpp:123-165);
+ * such a graph supports gb_wcc only. */
+gb_status gb_graph_from_csr(gb_ctx* ctx, int32_t n, int64_t m, const int64_t* out_off,
+                            const int32_t* out_adj, const int64_t* in_off,
+                            const int32_t* in_adj, gb_graph** g);
+/* From the reference's own CSR layout (graph struct, scc_main.cpp:75-86):
+ * 32-bit unsigned offsets out_degree_list[n+1] / in_degree_list[n+1].
+ * in_* may be NULL (symmetric graph of cc_main.cpp:72-79). */
+gb_status gb_graph_from_csr32(gb_ctx* ctx, int32_t n, uint32_t m, const int32_t* out_array,
+                              const uint32_t* out_degree_list, const int32_t* in_array,
+                              const uint32_t* in_degree_list, gb_graph** g);
+/* Seeded directed R-MAT graph built on the device: edge_factor << scale
+ * edges drawn with probabilities (a, b, c, 1-a-b-c), self-loops and
+ * duplicates removed.  Same edges as gb_rmat_edges_host. */
+gb_status gb_graph_rmat(gb_ctx* ctx, int32_t scale, int32_t edge_factor, uint64_t seed, double a,
+                        double b, double c, gb_graph** g);
+gb_status gb_graph_info(const gb_graph* g, int32_t* n, int64_t* m, int32_t* symmetric);
+/* Copies the CSR to host arrays (n+1 offsets, m entries; in_* ignored when
+ * NULL). */
+gb_status gb_graph_csr_to_host(const gb_graph* g, int64_t* out_off, int32_t* out_adj,
+                               int64_t* in_off, int32_t* in_adj);
+/* Device pointers of the CSR arrays (in_* NULL for a symmetric graph). */
+gb_status gb_graph_device_csr(const gb_graph* g, const int64_t** out_off,
+                              const int32_t** out_adj, const int64_t** in_off,
+                              const int32_t** in_adj);
+/* The reference's pivot and average degree: kind 0 = SCC rule
+ * (scc_main.cpp:169-183), kind 1 = cc rule on the mirrored graph
+ * (cc_main.cpp:148-160).  *pivot = -1 when no vertex qualifies. */
+gb_status gb_graph_pivot(gb_ctx* ctx, const gb_graph* g, int32_t kind, int32_t* pivot,
+                         double* avg_degree);
+gb_status gb_graph_destroy(gb_graph* g);
+
+/* ---- runs ------------------------------------------------------------- */
+/* run_scc (multistep/scc_main.cpp:210-317): trim, FW-BW from the pivot,
+ * colour rounds until every vertex is labelled. */
+gb_status gb_scc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts* opts,
+                 gb_stats* stats);
+/* run_cc (multistep/cc_main.cpp:184-245) on the mirrored graph: weakly
+ * connected components of a directed graph, or connected components of an
+ * undirected graph given as a symmetric CSR or as an edge list with each
+ * edge once (cc mirrors it, cc_main.cpp:102-118). */
+gb_status gb_wcc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts* opts,
+                 gb_stats* stats);
+gb_status gb_cc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts* opts,
+                gb_stats* stats);
+/* As gb_scc / gb_wcc but without waiting: labels must be device memory; the
+ * status is collected by gb_ctx_sync. */
+gb_status gb_scc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, const gb_opts* opts);
+gb_status gb_wcc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, const gb_opts* opts);
+
+/* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
+/* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
+ * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
+ * fields passed one by one and scc_maps owned by the caller (n ints).  Uses
+ * a library-owned context on device 0.  avg_degree is accepted for parity;
+ * the direction switch uses exact edge counts. */
+gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_array,
+                     const unsigned* out_degree_list, const unsigned* in_degree_list,
+                     int* scc_maps, int max_deg_vert, double avg_degree, int vert_cutoff);
+/* run_cc(graph& g, int*& cc_maps, int max_deg_vert, double avg_degree),
+ * multistep/cc_main.cpp:184-185, on the mirrored out-CSR of cc's graph
+ * struct (cc_main.cpp:72-79). */
+gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out_degree_list,
+                    int* cc_maps, int max_deg_vert, double avg_degree);
+
+/* ---- host utilities --------------------------------------------------- */
+/* read_edge (scc_main.cpp:94-125): "n m" then m lines "src dst".  Returns
+ * malloc'd arrays (free with gb_free_host).  Ids are checked against n.  cc's
+ * reader mirrors the edges (cc_main.cpp:102-118); here mirroring is done by
+ * gb_wcc itself, so one reader serves both. */
+gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int32_t** srcs, int32_t** dsts);
+void gb_free_host(void* p);
+/* output_scc / output_cc (scc_main.cpp:193-202, cc_main.cpp:167-176): one
+ * label per line. */
+gb_status gb_output_labels(const char* path, int32_t n, const int32_t* labels);
+/* scc_verify (multistep/scc_verify.cpp:47-77): writes the exact line
+ * "Num SCCs: %d, Nontrivial: %d, Max SCC: %d, Unassigned %d\n" into line
+ * (cap bytes) and the four numbers into stats (either may be NULL). */
+gb_status gb_scc_verify(int32_t n, const int32_t* labels, char* line, size_t cap,
+                        int64_t stats[4]);
+/* cc_verify (multistep/cc_verify.cpp:47-74): "Num CCs: %d, Max CC: %d,
+ * Unassigned %d\n"; stats = components, largest, unassigned. */
+gb_status gb_cc_verify(int32_t n, const int32_t* labels, char* line, size_t cap,
+                       int64_t stats[3]);
+/* Host relabelling to the minimum member id. */
+gb_status gb_canonicalize(int32_t n, int32_t* labels);
+/* Seeded generators (host, deterministic across machines).
+ * R-MAT: as gb_graph_rmat; *src/*dst malloc'd, sorted by (src, dst). */
+gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint64_t seed, double a,
+                             double b, double c, int64_t* m, int32_t** src, int32_t** dst);
+/* side x side lattice, every lattice edge u->v, v->u, both or none with
+ * probability 1/4 each, plus `extra` vertices hung off random lattice
+ * vertices in chains of length 1..max_chain (half feeding in from an
+ * in-degree-0 head, half draining to an out-degree-0 tail). */
+gb_status gb_grid_edges_host(int32_t side, int32_t extra, int32_t max_chain, uint64_t seed,
+                             int32_t* n, int64_t* m, int32_t** src, int32_t** dst);
+/* Sizes of a batch of graphs: n_i = round(median * exp(sigma * z_i))
+ * clipped to [n_min, n_max], z_i standard normal (sum of 12 uniforms - 6),
+ * edge factor uniform in [ef_min, ef_max], per-graph seeds. */
+gb_status gb_batch_sizes(int32_t count, uint64_t seed, double median, double sigma,
+                         int32_t n_min, int32_t n_max, int32_t ef_min, int32_t ef_max,
+                         int32_t* n_out, int32_t* ef_out, uint64_t* seed_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBCONN_H */

@@ -1,0 +1,20 @@
+#!/bin/sh
+# Builds the unmodified reference Multistep code (HPCGraphAnalysis/Connectivity
+# multistep/) into oracle/_ref/ through oracle/ref_harness.cpp.
+# Test infrastructure only; needs the reference tree (default location below,
+# or REF_DIR=...).  Nothing is written outside oracle/_ref/.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF_DIR=${REF_DIR:-/root/reference/multistep}
+OUT="$HERE/_ref"
+if [ ! -f "$REF_DIR/scc_main.cpp" ]; then
+  echo "reference not found at $REF_DIR; oracle/_ref not built" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+CXX=${CXX:-g++}
+FLAGS="-O3 -fopenmp -w"
+$CXX $FLAGS -DREF_SRC_SCC="\"$REF_DIR/scc_main.cpp\"" "$HERE/ref_harness.cpp" -o "$OUT/ref_scc" &
+$CXX $FLAGS -DREF_CC -DREF_SRC_CC="\"$REF_DIR/cc_main.cpp\"" "$HERE/ref_harness.cpp" -o "$OUT/ref_cc" &
+wait
+echo "built $OUT/ref_scc $OUT/ref_cc"

@@ -1,0 +1,172 @@
+// oracle/ref_harness.cpp -- runs the UNMODIFIED reference Multistep code
+// (HPCGraphAnalysis/Connectivity multistep/) on binary edge lists.
+//
+// TEST INFRASTRUCTURE ONLY: built by oracle/build_ref.sh into oracle/_ref/
+// when the reference tree is present, used to pin the C restatement
+// (oracle/multistep.c) and to produce the golden fixtures.
+//
+// The reference's translation unit is included as-is with its main renamed
+// (a macro around the #include), so create_csr, run_scc / run_cc and
+// the verify functions are the reference's own code.  Two allocation
+// overrides make two reads of uninitialised memory in that code well defined
+// without editing it:
+//   SCC: bool arrays of n bytes are zero-filled, so fw[] reads of trimmed
+//        vertices (scc_fwbw.cpp:60-63 initialises only valid ones, :280 reads
+//        any in-neighbour) see "false".
+//   CC:  int arrays of n entries are filled with the BFS root, so the tail of
+//        valid_verts that update_valid walks past num_valid (cc_bfs.cpp:231-
+//        233) names the root, whose only effect is to relabel the root with
+//        itself.
+//
+// Usage:
+//   ref_scc --text <graph> [out]       the reference main, unchanged
+//   ref_scc --bin <edges.bin> <labels.bin> [reps]
+// edges.bin: int64 n, int64 m, int32 src[m], int32 dst[m] (directed edges).
+// labels.bin receives int32 labels[n].  Prints the reference's own stdout
+// lines ("Multistep SCC time: ..." / verify line), time = best of reps.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <new>
+
+static long long g_fill_bytes = -1;   // allocation size that gets the fill
+static int g_fill_value = 0;          // int pattern written into it
+
+void* operator new[](std::size_t sz) {
+  void* p = std::malloc(sz ? sz : 1);
+  if (!p) throw std::bad_alloc();
+  if (g_fill_bytes >= 0 && (long long)sz == g_fill_bytes) {
+    if (g_fill_value == 0 || sz % sizeof(int) != 0) {
+      std::memset(p, 0, sz);
+    } else {
+      int* q = static_cast<int*>(p);
+      for (std::size_t i = 0; i < sz / sizeof(int); ++i) q[i] = g_fill_value;
+    }
+  }
+  return p;
+}
+void operator delete[](void* p) noexcept { std::free(p); }
+void operator delete[](void* p, std::size_t) noexcept { std::free(p); }
+
+#define main ref_main
+#if defined(REF_CC)
+#include REF_SRC_CC
+#else
+#include REF_SRC_SCC
+#endif
+#undef main
+
+static int read_bin(const char* path, int& n, unsigned& m, int*& srcs, int*& dsts) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return 1;
+  long long hdr[2];
+  if (std::fread(hdr, sizeof(long long), 2, f) != 2) { std::fclose(f); return 1; }
+  n = (int)hdr[0];
+  unsigned long long mm = (unsigned long long)hdr[1];
+#if defined(REF_CC)
+  m = (unsigned)(2 * mm);   // read_edge mirrors every edge (cc_main.cpp:102-118)
+#else
+  m = (unsigned)mm;
+#endif
+  g_fill_bytes = -1;
+  srcs = new int[m];
+  dsts = new int[m];
+  int* s = (int*)std::malloc(mm * sizeof(int) + 1);
+  int* d = (int*)std::malloc(mm * sizeof(int) + 1);
+  bool ok = std::fread(s, sizeof(int), mm, f) == mm && std::fread(d, sizeof(int), mm, f) == mm;
+  std::fclose(f);
+  if (!ok) return 1;
+#if defined(REF_CC)
+  for (unsigned long long i = 0; i < mm; ++i) {
+    srcs[2 * i] = s[i]; dsts[2 * i] = d[i];
+    srcs[2 * i + 1] = d[i]; dsts[2 * i + 1] = s[i];
+  }
+#else
+  std::memcpy(srcs, s, mm * sizeof(int));
+  std::memcpy(dsts, d, mm * sizeof(int));
+#endif
+  std::free(s); std::free(d);
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  setbuf(stdout, NULL);
+  if (argc >= 3 && std::strcmp(argv[1], "--text") == 0) {
+#if defined(REF_CC)
+    // the text path cannot know the root before create_csr; the fill is the
+    // vertex the reference picks, computed here with the same rule
+    // (cc_main.cpp:148-160) from a first read of the file.
+    {
+      int n; unsigned m; int *s, *d;
+      read_edge(argv[2], n, m, s, d);
+      int* out_array; unsigned* odl; int root = 0; double avg;
+      create_csr(n, m, s, d, out_array, odl, root, avg);
+      delete[] s; delete[] d; delete[] out_array; delete[] odl;
+      g_fill_bytes = (long long)n * (long long)sizeof(int);
+      g_fill_value = root;
+    }
+#else
+    {
+      FILE* f = std::fopen(argv[2], "r");
+      int n = 0;
+      if (f) { if (std::fscanf(f, "%d", &n) != 1) n = 0; std::fclose(f); }
+      g_fill_bytes = n;
+      g_fill_value = 0;
+    }
+#endif
+    char* args[3] = {argv[0], argv[2], argc >= 4 ? argv[3] : nullptr};
+    return ref_main(argc >= 4 ? 3 : 2, args);
+  }
+  if (argc < 4 || std::strcmp(argv[1], "--bin") != 0) {
+    std::printf("Usage: %s --text <graph> [out] | --bin <edges.bin> <labels.bin> [reps]\n", argv[0]);
+    return 2;
+  }
+  int reps = argc >= 5 ? std::atoi(argv[4]) : 1;
+  if (reps < 1) reps = 1;
+  int n; unsigned m; int *srcs, *dsts;
+  if (read_bin(argv[2], n, m, srcs, dsts)) { std::printf("cannot read %s\n", argv[2]); return 1; }
+  double best = 1e30;
+  int* maps = nullptr;
+#if defined(REF_CC)
+  int* out_array; unsigned* odl; int root = 0; double avg;
+  create_csr(n, m, srcs, dsts, out_array, odl, root, avg);
+  graph g = {n, m, out_array, odl};
+  for (int r = 0; r < reps; ++r) {
+    if (maps) delete[] maps;
+    g_fill_bytes = (long long)n * (long long)sizeof(int);
+    g_fill_value = root;
+    double t = timer();
+    run_cc(g, maps, root, avg);
+    t = timer() - t;
+    g_fill_bytes = -1;
+    if (t < best) best = t;
+  }
+  std::printf("Multistep CC time: %9.6lf\n", best);
+  cc_verify(g, maps);
+#else
+  int* out_array; int* in_array; unsigned* odl; unsigned* idl; int root = -1; double avg;
+  create_csr(n, m, srcs, dsts, out_array, in_array, odl, idl, root, avg);
+  // every degree product zero: the reference leaves the pivot unset
+  // (scc_main.cpp:334); vertex 0 is used, which only relabels a trimmed vertex.
+  if (root < 0) root = 0;
+  graph g = {n, m, out_array, in_array, odl, idl};
+  for (int r = 0; r < reps; ++r) {
+    if (maps) delete[] maps;
+    g_fill_bytes = n;
+    g_fill_value = 0;
+    double t = timer();
+    run_scc(g, maps, root, avg, 10000);
+    t = timer() - t;
+    g_fill_bytes = -1;
+    if (t < best) best = t;
+  }
+  std::printf("Multistep SCC time: %9.6lf\n", best);
+  scc_verify(g, maps);
+#endif
+  FILE* f = std::fopen(argv[3], "wb");
+  if (!f) return 1;
+  std::fwrite(maps, sizeof(int), (size_t)n, f);
+  std::fclose(f);
+  return 0;
+}

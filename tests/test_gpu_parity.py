@@ -1,0 +1,182 @@
+"""Parity of the CUDA path with the oracle: canonical labels must be
+bit-identical, and the verify lines byte-identical, on every case.  Calls go
+through the C ABI (libgbconn.so via ctypes)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import connectivity_gb300 as gb
+import oracle
+from tests import graphs
+
+pytestmark = pytest.mark.gpu
+
+CASES = graphs.edge_cases()
+
+VARIANTS = {
+    "default": {},
+    "trim2": {"trim_level": 2},
+    # tiny tiers push every vertex through the block and grid-slice paths
+    "tiers": {"t_block": 33, "t_grid": 64},
+    "pull_early": {"alpha": 1e9, "beta": 1e-3, "k_pull": 1},
+    "push_only": {"alpha": 1e-9},
+    "small_grid": {"grid_blocks": 3},
+}
+
+
+def _scc_want(n, s, d):
+    return oracle.scc(oracle.CpuGraph(n, s, d))
+
+
+def _wcc_want(n, s, d):
+    return oracle.cc(oracle.CpuGraph(n, s, d, mirror=True))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_scc_edge_cases(ctx, case, variant):
+    name, n, s, d = case
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab, st = ctx.scc(g, o=gb.opts(**VARIANTS[variant]), stats=True)
+    want = _scc_want(n, s, d)
+    assert np.array_equal(lab, want), name
+    assert gb.scc_verify(lab) == gb.scc_verify(want)
+    assert st.unassigned == 0
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("variant", ["default", "tiers", "pull_early", "small_grid"])
+def test_wcc_edge_cases(ctx, case, variant):
+    name, n, s, d = case
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab = ctx.wcc(g, o=gb.opts(**VARIANTS[variant]))
+    want = _wcc_want(n, s, d)
+    assert np.array_equal(lab, want), name
+    assert gb.cc_verify(lab) == gb.cc_verify(want)
+
+
+def test_reference_golden_vector(ctx):
+    # multistep/test.graph: SCC {0,1},{2}; CC one component
+    n, s, d = graphs.test_graph()
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    assert ctx.scc(g).tolist() == [0, 0, 2]
+    assert ctx.wcc(g).tolist() == [0, 0, 0]
+    assert gb.scc_verify(ctx.scc(g)) == "Num SCCs: 2, Nontrivial: 1, Max SCC: 2, Unassigned 0\n"
+
+
+@pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
+@pytest.mark.parametrize("variant", ["default", "trim2", "tiers", "small_grid"])
+def test_rmat_scc(ctx, scale, ef, variant):
+    n, s, d = graphs.rmat(scale, ef)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab = ctx.scc(g, o=gb.opts(**VARIANTS[variant]))
+    want = _scc_want(n, s, d)
+    assert np.array_equal(lab, want)
+
+
+@pytest.mark.parametrize("scale,ef", [(10, 16), (14, 16), (16, 16), (18, 8)])
+def test_rmat_wcc(ctx, scale, ef):
+    n, s, d = graphs.rmat(scale, ef)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+
+
+@pytest.mark.parametrize("side", [16, 64, 128])
+@pytest.mark.parametrize("variant", ["default", "trim2"])
+def test_grid_scc(ctx, side, variant):
+    n, s, d = graphs.grid(side)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab = ctx.scc(g, o=gb.opts(**VARIANTS[variant]))
+    want = _scc_want(n, s, d)
+    assert np.array_equal(lab, want)
+
+
+@pytest.mark.parametrize("side", [64, 256])
+def test_grid_wcc(ctx, side):
+    n, s, d = graphs.grid(side)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+
+
+def test_device_rmat_matches_host_generator(ctx):
+    g = gb.Graph.rmat(ctx, 14, 16, 5)
+    n, s, d = gb.rmat_edges(14, 16, 5)
+    oo, oa, io, ia = g.to_host()
+    off, adj = gb.csr_from_edges(n, s, d)
+    assert np.array_equal(oo, off) and np.array_equal(oa, adj)
+    off, adj = gb.csr_from_edges(n, d, s)
+    assert np.array_equal(io, off) and np.array_equal(ia, adj)
+
+
+def test_from_csr_and_pivot(ctx):
+    n, s, d = graphs.rmat(12, 16, 3)
+    cg = oracle.CpuGraph(n, s, d)
+    g = gb.Graph.from_csr(ctx, n, cg.out_off, cg.out_adj, cg.in_off, cg.in_adj)
+    assert np.array_equal(ctx.scc(g), _scc_want(n, s, d))
+    assert ctx.pivot(g, 0)[0] == cg.pivot_scc()[0]
+    mg = oracle.CpuGraph(n, s, d, mirror=True)
+    assert ctx.pivot(g, 1)[0] == mg.pivot_cc()[0]
+    # symmetric CSR (cc's mirrored graph) gives the same WCC
+    sg = gb.Graph.from_csr(ctx, n, mg.out_off, mg.out_adj)
+    assert sg.symmetric
+    assert np.array_equal(ctx.wcc(sg), _wcc_want(n, s, d))
+
+
+def test_reference_shaped_dropins():
+    n, s, d = graphs.rmat(12, 16, 9)
+    cg = oracle.CpuGraph(n, s, d)
+    odl = cg.out_off.astype(np.uint32)
+    idl = cg.in_off.astype(np.uint32)
+    piv, avg = cg.pivot_scc()
+    lab = gb.run_scc_ref(n, cg.out_adj, cg.in_adj, odl, idl, piv, avg, 10000)
+    assert np.array_equal(lab, _scc_want(n, s, d))
+    mg = oracle.CpuGraph(n, s, d, mirror=True)
+    piv, avg = mg.pivot_cc()
+    lab = gb.run_cc_ref(n, mg.out_adj, mg.out_off.astype(np.uint32), piv, avg)
+    assert np.array_equal(lab, _wcc_want(n, s, d))
+
+
+def test_device_labels_and_async(ctx):
+    torch = pytest.importorskip("torch")
+    n, s, d = graphs.rmat(14, 16, 11)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    want = _scc_want(n, s, d)
+    out = torch.full((n,), -7, dtype=torch.int32, device="cuda:0")
+    ctx.scc(g, labels=out.data_ptr())
+    assert np.array_equal(out.cpu().numpy(), want)
+    out2 = torch.full((n,), -7, dtype=torch.int32, device="cuda:0")
+    for _ in range(3):
+        ctx.scc_async(g, out2.data_ptr())
+    ctx.sync()
+    assert np.array_equal(out2.cpu().numpy(), want)
+
+
+def test_raw_labels_partition(ctx):
+    n, s, d = graphs.rmat(14, 16, 13)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    raw = ctx.scc(g, o=gb.opts(canonical=0))
+    assert np.array_equal(gb.canonicalize(raw), _scc_want(n, s, d))
+
+
+def test_bad_edges_rejected(ctx):
+    with pytest.raises(gb.GBError):
+        gb.Graph.from_edges(ctx, 4, np.array([0, 5], np.int32), np.array([1, 2], np.int32))
+    off = np.array([0, 2, 1], np.int64)  # decreasing offsets
+    with pytest.raises(gb.GBError):
+        gb.Graph.from_csr(ctx, 2, off, np.array([1, 0], np.int32))
+
+
+def test_repeat_runs_identical(ctx):
+    n, s, d = graphs.rmat(16, 16, 21)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    first = ctx.scc(g)
+    for _ in range(5):
+        assert np.array_equal(ctx.scc(g), first)
+
+
+def test_rmat_s20_scc_and_wcc(ctx):
+    n, s, d = graphs.rmat(20, 16, 1)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    assert np.array_equal(ctx.scc(g), _scc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
