@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""SCC GTEPS on R-MAT-24 on one GB300, beside the reference's OpenMP Multistep.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbconn|reference]
+
+A step is one full SCC run (trim, FW-BW, colour rounds, canonical labels) of
+the directed R-MAT graph of scale 24, edge factor 16 (a=0.57 b=0.19 c=0.19,
+seed 1, self-loops and duplicates removed: 16,777,216 vertices,
+263,434,267 edges), the workload the headline metric is quoted on.  GTEPS =
+edges / seconds per step.
+
+value : the CSR already resident in HBM, labels written to device memory,
+        steps enqueued back to back, CUDA events on the library's stream.
+e2e   : the reference-shaped C-ABI call gb_run_scc (the run_scc signature
+        with the reference's 32-bit CSR layout) on pinned host buffers: every
+        step copies the CSR host->device and the labels device->host.
+For N > 1 (torchrun) every rank runs a replica on its own GPU ("replicas
+only": the path does not shard), barrier + max time over ranks.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement in oracle/ (OpenMP, all threads) on the same graph, each step
+one full run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SCC GTEPS on R-MAT-24 (1 GB300) vs host OpenMP; batched graphs/s and p99 ms"
+SCALE, EF, SEED = 24, 16, 1
+ABC = (0.57, 0.19, 0.19)
+
+
+def workload_name(n, m):
+    return (f"R-MAT scale {SCALE}, edge factor {EF}, a=0.57 b=0.19 c=0.19, seed {SEED}, "
+            f"self-loops and duplicates removed ({n:,} vertices, {m:,} edges); SCC")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gbconn", choices=["gbconn", "reference"])
+    p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--cpu-reps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the reach kernel from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        return d.get("k_reach_bytes_per_launch")
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the
+    timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline_run(n, m, oo, oa, io, ia, reps):
+    import oracle
+    cg = oracle.CpuGraph.from_csr(n, oo, oa, io, ia)
+    lab = oracle.scc(cg)  # warm-up, and the labels for the parity check
+    best = 1e30
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.scc(cg, canonical=False)
+        best = min(best, time.perf_counter() - t0)
+    return lab, best, oracle.num_threads()
+
+
+def run_reference(args):
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import connectivity_gb300 as gb
+    import oracle
+    t0 = time.time()
+    n, s, d = gb.rmat_edges(SCALE, EF, SEED, ABC)
+    cg = oracle.CpuGraph(n, s, d)
+    del s, d
+    prep = time.time() - t0
+    m = cg.m
+    for _ in range(max(args.warmup, 0)):
+        oracle.scc(cg, canonical=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.scc(cg, canonical=False)
+    T = time.perf_counter() - t0
+    val = m / (T / args.steps) / 1e9
+    cores = oracle.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "GTEPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(T / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": workload_name(n, m), "graph_build_s": round(prep, 1),
+                   "l2": "inputs larger than L2 (2.1 GB CSR)"},
+        "cpu_baseline": {"value": round(val, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
+                         "sample": "each step one full SCC run of the workload on the host "
+                                   "(oracle/multistep.c, OpenMP restatement of run_scc)"},
+        "e2e": {"value": round(val, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gbconn(args):
+    import numpy as np
+    import torch
+
+    import __graft_entry__
+    if not os.path.exists(os.path.join(ROOT, "connectivity_gb300", "libgbconn.so")):
+        __graft_entry__.build()
+    import connectivity_gb300 as gb
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as tdist
+            tdist.barrier()
+
+    def allmax(x):
+        if ws == 1:
+            return x
+        import torch.distributed as tdist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    ctx = gb.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    g = gb.Graph.rmat(ctx, SCALE, EF, SEED, ABC)
+    n, m = g.n, g.m
+    labels = torch.empty(n, dtype=torch.int32, device="cuda")
+    o = gb.opts()
+
+    # warm-up
+    for _ in range(max(args.warmup, 3)):
+        ctx.scc_async(g, labels.data_ptr(), o)
+    ctx.sync()
+
+    phys = local
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd:
+        try:
+            phys = int(cvd.split(",")[local])
+        except ValueError:
+            phys = local
+    clocks = Clocks(phys)
+    K = args.steps
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)  # first sample lands inside the timed region
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        ctx.scc_async(g, labels.data_ptr(), o)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    barrier()
+    ctx.sync()  # raises if any timed run failed on the device
+    T = e0.elapsed_time(e1) / 1e3
+    T = allmax(T)
+    phases = ctx.phase_times(min(K, 64))
+    reach_ms = float(phases[:, 1].mean())
+    step_ms = T / K * 1e3
+    value = ws * m / (T / K) / 1e9
+
+    # one more run with statistics (algorithmic bytes of each kernel)
+    lab_dev, st = ctx.scc(g, labels=labels.data_ptr(), stats=True)
+    gpu_labels = labels.cpu().numpy()
+
+    # e2e through the reference-shaped C ABI on pinned host buffers
+    oo, oa, io, ia = g.to_host()
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    odl, idl = pin(oo.astype(np.uint32)), pin(io.astype(np.uint32))
+    oa_p, ia_p = pin(oa), pin(ia)
+    out_p = pin(np.empty(n, np.int32))
+    piv, avg = ctx.pivot(g, 0)
+    gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)  # warm-up
+    KE = max(1, min(args.e2e_steps, K))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(KE):
+        gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
+    TE = allmax(time.perf_counter() - t0)
+    e2e_ok = bool(np.array_equal(out_p, gpu_labels))
+    h2d = (n + 1) * 4 * 2 + m * 4 * 2
+    d2h = n * 4
+
+    peak, peak_kind = peaks()
+    achieved = st.bytes_reach / (reach_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": K,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(step_ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": workload_name(n, m),
+                   "l2": "inputs larger than L2 (2.1 GB CSR, 129 MB L2); no flush",
+                   "parallelism": "replicas only" if ws > 1 else "single GPU",
+                   "trim_level": 1, "labels": "canonical minimum member id, device memory"},
+        "e2e": {"value": round(ws * m / (TE / KE) / 1e9, 3), "unit": "GTEPS",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(TE / KE * 1e3, 3), "steps": KE,
+                "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers)",
+                "labels_match_device_run": e2e_ok},
+        "roofline": {"bound": "hbm", "kernel": "k_reach (FW-BW reachability + commit)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": profile_traffic(),
+                     "algorithmic_bytes_per_launch": int(st.bytes_reach),
+                     "launch_ms": round(reach_ms, 4)},
+        "phases_ms": {k: round(float(v), 4) for k, v in
+                      zip(("trim", "reach", "colour", "canon", "total"), phases.mean(axis=0))},
+        "gpu_launches": 5 * K,
+        "clocks": ck,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        want, tcpu, cores = cpu_baseline_run(n, m, oo, oa, io, ia, args.cpu_reps)
+        line["cpu_baseline"] = {
+            "value": round(m / tcpu / 1e9, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
+            "sample": f"full workload, best of {args.cpu_reps} runs after 1 warm-up "
+                      "(oracle/multistep.c, OpenMP restatement of run_scc)"}
+        line["parity"] = {"labels_equal_oracle": bool(np.array_equal(gpu_labels, want)),
+                          "verify_line": gb.scc_verify(gpu_labels).strip()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gbconn(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -64,7 +64,8 @@ class Stats(C.Structure):
         ("pivot", C.c_int32), ("colour_rounds", C.c_int32),
         ("n_trim", C.c_int64), ("n_visit_fw", C.c_int64), ("n_fwbw", C.c_int64),
         ("unassigned", C.c_int64), ("vtx_reads", C.c_int64), ("edge_reads", C.c_int64),
-        ("list_rw", C.c_int64), ("trim_steps", C.c_int64), ("fw_steps", C.c_int64),
+        ("list_rw", C.c_int64), ("bytes_trim", C.c_int64), ("bytes_reach", C.c_int64),
+        ("bytes_colour", C.c_int64), ("bytes_canon", C.c_int64), ("trim_steps", C.c_int64), ("fw_steps", C.c_int64),
         ("bw_steps", C.c_int64), ("pull_steps", C.c_int64), ("colour_steps", C.c_int64),
         ("mark_steps", C.c_int64), ("grid_blocks", C.c_int32), ("err_where", C.c_int32),
     ]
@@ -93,6 +94,8 @@ _sig("gb_ctx_destroy", C.c_int32, [_P])
 _sig("gb_ctx_set_stream", C.c_int32, [_P, _P])
 _sig("gb_ctx_stream", _P, [_P])
 _sig("gb_ctx_sync", C.c_int32, [_P])
+_sig("gb_ctx_phase_times", C.c_int32, [_P, C.c_int32, _P])
+_sig("gb_ctx_reach_trace", C.c_int32, [_P, _P, _P, _P, C.c_int32])
 _sig("gb_graph_from_edges", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, C.POINTER(_P)])
 _sig("gb_graph_from_csr", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, _P, _P, C.POINTER(_P)])
 _sig("gb_graph_from_csr32", C.c_int32, [_P, C.c_int32, C.c_uint32, _P, _P, _P, _P, C.POINTER(_P)])
@@ -268,6 +271,21 @@ class Context:
 
     def sync(self) -> None:
         _check(_lib.gb_ctx_sync(self._h), "gb_ctx_sync")
+
+    def reach_trace(self, cap: int = 128) -> list[tuple[int, int, int]]:
+        """(device ns, vertices appended, mode bits) per reachability step of
+        the last completed run."""
+        t = np.zeros(cap, np.int64)
+        cnt = np.zeros(cap, np.int32)
+        mode = np.zeros(cap, np.int32)
+        k = _lib.gb_ctx_reach_trace(self._h, _ptr(t), _ptr(cnt), _ptr(mode), cap)
+        return [(int(t[i]), int(cnt[i]), int(mode[i])) for i in range(k)]
+
+    def phase_times(self, count: int) -> np.ndarray:
+        """(count, 5) ms of the last runs: trim, reach, colour, canon, total."""
+        out = np.zeros((count, 5), np.float64)
+        _check(_lib.gb_ctx_phase_times(self._h, count, _ptr(out)), "gb_ctx_phase_times")
+        return out
 
     def _run(self, fn, name, g: "Graph", labels, o: Opts | None, want_stats: bool):
         st = Stats()

@@ -23,7 +23,9 @@ struct gb_ctx {
   gb::Ctl* h_ctl = nullptr;     // pinned
   int* d_sticky = nullptr;      // first error of any run since the last sync
   int* h_sticky = nullptr;      // pinned
-  cudaEvent_t ev[5] = {};
+  static constexpr int kRing = 64;
+  cudaEvent_t ev[kRing][5] = {};  // phase events of the last kRing runs
+  long long runs = 0;             // runs issued on this context
 };
 
 struct gb_graph {
@@ -151,12 +153,14 @@ void graph_free(gb_graph* g) {
 
 gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
   CK(cudaStreamSynchronize(c->stream), "run");
+  (void)g;
   const gb::Ctl& h = *c->h_ctl;
   if (st) {
     std::memset(st, 0, sizeof(*st));
     float ms[4] = {0, 0, 0, 0}, tot = 0;
-    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
-    cudaEventElapsedTime(&tot, c->ev[0], c->ev[4]);
+    cudaEvent_t* ev = c->ev[(c->runs - 1) % gb_ctx::kRing];
+    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    cudaEventElapsedTime(&tot, ev[0], ev[4]);
     st->ms_trim = ms[0];
     st->ms_reach = ms[1];
     st->ms_colour = ms[2];
@@ -168,9 +172,31 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
     st->n_visit_fw = h.nvisit_fw;
     st->n_fwbw = h.nscc_fwbw;
     st->unassigned = h.unassigned;
-    st->vtx_reads = (int64_t)h.stat[gb::kStVtx];
-    st->edge_reads = (int64_t)h.stat[gb::kStEdges];
-    st->list_rw = (int64_t)h.stat[gb::kStList];
+    int64_t tv = 0, te = 0, tl = 0;
+    for (int k = 0; k < 4; ++k) {
+      tv += (int64_t)h.kst[k][0];
+      te += (int64_t)h.kst[k][1];
+      tl += (int64_t)h.kst[k][2];
+    }
+    st->vtx_reads = tv;
+    st->edge_reads = te;
+    st->list_rw = tl;
+    const int64_t n = g->n, nb = (n + 7) / 8;
+    auto kb = [&](int k) {
+      return 16 * (int64_t)h.kst[k][0] + 4 * (int64_t)h.kst[k][1] + 4 * (int64_t)h.kst[k][2];
+    };
+    // trim: degrees (counted as offset records), labels, valid bitmap
+    // written and re-read for the ordered list
+    st->bytes_trim = kb(gb::kKTrim) + 4 * n + 2 * nb;
+    // reach: per traversal the visited bitmap (read + write) and the allowed
+    // bitmap (read); then labels of the found component and the valid
+    // bitmap update
+    const int64_t trav = (h.stat[gb::kStFwSteps] ? 1 : 0) + (h.stat[gb::kStBwSteps] ? 1 : 0);
+    st->bytes_reach = kb(gb::kKReach) + trav * 3 * nb + 4 * (int64_t)h.nscc_fwbw + 2 * nb;
+    // colour: every list entry also touches its colour (init + read)
+    st->bytes_colour = kb(gb::kKColour) + 4 * (int64_t)h.kst[gb::kKColour][2];
+    // final pass: one label read per vertex
+    st->bytes_canon = 4 * n;
     st->trim_steps = (int64_t)h.stat[gb::kStTrimSteps];
     st->fw_steps = (int64_t)h.stat[gb::kStFwSteps];
     st->bw_steps = (int64_t)h.stat[gb::kStBwSteps];
@@ -222,6 +248,7 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   if (dev_labels) w.label = labels;
   gb::RunParams p;
   fill_params(o, p);
+  p.count_unassigned = st != nullptr ? 1 : 0;
   int grid = c->grid;
   if (o && o->grid_blocks > 0 && o->grid_blocks < grid) grid = o->grid_blocks;
   gb::GraphView gv;
@@ -240,7 +267,9 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   CK(cudaMemsetAsync(w.bvis, 0, (size_t)w.nwords * 4, sm), "memset");
   CK(cudaMemsetAsync(w.done, 0, (size_t)w.nwords * 4, sm), "memset");
   CK(cudaMemsetAsync(w.stamp, 0xff, (size_t)g->n * 4, sm), "memset");
-  CK(gb::launch_run(gv, kind, p, w, grid, sm, c->ev), "kernel launch");
+  cudaEvent_t* ev = c->ev[c->runs % gb_ctx::kRing];
+  c->runs++;
+  CK(gb::launch_run(gv, kind, p, w, grid, sm, ev), "kernel launch");
   CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
   if (!dev_labels)
     CK(cudaMemcpyAsync(labels, w.label, (size_t)g->n * 4, cudaMemcpyDeviceToHost, sm), "labels copy");
@@ -267,7 +296,7 @@ void gb_opts_default(gb_opts* o) {
   o->vert_cutoff = 10000;
   o->t_block = 512;
   o->t_grid = 32768;
-  o->k_pull = 8;
+  o->k_pull = 4;
   o->alpha = 15.0f;
   o->beta = 25.0f;
   o->max_steps = 1 << 30;
@@ -310,8 +339,9 @@ gb_status gb_ctx_create(int device, gb_ctx** out) {
     cudaMemset(c->d_sticky, 0, 2 * sizeof(int));
     std::memset(c->h_ctl, 0, sizeof(gb::Ctl));
     c->h_sticky[0] = c->h_sticky[1] = 0;
-    for (int i = 0; i < 5 && s == GB_OK; ++i)
-      if ((r = cudaEventCreate(&c->ev[i])) != cudaSuccess) s = cuda_fail(r, "event");
+    for (int k = 0; k < gb_ctx::kRing && s == GB_OK; ++k)
+      for (int i = 0; i < 5 && s == GB_OK; ++i)
+        if ((r = cudaEventCreate(&c->ev[k][i])) != cudaSuccess) s = cuda_fail(r, "event");
     if (s != GB_OK) break;
     c->grid = gb::max_coop_grid(device);
     if (c->grid <= 0) { gb_set_error("gb_ctx_create: %s", "no cooperative occupancy"); s = GB_ERR_UNSUPPORTED; break; }
@@ -333,8 +363,9 @@ gb_status gb_ctx_destroy(gb_ctx* c) {
   cudaFree(c->d_sticky);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
   if (c->h_sticky) cudaFreeHost(c->h_sticky);
-  for (auto& e : c->ev)
-    if (e) cudaEventDestroy(e);
+  for (auto& set : c->ev)
+    for (auto& e : set)
+      if (e) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return GB_OK;
@@ -362,6 +393,39 @@ gb_status gb_ctx_sync(gb_ctx* c) {
     return (gb_status)err;
   }
   return GB_OK;
+}
+
+gb_status gb_ctx_phase_times(gb_ctx* c, int32_t count, double* ms) {
+  if (!c || !ms || count < 0 || count > gb_ctx::kRing || count > c->runs) return GB_ERR_INVALID;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaStreamSynchronize(c->stream), "phase times");
+  for (int32_t i = 0; i < count; ++i) {
+    cudaEvent_t* ev = c->ev[(c->runs - count + i) % gb_ctx::kRing];
+    float x = 0;
+    for (int j = 0; j < 4; ++j) {
+      CK(cudaEventElapsedTime(&x, ev[j], ev[j + 1]), "phase times");
+      ms[i * 5 + j] = x;
+    }
+    CK(cudaEventElapsedTime(&x, ev[0], ev[4]), "phase times");
+    ms[i * 5 + 4] = x;
+  }
+  return GB_OK;
+}
+
+int32_t gb_ctx_reach_trace(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mode, int32_t cap) {
+  if (!c || cap < 0) return 0;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return 0;
+  const gb::Ctl& h = *c->h_ctl;
+  const int total = h.ntrace;
+  const int have = total < gb::kTrace ? total : gb::kTrace;
+  const int k = have < cap ? have : cap;
+  for (int i = 0; i < k; ++i) {
+    const auto& e = h.trace[(total - k + i) % gb::kTrace];
+    if (t_ns) t_ns[i] = (int64_t)e.t;
+    if (count) count[i] = e.count;
+    if (mode) mode[i] = e.mode;
+  }
+  return k;
 }
 
 gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
@@ -587,7 +651,12 @@ gb_status gb_wcc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_o
 // device 0 and reusable device buffers for the graph.
 static gb_status default_ctx(gb_ctx** c) {
   if (!g_default_ctx) {
-    gb_status s = gb_ctx_create(0, &g_default_ctx);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+      cudaGetLastError();
+      dev = 0;
+    }
+    gb_status s = gb_ctx_create(dev, &g_default_ctx);
     if (s != GB_OK) return s;
   }
   *c = g_default_ctx;

@@ -39,10 +39,7 @@ struct Slot {
 
 // Statistic slots (64-bit counters, summed over the whole run).
 enum Stat : int {
-  kStVtx = 0,        // vertex offset records read (one per vertex per CSR)
-  kStEdges,          // adjacency entries read
-  kStList,           // list entries read or written (frontiers, candidates)
-  kStTrimSteps,
+  kStTrimSteps = 0,
   kStFwSteps,
   kStBwSteps,
   kStPullSteps,
@@ -67,10 +64,29 @@ struct Ctl {
   int32_t ntrim;          // vertices labelled by trim
   int32_t ncolour_rounds;
   int32_t unassigned;
-  int32_t pad;
+  int32_t ncolour;        // vertices labelled by the colour rounds
+  int32_t minv[2];        // smallest vertex reached forward / backward
+  int32_t lcount[2][2];   // pull steps: warp- and block-tier list lengths
+                          // (two sets, used by alternate pull steps)
+  int32_t pad1;
   unsigned long long m_cand;   // push-degree sum of the valid list after trim
   unsigned long long stat[kStNum];
+  // Algorithmic traffic per kernel (trim, reach, colour, canon): vertex
+  // offset records read, adjacency entries read, list entries read/written.
+  unsigned long long kst[4][3];
+  // Per-step trace of the reachability kernel (last kTrace steps): device
+  // time at the end of the step, vertices appended, mode (1 = pull).
+  struct Trace {
+    unsigned long long t;
+    int32_t count;
+    int32_t mode;
+  } trace[128];
+  int32_t ntrace;
+  int32_t pad2;
 };
+constexpr int kTrace = 128;
+
+enum KernelId : int { kKTrim = 0, kKReach = 1, kKColour = 2, kKCanon = 3 };
 
 struct Tune {
   int32_t t_block;        // degree from which a whole block expands a vertex
@@ -125,6 +141,7 @@ struct RunParams {
   int32_t trim_level;     // 1: one pass, 2: fixed point
   int32_t canonical;      // 1: relabel with the minimum member id
   int32_t pivot_hint;     // >= 0: use as FW-BW source if still valid
+  int32_t count_unassigned;  // 1: a final pass counts labels outside [0, n)
   Tune tune;
 };
 

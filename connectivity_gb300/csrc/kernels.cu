@@ -208,12 +208,12 @@ __device__ __forceinline__ void steps_close(Ctl* c, const Steps& st) {
 struct Tally {
   unsigned long long vtx = 0, edges = 0, list = 0;
 };
-__device__ void tally_flush(const Tally& t, Ctl* c) {
+__device__ void tally_flush(const Tally& t, Ctl* c, int kernel) {
   const unsigned long long a = warp_sum64(t.vtx), b = warp_sum64(t.edges), d = warp_sum64(t.list);
   if (lane_id() == 0) {
-    if (a) atomicAdd(&c->stat[kStVtx], a);
-    if (b) atomicAdd(&c->stat[kStEdges], b);
-    if (d) atomicAdd(&c->stat[kStList], d);
+    if (a) atomicAdd(&c->kst[kernel][0], a);
+    if (b) atomicAdd(&c->kst[kernel][1], b);
+    if (d) atomicAdd(&c->kst[kernel][2], d);
   }
 }
 __device__ __forceinline__ void stat_inc(Ctl* c, int slot) {
@@ -231,38 +231,53 @@ __device__ __forceinline__ long long warp_excl64(long long x, long long& total) 
   total = (long long)__shfl_sync(kFull, (unsigned long long)inc, 31);
   return inc - x;
 }
+__device__ __forceinline__ int32_t warp_min(int32_t x) {
+  for (int o = 16; o; o >>= 1) x = min(x, __shfl_xor_sync(kFull, x, o));
+  return x;
+}
 
 // ------------------------------------------------------------------------
 // Adjacency of a vertex over one or two CSRs (two: the union of out- and
 // in-edges, which is the mirrored graph that cc builds, cc_main.cpp:102-118).
+// The CSR arrays are read-only for a whole run (__ldg).
 // ------------------------------------------------------------------------
+// NC (1 or 2) is a compile-time copy of a.n, so the one-CSR paths carry no
+// second-CSR state.
 struct Adj {
   Csr c[2];
   int n;
 };
+template <int NC>
 __device__ __forceinline__ void rec_load(const Adj& a, int32_t v, long long& s0, long long& d0,
                                          long long& s1, long long& d1) {
-  s0 = a.c[0].off[v];
-  d0 = a.c[0].off[v + 1] - s0;
+  s0 = __ldg(a.c[0].off + v);
+  d0 = __ldg(a.c[0].off + v + 1) - s0;
   s1 = 0;
   d1 = 0;
-  if (a.n > 1) {
-    s1 = a.c[1].off[v];
-    d1 = a.c[1].off[v + 1] - s1;
+  if constexpr (NC > 1) {
+    s1 = __ldg(a.c[1].off + v);
+    d1 = __ldg(a.c[1].off + v + 1) - s1;
   }
 }
+template <int NC>
 __device__ __forceinline__ int32_t adj_at(const Adj& a, long long s0, long long d0, long long s1,
                                           long long e, int& k) {
-  if (e < d0) {
+  if constexpr (NC == 1) {
     k = 0;
-    return a.c[0].adj[s0 + e];
+    return __ldg(a.c[0].adj + s0 + e);
+  } else {
+    if (e < d0) {
+      k = 0;
+      return __ldg(a.c[0].adj + s0 + e);
+    }
+    k = 1;
+    return __ldg(a.c[1].adj + s1 + (e - d0));
   }
-  k = 1;
-  return a.c[1].adj[s1 + (e - d0)];
 }
+template <int NC>
 __device__ __forceinline__ unsigned long long adj_degree(const Adj& a, int32_t v) {
-  long long d = a.c[0].off[v + 1] - a.c[0].off[v];
-  if (a.n > 1) d += a.c[1].off[v + 1] - a.c[1].off[v];
+  long long d = __ldg(a.c[0].off + v + 1) - __ldg(a.c[0].off + v);
+  if constexpr (NC > 1) d += __ldg(a.c[1].off + v + 1) - __ldg(a.c[1].off + v);
   return (unsigned long long)d;
 }
 __device__ __forceinline__ Adj adj1(Csr x) {
@@ -285,67 +300,82 @@ __device__ __forceinline__ Adj adj_undirected(const GraphView& g) {
   return g.in.off != nullptr ? adj2(g.out, g.in) : adj1(g.out);
 }
 
-// Output of one expansion step.
-struct Sink {
-  int32_t* arr;               // receives appended vertices at base + slot
+// ------------------------------------------------------------------------
+// Appends.  Each warp stages the vertices it appends in shared memory and
+// moves them to the global list in one atomic + coalesced copy per kWB
+// entries, which keeps the step counters (a single L2 word) cool.
+// ------------------------------------------------------------------------
+constexpr int kWB = 128;
+
+// A global output list.
+struct Out {
+  int32_t* arr;               // receives vertices at base + slot
   long long base;
   long long cap;              // bound on base + slot
-  int32_t* counter;           // Slot::count of the step
-  unsigned long long* edges;  // Slot::edges, or null
-  int32_t* harr;              // heavy list for the next step, or null
-  int32_t hcap;
-  int32_t* hcounter;          // Slot::huge
+  int32_t* counter;           // slot counter
+  unsigned long long* edges;  // weight sum, or null
+  int32_t* minv;              // smallest appended id, or null
+  int where;                  // error site
 };
-__device__ __forceinline__ Sink sink_make(int32_t* arr, long long base, long long cap, Slot* o,
-                                          bool weighted, int32_t* harr, int32_t hcap) {
-  Sink k;
-  k.arr = arr;
-  k.base = base;
-  k.cap = cap;
-  k.counter = &o->count;
-  k.edges = weighted ? &o->edges : nullptr;
-  k.harr = harr;
-  k.hcap = hcap;
-  k.hcounter = &o->huge;
-  return k;
-}
 
-// Warp-aggregated append: one atomic per warp and call.  All 32 lanes call.
-template <class V>
-__device__ __forceinline__ void sink_append(bool app, int32_t w, const Sink& sk, const V& vis,
-                                            Ctl* c) {
-  const unsigned mask = __ballot_sync(kFull, app);
+// One warp's staging buffer for one Out (n is warp-uniform).
+struct Stage {
+  int32_t* buf;
+  int n;
+  unsigned long long wsum;
+  int32_t vmin;
+};
+__device__ __forceinline__ Stage stage_make(int32_t* buf) {
+  Stage s;
+  s.buf = buf;
+  s.n = 0;
+  s.wsum = 0ull;
+  s.vmin = 0x7fffffff;
+  return s;
+}
+// All 32 lanes call.
+__device__ __noinline__ void stage_flush(Stage& s, const Out& o, Ctl* c) {
+  __syncwarp();
+  const int lane = lane_id();
+  if (s.n > 0) {
+    int pos = 0;
+    if (lane == 0) pos = atomicAdd(o.counter, s.n);
+    pos = __shfl_sync(kFull, pos, 0);
+    for (int i = lane; i < s.n; i += 32) {
+      const long long at = o.base + pos + i;
+      if (at < o.cap) o.arr[at] = s.buf[i];
+      else set_err(c, kErrCapacity, o.where);
+    }
+  }
+  if (o.edges != nullptr) {
+    const unsigned long long ws = warp_sum64(s.wsum);
+    if (lane == 0 && ws) atomicAdd(o.edges, ws);
+  }
+  if (o.minv != nullptr) {
+    const int32_t mn = warp_min(s.vmin);
+    if (lane == 0 && mn != 0x7fffffff) atomicMin(o.minv, mn);
+  }
+  __syncwarp();
+  s.n = 0;
+  s.wsum = 0ull;
+  s.vmin = 0x7fffffff;
+}
+// All 32 lanes call; lanes with `flag` append v (weight wt).
+__device__ __forceinline__ void stage_push(Stage& s, bool flag, int32_t v, unsigned long long wt,
+                                           const Out& o, Ctl* c) {
+  const unsigned mask = __ballot_sync(kFull, flag);
   if (mask == 0u) return;
-  const int leader = __ffs(mask) - 1;
-  int pos = 0;
-  if ((int)lane_id() == leader) pos = atomicAdd(sk.counter, __popc(mask));
-  pos = __shfl_sync(kFull, pos, leader) + __popc(mask & lanemask_lt());
-  if (app) {
-    const long long at = sk.base + pos;
-    if (at < sk.cap) sk.arr[at] = w;
-    else set_err(c, kErrCapacity, 101);
+  const int cnt = __popc(mask);
+  if (s.n + cnt > kWB) stage_flush(s, o, c);
+  if (flag) {
+    s.buf[s.n + __popc(mask & lanemask_lt())] = v;
+    s.wsum += wt;
+    s.vmin = min(s.vmin, v);
   }
-  if (V::kWeighted && sk.edges != nullptr) {
-    unsigned long long wt = app ? vis.weight(w) : 0ull;
-    wt = warp_sum64(wt);
-    if ((int)lane_id() == leader && wt) atomicAdd(sk.edges, wt);
-  }
+  s.n += cnt;
 }
 
-__device__ __forceinline__ void heavy_append(bool app, int32_t v, const Sink& sk, Ctl* c) {
-  const unsigned mask = __ballot_sync(kFull, app);
-  if (mask == 0u) return;
-  const int leader = __ffs(mask) - 1;
-  int pos = 0;
-  if ((int)lane_id() == leader) pos = atomicAdd(sk.hcounter, __popc(mask));
-  pos = __shfl_sync(kFull, pos, leader) + __popc(mask & lanemask_lt());
-  if (app) {
-    if (pos < sk.hcap) sk.harr[pos] = v;
-    else set_err(c, kErrCapacity, 102);
-  }
-}
-
-// Plain warp-aggregated append into a list with a slot counter.
+// Plain warp-aggregated append (used for the rare heavy-vertex lists).
 __device__ __forceinline__ void list_append(bool app, int32_t v, int32_t* arr, int32_t* counter,
                                             long long cap, Ctl* c, int where) {
   const unsigned mask = __ballot_sync(kFull, app);
@@ -375,7 +405,44 @@ struct Smem {
   int warp_tmp[kWarps + 1];
   long long red_l[kWarps];
   int red_i[kWarps];
+  int32_t stage[kWarps][2][kWB];
 };
+
+// Output of one expansion step: the main list and the heavy list.
+struct Sink {
+  Out out;
+  int32_t* harr;              // heavy list for the next step, or null
+  int32_t hcap;
+  int32_t* hcounter;
+};
+__device__ __forceinline__ Sink sink_make(int32_t* arr, long long base, long long cap, Slot* o,
+                                          bool weighted, int32_t* minv, int32_t* harr,
+                                          int32_t hcap, int where) {
+  Sink k;
+  k.out.arr = arr;
+  k.out.base = base;
+  k.out.cap = cap;
+  k.out.counter = &o->count;
+  k.out.edges = weighted ? &o->edges : nullptr;
+  k.out.minv = minv;
+  k.out.where = where;
+  k.harr = harr;
+  k.hcap = hcap;
+  k.hcounter = &o->huge;
+  return k;
+}
+
+// Appends the far end of an edge when the visitor accepts it.
+template <class V>
+__device__ __forceinline__ void visit_edge(const V& vis, int32_t sv, int32_t w, int k, bool act,
+                                           Stage& st, const Sink& sk, Ctl* c) {
+  const bool app = vis.edge(sv, w, k, act);
+  unsigned long long wt = 0ull;
+  if (V::kWeighted && app && sk.out.edges != nullptr) wt = vis.weight(w);
+  stage_push(st, app, w, wt, sk.out, c);
+}
+
+constexpr int kSmallFront = 8;
 
 // ------------------------------------------------------------------------
 // Frontier expansion (push).  Three tiers by degree:
@@ -384,39 +451,48 @@ struct Smem {
 //   d >= t_block: the whole block walks the edges (per-block list);
 //   otherwise   : a warp takes 32 vertices, scans their degrees and walks
 //                 the concatenated edge lists 32 edges at a time.
-// The visitor decides per edge whether the far end is appended.
+// A frontier of at most kSmallFront vertices is sliced across all blocks in
+// the same step.  The visitor decides per edge whether the far end is
+// appended.  Ends with every warp's staging flushed.
 // ------------------------------------------------------------------------
-template <class V>
+template <int NC, class V>
 __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heavy, int32_t nheavy,
                        const Adj& a, const V& vis, const Sink& sk, const Tune& tn, Smem& sm,
                        Ctl* c, Tally& ty) {
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
-  // (1) heavy vertices deferred by the previous step: block b takes slice b
-  for (int j = 0; j < nheavy; ++j) {
-    const int32_t v = __ldcg(heavy + j);
+  const int warp = t >> 5, lane = t & 31;
+  Stage st = stage_make(sm.stage[warp][0]);
+  const bool small = nfront <= kSmallFront;
+  // (1) heavy vertices deferred by the previous step, and a small frontier:
+  // block b takes slice b of each vertex's edges
+  const int nsl = nheavy + (small ? nfront : 0);
+  for (int j = 0; j < nsl; ++j) {
+    const int32_t v = j < nheavy ? __ldcg(heavy + j) : __ldcg(front + (j - nheavy));
     long long s0, d0, s1, d1;
-    rec_load(a, v, s0, d0, s1, d1);
+    rec_load<NC>(a, v, s0, d0, s1, d1);
     const long long d = d0 + d1;
     const long long lo = d * b / G, hi = d * (b + 1) / G;
     const int32_t sv = vis.source(v);
-    if (t == 0) ty.vtx += a.n;
+    if (t == 0) ty.vtx += NC;
     for (long long e0 = lo; e0 < hi; e0 += T) {
       const long long e = e0 + t;
       const bool act = e < hi;
       int32_t w = 0;
       int k = 0;
       if (act) {
-        w = adj_at(a, s0, d0, s1, e, k);
+        w = adj_at<NC>(a, s0, d0, s1, e, k);
         ty.edges++;
       }
-      const bool app = vis.edge(sv, w, k, act);
-      sink_append(app, w, sk, vis, c);
+      visit_edge(vis, sv, w, k, act, st, sk, c);
     }
+  }
+  if (small) {
+    stage_flush(st, sk.out, c);
+    return;
   }
   // (2) regular frontier, warp-gathered
   if (t == 0) sm.bl.cnt = 0;
   __syncthreads();
-  const int warp = t >> 5, lane = t & 31;
   const long long nw = (long long)G * (T >> 5);
   for (long long base = ((long long)b * (T >> 5) + warp) * 32; base < nfront; base += nw * 32) {
     const long long i = base + lane;
@@ -424,13 +500,13 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
     long long s0 = 0, d0 = 0, s1 = 0, d1 = 0;
     if (i < nfront) {
       v = __ldcg(front + i);
-      rec_load(a, v, s0, d0, s1, d1);
+      rec_load<NC>(a, v, s0, d0, s1, d1);
       ty.list++;
-      ty.vtx += a.n;
+      ty.vtx += NC;
     }
     const long long d = d0 + d1;
     const bool to_grid = v >= 0 && d >= tn.t_grid && sk.harr != nullptr;
-    heavy_append(to_grid, v, sk, c);
+    list_append(to_grid, v, sk.harr, sk.hcounter, sk.hcap, c, 102);
     bool to_block = false;
     if (v >= 0 && !to_grid && d >= tn.t_block) {
       const int slot = atomicAdd(&sm.bl.cnt, 1);
@@ -453,8 +529,8 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
       const bool act = e < tot;
       int j = 0;
 #pragma unroll
-      for (int st = 16; st; st >>= 1) {
-        const int cnd = j + st;
+      for (int stp = 16; stp; stp >>= 1) {
+        const int cnd = j + stp;
         const long long exc = shfl64(ex, cnd);
         if (exc <= e) j = cnd;
       }
@@ -464,11 +540,10 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
       int32_t w = 0;
       int k = 0;
       if (act) {
-        w = adj_at(a, s0j, d0j, s1j, e - ej, k);
+        w = adj_at<NC>(a, s0j, d0j, s1j, e - ej, k);
         ty.edges++;
       }
-      const bool app = vis.edge(svj, w, k, act);
-      sink_append(app, w, sk, vis, c);
+      visit_edge(vis, svj, w, k, act, st, sk, c);
     }
   }
   __syncthreads();
@@ -484,13 +559,13 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
       int32_t w = 0;
       int k = 0;
       if (act) {
-        w = adj_at(a, s0, d0, s1, e, k);
+        w = adj_at<NC>(a, s0, d0, s1, e, k);
         ty.edges++;
       }
-      const bool app = vis.edge(sv, w, k, act);
-      sink_append(app, w, sk, vis, c);
+      visit_edge(vis, sv, w, k, act, st, sk, c);
     }
   }
+  stage_flush(st, sk.out, c);
   __syncthreads();
 }
 
@@ -498,6 +573,7 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
 // Visitors: edge(source value, far end, which CSR, active) -> append?
 // ------------------------------------------------------------------------
 // Reachability: the far end is taken if allowed and not yet reached.
+template <int NC>
 struct ReachVisit {
   static constexpr bool kWeighted = true;
   const uint32_t* allow;
@@ -510,12 +586,16 @@ struct ReachVisit {
     if (!bit_get(allow, w)) return false;
     return bit_claim(vis, w);
   }
-  __device__ __forceinline__ unsigned long long weight(int32_t w) const { return adj_degree(push, w); }
+  __device__ __forceinline__ unsigned long long weight(int32_t w) const {
+    return adj_degree<NC>(push, w);
+  }
 };
 
-// Max-colour push: colour[w] = max(colour[w], colour[v]) over valid w
-// (scc_color.cpp:89-113); a vertex whose colour rose is queued once per step
-// (iteration stamp).
+// Colour push: colour[w] = min(colour[w], colour[v]) over valid w.  The
+// reference pushes the maximum (scc_color.cpp:89-113, cc_color.cpp:103-127);
+// pushing the minimum is the same algorithm mirrored, and its roots are the
+// smallest ids of their SCCs, so the labels come out canonical.  A vertex
+// whose colour fell is queued once per step (iteration stamp).
 struct ColourVisit {
   static constexpr bool kWeighted = false;
   const uint32_t* valid;
@@ -526,8 +606,8 @@ struct ColourVisit {
   __device__ __forceinline__ bool edge(int32_t cv, int32_t w, int, bool act) const {
     if (!act) return false;
     if (!bit_get(valid, w)) return false;
-    if (__ldcg(colour + w) >= cv) return false;
-    if (atomicMax(colour + w, cv) >= cv) return false;
+    if (__ldcg(colour + w) <= cv) return false;
+    if (atomicMin(colour + w, cv) <= cv) return false;
     return atomicExch(stamp + w, iter) != iter;
   }
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
@@ -645,7 +725,7 @@ __device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsign
   return k2 > k || (k2 == k && v2 >= 0 && (v < 0 || v2 < v));
 }
 
-__global__ void __launch_bounds__(kBlock) k_trim(Args A) {
+__global__ void __launch_bounds__(kBlock, 2) k_trim(Args A) {
   __shared__ Smem sm;
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -663,45 +743,75 @@ __global__ void __launch_bounds__(kBlock) k_trim(Args A) {
   int32_t best_v = -1;
   unsigned long long mc = 0ull;
   int removed = 0;
-  TrimVisit tv{w.vbits, w.live_in, w.live_out, w.label};
-  const Sink rsink = sink_make(w.x0, 0, g.n, step_out(c, st.s), false, nullptr, 0);
+  const TrimVisit tv{w.vbits, w.live_in, w.live_out, w.label};
+  Stage rs = stage_make(sm.stage[warp][0]);
+  Out ro;
+  ro.arr = w.x0;
+  ro.base = 0;
+  ro.cap = g.n;
+  ro.counter = &step_out(c, st.s)->count;
+  ro.edges = nullptr;
+  ro.minv = nullptr;
+  ro.where = 103;
+  // Each warp takes kTrimU consecutive words per iteration and issues all
+  // their offset loads before using any.
+  constexpr int kTrimU = 4;
   const long long nwarps = (long long)G * (T >> 5);
-  for (long long wd = (long long)b * (T >> 5) + warp; wd < w.nwords; wd += nwarps) {
-    const long long vv = wd * 32 + lane;
-    bool keep = false, gone = false;
-    if (vv < g.n) {
-      const int32_t v = (int32_t)vv;
-      const long long dout = g.out.off[v + 1] - g.out.off[v];
-      long long din = 0;
-      if (g.in.off != nullptr) din = g.in.off[v + 1] - g.in.off[v];
-      ty.vtx += g.in.off != nullptr ? 2 : 1;
-      if (scc) {
-        keep = dout > 0 && din > 0;
-        if (keep) {
-          const unsigned long long prod = (unsigned long long)dout * (unsigned long long)din;
-          if (prod > best_key) { best_key = prod; best_v = v; }
-          mc += (unsigned long long)dout;
-        }
-      } else {
-        const long long deg = dout + din;
-        keep = deg > 0;
-        if (keep) {
-          if ((unsigned long long)deg > best_key) { best_key = (unsigned long long)deg; best_v = v; }
-          mc += (unsigned long long)deg;
+  for (long long wd0 = ((long long)b * (T >> 5) + warp) * kTrimU; wd0 < w.nwords;
+       wd0 += nwarps * kTrimU) {
+    long long o0[kTrimU], o1[kTrimU], i0[kTrimU], i1[kTrimU];
+#pragma unroll
+    for (int j = 0; j < kTrimU; ++j) {
+      const long long vv = (wd0 + j) * 32 + lane;
+      o0[j] = o1[j] = i0[j] = i1[j] = 0;
+      if (vv < g.n) {
+        o0[j] = __ldg(g.out.off + vv);
+        o1[j] = __ldg(g.out.off + vv + 1);
+        if (g.in.off != nullptr) {
+          i0[j] = __ldg(g.in.off + vv);
+          i1[j] = __ldg(g.in.off + vv + 1);
         }
       }
-      gone = !keep;
-      w.label[v] = keep ? -1 : v;
-      if (level2) {
-        w.live_out[v] = (int32_t)(dout < 0x7fffffffll ? dout : 0x7fffffffll);
-        w.live_in[v] = (int32_t)(din < 0x7fffffffll ? din : 0x7fffffffll);
-      }
-      if (gone) ++removed;
     }
-    const unsigned bits = __ballot_sync(kFull, keep);
-    if (lane == 0) w.vbits[wd] = bits;
-    if (level2) sink_append(gone, (int32_t)vv, rsink, tv, c);
+#pragma unroll
+    for (int j = 0; j < kTrimU; ++j) {
+      const long long wd = wd0 + j;
+      const long long vv = wd * 32 + lane;
+      bool keep = false, gone = false;
+      if (vv < g.n) {
+        const int32_t v = (int32_t)vv;
+        const long long dout = o1[j] - o0[j];
+        const long long din = i1[j] - i0[j];
+        ty.vtx += g.in.off != nullptr ? 2 : 1;
+        if (scc) {
+          keep = dout > 0 && din > 0;
+          if (keep) {
+            const unsigned long long prod = (unsigned long long)dout * (unsigned long long)din;
+            if (prod > best_key) { best_key = prod; best_v = v; }
+            mc += (unsigned long long)dout;
+          }
+        } else {
+          const long long deg = dout + din;
+          keep = deg > 0;
+          if (keep) {
+            if ((unsigned long long)deg > best_key) { best_key = (unsigned long long)deg; best_v = v; }
+            mc += (unsigned long long)deg;
+          }
+        }
+        gone = !keep;
+        w.label[v] = keep ? -1 : v;
+        if (level2) {
+          w.live_out[v] = (int32_t)(dout < 0x7fffffffll ? dout : 0x7fffffffll);
+          w.live_in[v] = (int32_t)(din < 0x7fffffffll ? din : 0x7fffffffll);
+        }
+        if (gone) ++removed;
+      }
+      const unsigned bits = __ballot_sync(kFull, keep);
+      if (wd < w.nwords && lane == 0) w.vbits[wd] = bits;
+      if (level2) stage_push(rs, gone, (int32_t)vv, 0ull, ro, c);
+    }
   }
+  if (level2) stage_flush(rs, ro, c);
   {
     unsigned long long k = best_key;
     int32_t v = best_v;
@@ -753,8 +863,9 @@ __global__ void __launch_bounds__(kBlock) k_trim(Args A) {
       if (st.s - st.s0 >= A.p.tune.max_steps) { set_err(c, kErrIterLimit, 2); return; }
       const StepIn in = step_read(c, st.s);
       if (in.count == 0) break;
-      const Sink sk = sink_make(bufs[cur ^ 1], 0, g.n, step_out(c, st.s), false, nullptr, 0);
-      expand(bufs[cur], in.count, nullptr, 0, both, tv, sk, A.p.tune, sm, c, ty);
+      const Sink sk = sink_make(bufs[cur ^ 1], 0, g.n, step_out(c, st.s), false, nullptr, nullptr,
+                                0, 104);
+      expand<2>(bufs[cur], in.count, nullptr, 0, both, tv, sk, A.p.tune, sm, c, ty);
       stat_inc(c, kStTrimSteps);
       if (!step_sync(c, st, 3)) return;
       cur ^= 1;
@@ -806,7 +917,7 @@ __global__ void __launch_bounds__(kBlock) k_trim(Args A) {
     if (pv >= 0 && !bit_get(w.vbits, pv)) pv = -1;
     c->pivot = pv;
   }
-  tally_flush(ty, c);
+  tally_flush(ty, c, kKTrim);
   steps_close(c, st);
 }
 
@@ -818,7 +929,8 @@ __global__ void __launch_bounds__(kBlock) k_trim(Args A) {
 // (scc_fwbw.cpp:116-149).  Push -> pull when the frontier's edge count times
 // alpha exceeds the unvisited edge estimate; pull -> push when the frontier
 // has fewer than ncand / beta vertices.  q receives every reached vertex
-// exactly once, so q[0, result) is the reached set.  Returns -1 on error.
+// exactly once, so q[0, result) is the reached set; *minv gets its smallest
+// id.  Returns -1 on error.
 // ------------------------------------------------------------------------
 struct ReachSpec {
   Adj push, pull;
@@ -829,27 +941,213 @@ struct ReachSpec {
   unsigned long long m_cand;
   int32_t root;
   int32_t* q;
+  int32_t* minv;
   int stat_slot;
 };
 
-__device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps& st, Tally& ty) {
+constexpr int kPullU = 4;  // candidates per thread per pull iteration
+
+// One pull step: every unreached candidate looks for a reached
+// pull-neighbour (scc_fwbw.cpp:116-149, which scans until the first hit).
+// Three tiers keep the work balanced:
+//   thread: up to kPullThread edges, kPullU candidates per thread with
+//           their loads overlapped;
+//   warp  : candidates with more edges, one warp each, 32 edges per
+//           iteration, up to kPullWarpEdges edges;
+//   block : the rest, one block each, kBlock edges per iteration.
+// The warp and block tiers run after a grid barrier on lists the thread
+// tier filled, spread over the whole grid.  Found candidates are appended
+// to q; candidates with no reached neighbour are kept in cand_next.
+constexpr int kPullThread = 4;
+constexpr long long kPullWarpEdges = 2048;
+
+template <int NC>
+__device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
+                          const int32_t* cand_cur, int32_t ncur, int32_t* cand_next, long long qhi,
+                          Slot* o, int pp) {
+  Ctl* c = w.ctl;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  int32_t* lc = c->lcount[pp & 1];
+  if (b == 0 && t == 0) {
+    c->lcount[(pp + 1) & 1][0] = 0;
+    c->lcount[(pp + 1) & 1][1] = 0;
+  }
+  const int kt = A.p.tune.k_pull < kPullThread ? (A.p.tune.k_pull > 0 ? A.p.tune.k_pull : 1)
+                                                : kPullThread;
+  Out of;
+  of.arr = R.q;
+  of.base = qhi;
+  of.cap = w.n;
+  of.counter = &o->count;
+  of.edges = nullptr;
+  of.minv = R.minv;
+  of.where = 202;
+  Out ok;
+  ok.arr = cand_next;
+  ok.base = 0;
+  ok.cap = w.n;
+  ok.counter = &o->cand;
+  ok.edges = nullptr;
+  ok.minv = nullptr;
+  ok.where = 203;
+  Stage sf = stage_make(sm.stage[warp][0]);
+  Stage sk = stage_make(sm.stage[warp][1]);
+  int32_t* wl = w.x1;  // warp-tier list
+  int32_t* bl = w.h1;  // block-tier list
+  const long long nw = (long long)G * (T >> 5);
+  for (long long base = ((long long)b * (T >> 5) + warp) * 32 * kPullU; base < ncur;
+       base += nw * 32 * kPullU) {
+    int32_t v[kPullU];
+    bool unv[kPullU], found[kPullU];
+    long long s0[kPullU], d0[kPullU], s1[kPullU], d1[kPullU];
+    int32_t u[kPullU][kPullThread];
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      const long long i = base + j * 32 + lane;
+      v[j] = i < ncur ? __ldcg(cand_cur + i) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) unv[j] = v[j] >= 0 && !bit_get(R.vis, v[j]);
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      s0[j] = d0[j] = s1[j] = d1[j] = 0;
+      if (unv[j]) rec_load<NC>(R.pull, v[j], s0[j], d0[j], s1[j], d1[j]);
+    }
+    // first edge of every candidate, then the next kt-1 of those still open
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      u[j][0] = -1;
+      if (unv[j] && d0[j] + d1[j] > 0) {
+        int k;
+        u[j][0] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], 0, k);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      found[j] = u[j][0] >= 0 && bit_get(R.vis, u[j][0]);
+      if (v[j] >= 0) ty.list++;
+      if (unv[j]) {
+        ty.vtx += NC;
+        if (u[j][0] >= 0) ty.edges++;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+#pragma unroll
+      for (int e = 1; e < kPullThread; ++e) {
+        u[j][e] = -1;
+        if (unv[j] && !found[j] && e < kt && e < d0[j] + d1[j]) {
+          int k;
+          u[j][e] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], e, k);
+        }
+      }
+    }
+    bool to_warp[kPullU], to_block[kPullU], keep[kPullU];
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+#pragma unroll
+      for (int e = 1; e < kPullThread; ++e) {
+        if (u[j][e] >= 0) {
+          ty.edges++;
+          if (!found[j] && bit_get(R.vis, u[j][e])) found[j] = true;
+        }
+      }
+      const long long d = d0[j] + d1[j];
+      const bool open = unv[j] && !found[j];
+      to_warp[j] = open && d > kt && d <= kt + kPullWarpEdges;
+      to_block[j] = open && d > kt + kPullWarpEdges;
+      keep[j] = open && d <= kt;
+    }
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      const bool f = found[j] && bit_claim(R.vis, v[j]);
+      stage_push(sf, f, v[j], 0ull, of, c);
+      stage_push(sk, keep[j], v[j], 0ull, ok, c);
+      list_append(to_warp[j], v[j], wl, &lc[0], w.n, c, 204);
+      list_append(to_block[j], v[j], bl, &lc[1], w.n, c, 205);
+    }
+  }
+  // the warp and block tiers need the complete lists
+  if (!grid_barrier(c, 206)) return false;
+  const int32_t nwl = __ldcg(&lc[0]), nbl = __ldcg(&lc[1]);
+  for (long long j = (long long)b * (T >> 5) + warp; j < nwl; j += nw) {
+    const int32_t v = __ldcg(wl + j);
+    long long s0, d0, s1, d1;
+    rec_load<NC>(R.pull, v, s0, d0, s1, d1);
+    const long long d = d0 + d1;
+    bool found = false;
+    for (long long e0 = kt; e0 < d; e0 += 32) {
+      const long long e = e0 + lane;
+      bool hit = false;
+      if (e < d) {
+        int k;
+        const int32_t x = adj_at<NC>(R.pull, s0, d0, s1, e, k);
+        ty.edges++;
+        hit = bit_get(R.vis, x);
+      }
+      if (__any_sync(kFull, hit)) {
+        found = true;
+        break;
+      }
+    }
+    const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
+    stage_push(sf, f, v, 0ull, of, c);
+    stage_push(sk, !found && lane == 0, v, 0ull, ok, c);
+  }
+  for (long long j = b; j < nbl; j += G) {
+    const int32_t v = __ldcg(bl + j);
+    long long s0, d0, s1, d1;
+    rec_load<NC>(R.pull, v, s0, d0, s1, d1);
+    const long long d = d0 + d1;
+    bool found = false;
+    for (long long e0 = kt; e0 < d; e0 += T) {
+      const long long e = e0 + t;
+      bool hit = false;
+      if (e < d) {
+        int k;
+        const int32_t x = adj_at<NC>(R.pull, s0, d0, s1, e, k);
+        ty.edges++;
+        hit = bit_get(R.vis, x);
+      }
+      if (__syncthreads_or(hit)) {
+        found = true;
+        break;
+      }
+    }
+    if (warp == 0) {
+      const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
+      stage_push(sf, f, v, 0ull, of, c);
+      stage_push(sk, !found && lane == 0, v, 0ull, ok, c);
+    }
+  }
+  stage_flush(sf, of, c);
+  stage_flush(sk, ok, c);
+  return true;
+}
+
+template <int NC>
+__device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps& st, Tally& ty,
+                     int& pp) {
   Ctl* c = w.ctl;
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
   const Tune& tn = A.p.tune;
-  const ReachVisit rv{R.allow, R.vis, R.push};
+  const ReachVisit<NC> rv{R.allow, R.vis, R.push};
   if (b == 0 && t == 0) {
     if (bit_claim(R.vis, R.root)) {
       R.q[0] = R.root;
       Slot* o = step_out(c, st.s);
       o->count = 1;
-      o->edges = adj_degree(R.push, R.root);
+      o->edges = adj_degree<NC>(R.push, R.root);
+      *R.minv = R.root;
     }
   }
   if (!step_sync(c, st, 20)) return -1;
   long long qlo = 0, qhi = 0;
   bool pull = false, prev_pull = false;
   unsigned long long edges_seen = 0ull;
+  const double avg = R.ncand > 0 ? (double)R.m_cand / (double)R.ncand : 0.0;
   const int32_t* cand_cur = R.cand;
   int32_t ncur = R.ncand;
   int32_t* cand_next = w.candA;
@@ -861,7 +1159,11 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
     const StepIn in = step_read(c, st.s);
     qlo = qhi;
     qhi = qlo + in.count;
-    edges_seen += in.edges;
+    // a pull step does not read the push degrees of what it finds; its
+    // frontier edge count is estimated from the average degree
+    const unsigned long long medges =
+        prev_pull ? (unsigned long long)((double)in.count * avg) : in.edges;
+    edges_seen += medges;
     if (prev_pull) {
       cand_cur = cand_next;
       ncur = in.cand;
@@ -869,92 +1171,26 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
     }
     if (!pull) {
       const unsigned long long mu = R.m_cand > edges_seen ? R.m_cand - edges_seen : 0ull;
-      if ((double)in.edges * (double)tn.alpha > (double)mu) pull = true;
+      if ((double)medges * (double)tn.alpha > (double)mu) pull = true;
     } else if ((double)in.count * (double)tn.beta < (double)R.ncand) {
       pull = false;
     }
+    if (b == 0 && t == 0) {
+      const int ti = c->ntrace % kTrace;
+      c->trace[ti].t = gtimer();
+      c->trace[ti].count = in.count;
+      c->trace[ti].mode = (pull ? 1 : 0) | (in.huge > 0 ? 2 : 0) | (R.stat_slot == kStBwSteps ? 4 : 0);
+      c->ntrace++;
+    }
     if (in.count == 0 && (pull || in.huge == 0)) break;
     Slot* o = step_out(c, st.s);
-    const Sink sk = sink_make(R.q, qhi, w.n, o, true, hl[hsel ^ 1], w.n);
     if (!pull) {
-      expand(R.q + qlo, (int32_t)(qhi - qlo), hl[hsel], in.huge, R.push, rv, sk, tn, sm, c, ty);
+      const Sink sk = sink_make(R.q, qhi, w.n, o, true, R.minv, hl[hsel ^ 1], w.n, 201);
+      expand<NC>(R.q + qlo, (int32_t)(qhi - qlo), hl[hsel], in.huge, R.push, rv, sk, tn, sm, c, ty);
       prev_pull = false;
     } else {
-      // every unreached candidate looks for a reached pull-neighbour; the
-      // still-unreached ones are kept (any order) for the next pull step
-      if (t == 0) sm.bl.cnt = 0;
-      __syncthreads();
-      const long long nw = (long long)G * (T >> 5);
-      for (long long base = ((long long)b * (T >> 5) + warp) * 32; base < ncur; base += nw * 32) {
-        const long long i = base + lane;
-        int32_t v = -1;
-        bool found = false, keep = false;
-        if (i < ncur) {
-          v = __ldcg(cand_cur + i);
-          ty.list++;
-          if (!bit_get(R.vis, v)) {
-            long long s0, d0, s1, d1;
-            rec_load(R.pull, v, s0, d0, s1, d1);
-            ty.vtx += R.pull.n;
-            const long long d = d0 + d1;
-            const long long lim = d < tn.k_pull ? d : tn.k_pull;
-            for (long long e = 0; e < lim; ++e) {
-              int k;
-              const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
-              ty.edges++;
-              if (bit_get(R.vis, u)) { found = true; break; }
-            }
-            if (!found && d > lim) {
-              const int slot = atomicAdd(&sm.bl.cnt, 1);
-              if (slot < kBlkList) {
-                sm.bl.v[slot] = v;
-                sm.bl.s0[slot] = s0;
-                sm.bl.d0[slot] = d0;
-                sm.bl.s1[slot] = s1;
-                sm.bl.d1[slot] = d1;
-              } else {
-                for (long long e = lim; e < d; ++e) {
-                  int k;
-                  const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
-                  ty.edges++;
-                  if (bit_get(R.vis, u)) { found = true; break; }
-                }
-                keep = !found;
-              }
-            } else if (!found) {
-              keep = true;
-            }
-          }
-        }
-        if (found) found = bit_claim(R.vis, v);
-        sink_append(found, v, sk, rv, c);
-        list_append(keep, v, cand_next, &o->cand, w.n, c, 22);
-        if (keep) ty.list++;
-      }
-      __syncthreads();
-      // candidates with long pull lists: one warp each, 32 edges at a time
-      const int nb = sm.bl.cnt < kBlkList ? sm.bl.cnt : kBlkList;
-      for (int j = warp; j < nb; j += kWarps) {
-        const int32_t v = sm.bl.v[j];
-        const long long s0 = sm.bl.s0[j], d0 = sm.bl.d0[j], s1 = sm.bl.s1[j];
-        const long long d = d0 + sm.bl.d1[j];
-        bool found = false;
-        for (long long e0 = tn.k_pull; e0 < d; e0 += 32) {
-          const long long e = e0 + lane;
-          bool hit = false;
-          if (e < d) {
-            int k;
-            const int32_t u = adj_at(R.pull, s0, d0, s1, e, k);
-            ty.edges++;
-            hit = bit_get(R.vis, u);
-          }
-          if (__any_sync(kFull, hit)) { found = true; break; }
-        }
-        const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
-        sink_append(f, v, sk, rv, c);
-        list_append(!found && lane == 0, v, cand_next, &o->cand, w.n, c, 23);
-      }
-      __syncthreads();
+      if (!pull_step<NC>(R, A, w, sm, ty, cand_cur, ncur, cand_next, qhi, o, pp)) return -1;
+      ++pp;
       prev_pull = true;
       stat_inc(c, kStPullSteps);
     }
@@ -967,11 +1203,13 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
 
 // ------------------------------------------------------------------------
 // k_reach: SCC -> forward and backward reachability from the pivot; the SCC
-// (reached both ways) takes the pivot as label and leaves the valid list
-// (scc_fwbw, scc_fwbw.cpp:469-513).  WCC -> one search over the union
-// adjacency (cc_bfs, cc_bfs.cpp:273-291).
+// (reached both ways) leaves the valid list labelled with its smallest id
+// (or the pivot, with canonical labels off), as update_valid does with the
+// pivot (scc_fwbw, scc_fwbw.cpp:412-513).  WCC -> one search over the union
+// adjacency (cc_bfs, cc_bfs.cpp:217-291).
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_reach(Args A) {
+template <int NC>
+__global__ void __launch_bounds__(kBlock, 2) k_reach(Args A) {
   __shared__ Smem sm;
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -985,6 +1223,7 @@ __global__ void __launch_bounds__(kBlock) k_reach(Args A) {
   Steps st = steps_open(c);
   const bool scc = A.kind == kSCC;
   const uint32_t* hit;
+  int32_t* hit_min;
   ReachSpec F;
   F.push = scc ? adj1(g.out) : adj_undirected(g);
   F.pull = scc ? adj1(g.in) : F.push;
@@ -995,8 +1234,10 @@ __global__ void __launch_bounds__(kBlock) k_reach(Args A) {
   F.m_cand = __ldcg(&c->m_cand);
   F.root = pivot;
   F.q = w.q;
+  F.minv = &c->minv[0];
   F.stat_slot = kStFwSteps;
-  const int nf = reach(F, A, w, sm, st, ty);
+  int pp = 0;  // pull steps so far (selects the long-list counters)
+  const int nf = reach<NC>(F, A, w, sm, st, ty, pp);
   if (nf < 0) return;
   if (b == 0 && t == 0) c->nvisit_fw = nf;
   if (scc) {
@@ -1011,15 +1252,19 @@ __global__ void __launch_bounds__(kBlock) k_reach(Args A) {
     B.m_cand = F.m_cand;
     B.root = pivot;
     B.q = w.x0;
+    B.minv = &c->minv[1];
     B.stat_slot = kStBwSteps;
-    const int nb = reach(B, A, w, sm, st, ty);
+    const int nb = reach<1>(B, A, w, sm, st, ty, pp);
     if (nb < 0) return;
     if (b == 0 && t == 0) c->nscc_fwbw = nb;
     hit = w.bvis;
+    hit_min = &c->minv[1];
   } else {
     if (b == 0 && t == 0) c->nscc_fwbw = nf;
     hit = w.fvis;
+    hit_min = &c->minv[0];
   }
+  const int32_t lab = A.p.canonical ? __ldcg(hit_min) : pivot;
   // label the component and take it out of the valid set (update_valid,
   // scc_fwbw.cpp:425-433)
   for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
@@ -1030,7 +1275,7 @@ __global__ void __launch_bounds__(kBlock) k_reach(Args A) {
       while (x) {
         const int bit = __ffs(x) - 1;
         x &= x - 1;
-        w.label[wd * 32 + bit] = pivot;
+        w.label[wd * 32 + bit] = lab;
       }
     }
   }
@@ -1038,27 +1283,29 @@ __global__ void __launch_bounds__(kBlock) k_reach(Args A) {
   if (!step_sync(c, st, 27)) return;
   const int32_t nv = __ldcg(&c->nvalid);
   for (long long i = (long long)b * T + t; i < nv; i += (long long)G * T) w.listA[i] = __ldcg(w.listB + i);
-  tally_flush(ty, c);
+  tally_flush(ty, c, kKReach);
   steps_close(c, st);
 }
 
 // ------------------------------------------------------------------------
-// k_colour: rounds of max-colour propagation until no vertex is left.
+// k_colour: rounds of colour propagation until no vertex is left.
 // SCC: each round propagates colours along out-edges to the fixed point;
 // every vertex whose colour is its own id is a root; a backward search over
 // same-colour vertices labels the root's SCC with the colour; the rest stay
 // for the next round (scc_color, scc_color.cpp:340-373).  The reference
 // hands the last <= vert_cutoff vertices to serial Tarjan; here the rounds
 // simply continue to the end.  WCC: one propagation over the union
-// adjacency; every vertex takes its colour (its component's largest id) as
-// label (cc_color_propagate, cc_color.cpp:47-175).
+// adjacency; every vertex takes its colour as label (cc_color_propagate,
+// cc_color.cpp:47-175).  Colours are minima (see ColourVisit), so a root is
+// the smallest id of its SCC and every label is canonical.
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_colour(Args A) {
-  __shared__ Smem sm;
-  Work& w = A.w;
+template <int NC>
+__device__ void colour_rounds(const Args& A, Smem& sm) {
+  Work w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5;
   const long long gt = (long long)b * T + t, gstride = (long long)G * T;
   Tally ty;
   if (ld_vol(&c->err)) return;
@@ -1072,6 +1319,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
   int32_t* L2 = w.listB;
   int32_t iter = 0;
   int rounds = 0;
+  long long labelled = 0;
   int32_t* bufs[2] = {w.x0, w.x1};
   int32_t* hl[2] = {w.h0, w.h1};
   const Tune& tn = A.p.tune;
@@ -1091,8 +1339,9 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
       for (;;) {
         if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 32); return; }
         const ColourVisit cv{w.vbits, w.colour, w.stamp, iter++};
-        const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, hl[hs ^ 1], w.n);
-        expand(front, nfront, hl[hs], nheavy, prop, cv, sk, tn, sm, c, ty);
+        const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, nullptr,
+                                  hl[hs ^ 1], w.n, 301);
+        expand<NC>(front, nfront, hl[hs], nheavy, prop, cv, sk, tn, sm, c, ty);
         stat_inc(c, kStColourSteps);
         if (!step_sync(c, st, 33)) return;
         const StepIn in = step_read(c, st.s);
@@ -1109,6 +1358,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
         const int32_t v = __ldcg(L + i);
         w.label[v] = __ldcg(w.colour + v);
       }
+      labelled += nl;
       nl = 0;
       ++rounds;
       break;
@@ -1116,7 +1366,15 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
     // roots: colour == own id (scc_color_get_roots, scc_color.cpp:179-201)
     const MarkVisit mv{w.vbits, w.done, w.colour, w.label};
     {
-      const Sink sk = sink_make(bufs[0], 0, w.n, step_out(c, st.s), false, nullptr, 0);
+      Out ro;
+      ro.arr = bufs[0];
+      ro.base = 0;
+      ro.cap = w.n;
+      ro.counter = &step_out(c, st.s)->count;
+      ro.edges = nullptr;
+      ro.minv = nullptr;
+      ro.where = 302;
+      Stage rs = stage_make(sm.stage[warp][0]);
       for (long long base = gt - (t & 31); base < nl; base += gstride) {
         const long long i = base + (t & 31);
         bool root = false;
@@ -1128,8 +1386,9 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
             root = true;
           }
         }
-        sink_append(root, v, sk, mv, c);
+        stage_push(rs, root, v, 0ull, ro, c);
       }
+      stage_flush(rs, ro, c);
       if (!step_sync(c, st, 34)) return;
     }
     // backward same-colour search from the roots
@@ -1139,8 +1398,9 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
         if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 35); return; }
         const StepIn in = step_read(c, st.s);
         if (in.count == 0 && in.huge == 0) break;
-        const Sink sk = sink_make(bufs[cur ^ 1], 0, w.n, step_out(c, st.s), false, hl[hs ^ 1], w.n);
-        expand(bufs[cur], in.count, hl[hs], in.huge, back, mv, sk, tn, sm, c, ty);
+        const Sink sk = sink_make(bufs[cur ^ 1], 0, w.n, step_out(c, st.s), false, nullptr,
+                                  hl[hs ^ 1], w.n, 303);
+        expand<1>(bufs[cur], in.count, hl[hs], in.huge, back, mv, sk, tn, sm, c, ty);
         stat_inc(c, kStMarkSteps);
         if (!step_sync(c, st, 36)) return;
         cur ^= 1;
@@ -1154,54 +1414,31 @@ __global__ void __launch_bounds__(kBlock) k_colour(Args A) {
     }
     if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 37, &c->nvalid, ty)) return;
     if (!step_sync(c, st, 38)) return;
-    nl = __ldcg(&c->nvalid);
+    const int32_t nn = __ldcg(&c->nvalid);
+    labelled += nl - nn;
+    nl = nn;
     int32_t* tmp = L;
     L = L2;
     L2 = tmp;
     ++rounds;
     stat_inc(c, kStColourRounds);
   }
-  if (b == 0 && t == 0) c->ncolour_rounds = rounds;
-  tally_flush(ty, c);
+  if (b == 0 && t == 0) {
+    c->ncolour_rounds = rounds;
+    c->ncolour = (int32_t)labelled;
+  }
+  tally_flush(ty, c, kKColour);
   steps_close(c, st);
 }
 
-// ------------------------------------------------------------------------
-// k_canon: label[v] <- min { u : label[u] == label[v] }.  rep[r] starts at r
-// (every representative is a member of its own component) and takes an
-// atomicMin from each member.  Also counts unassigned vertices.
-// ------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_canon(Args A) {
-  Work& w = A.w;
-  Ctl* c = w.ctl;
-  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
-  const long long gt = (long long)b * T + t, gs = (long long)G * T;
-  const int32_t n = A.g.n;
-  if (ld_vol(&c->err)) return;
-  Steps st = steps_open(c);
-  int32_t* rep = w.colour;
-  for (long long v = gt; v < n; v += gs) rep[v] = (int32_t)v;
-  if (!step_sync(c, st, 40)) return;
-  int un = 0;
-  for (long long v = gt; v < n; v += gs) {
-    const int32_t l = __ldcg(w.label + v);
-    if (l >= 0 && l < n) {
-      if (l != v) atomicMin(rep + l, (int32_t)v);
-    } else {
-      ++un;
-    }
-  }
-  for (int o = 16; o; o >>= 1) un += __shfl_xor_sync(kFull, un, o);
-  if (lane_id() == 0 && un) atomicAdd(&c->unassigned, un);
-  if (!step_sync(c, st, 41)) return;
-  for (long long v = gt; v < n; v += gs) {
-    const int32_t l = __ldcg(w.label + v);
-    if (l >= 0 && l < n) w.label[v] = __ldcg(rep + l);
-  }
-  steps_close(c, st);
+__global__ void __launch_bounds__(kBlock, 2) k_colour(Args A) {
+  __shared__ Smem sm;
+  if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
+  else colour_rounds<2>(A, sm);
 }
 
-// Unassigned count only (labels kept as produced).
+// Counts labels outside [0, n) (0 after a complete run); enqueued when the
+// caller asks for statistics.
 __global__ void k_count_unassigned(Args A) {
   Work& w = A.w;
   const int32_t n = A.g.n;
@@ -1227,8 +1464,8 @@ int max_coop_grid(int device) {
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   int best = 1 << 30;
-  const void* ks[] = {(const void*)k_trim, (const void*)k_reach, (const void*)k_colour,
-                      (const void*)k_canon};
+  const void* ks[] = {(const void*)k_trim, (const void*)k_reach<1>, (const void*)k_reach<2>,
+                      (const void*)k_colour};
   for (const void* k : ks) {
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, 0) != cudaSuccess) return 0;
@@ -1250,19 +1487,20 @@ cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p, con
   e = coop(k_trim, grid, a, stream);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], stream);
-  e = coop(k_reach, grid, a, stream);
+  // SCC and symmetric graphs walk one CSR per direction; WCC of a directed
+  // graph walks the union of both
+  e = (kind == kSCC || g.in.off == nullptr) ? coop(k_reach<1>, grid, a, stream)
+                                            : coop(k_reach<2>, grid, a, stream);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[2], stream);
   e = coop(k_colour, grid, a, stream);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[3], stream);
-  if (p.canonical) {
-    e = coop(k_canon, grid, a, stream);
-  } else {
+  if (p.count_unassigned) {
     k_count_unassigned<<<grid, kBlock, 0, stream>>>(a);
     e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
-  if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[4], stream);
   return cudaSuccess;
 }

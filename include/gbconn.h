@@ -73,7 +73,8 @@ typedef struct gb_opts {
                           the device colours every remaining vertex */
   int32_t t_block;     /* degree from which a block expands one vertex (512) */
   int32_t t_grid;      /* degree from which all blocks share one vertex (32768) */
-  int32_t k_pull;      /* in-edges one thread scans in a pull step (8) */
+  int32_t k_pull;      /* in-edges one thread scans in a pull step before the
+                          candidate moves to a warp (1..4, default 4) */
   float alpha;         /* push -> pull when frontier edges * alpha > unvisited
                           edges (15, the reference's ALPHA scc_main.cpp:64) */
   float beta;          /* pull -> push when frontier * beta < candidates
@@ -97,6 +98,10 @@ typedef struct gb_stats {
   int64_t vtx_reads;      /* vertex offset records read (8 B x 2 each) */
   int64_t edge_reads;     /* adjacency entries read (4 B each) */
   int64_t list_rw;        /* list entries read or written (4 B each) */
+  /* algorithmic bytes moved by each kernel (trim, reach, colour, canon):
+   * offset records x 16 + adjacency x 4 + list entries x 4 + the per-vertex
+   * arrays and bitmaps each kernel must read or write once */
+  int64_t bytes_trim, bytes_reach, bytes_colour, bytes_canon;
   int64_t trim_steps, fw_steps, bw_steps, pull_steps, colour_steps, mark_steps;
   int32_t grid_blocks;
   int32_t err_where;      /* device location code of a failure, 0 if none */
@@ -112,6 +117,17 @@ void* gb_ctx_stream(gb_ctx* ctx);
 /* Wait for all work queued on the context; returns the first device error
  * raised by any run since the last wait. */
 gb_status gb_ctx_sync(gb_ctx* ctx);
+/* Device times of the last `count` runs (count <= 64), oldest first, five
+ * values per run in milliseconds: trim, reach, colour, canon, total.  Waits
+ * for the context's stream.  Lets a caller time every kernel of a run of
+ * asynchronous calls. */
+gb_status gb_ctx_phase_times(gb_ctx* ctx, int32_t count, double* ms);
+/* Diagnostic: the step trace of the reachability phase of the context's
+ * last completed run, oldest first: device time (ns) at the start of each
+ * step's decision, vertices appended by the previous step, and mode bits
+ * (1: pull step, 2: heavy vertices pending, 4: backward search).  Writes up
+ * to cap entries and returns how many were written (0 on error). */
+int32_t gb_ctx_reach_trace(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* mode, int32_t cap);
 
 /* ---- graphs: create_csr (multistep/scc_main.cpp:127-191) --------------- */
 /* Device CSR build from an edge list (host or device arrays, m entries
@@ -174,7 +190,8 @@ gb_status gb_wcc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, cons
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
  * fields passed one by one and scc_maps owned by the caller (n ints).  Uses
- * a library-owned context on device 0.  avg_degree is accepted for parity;
+ * a library-owned context on the calling thread's current CUDA device
+ * (created at the first call) and keeps the graph's device buffers for reuse.  avg_degree is accepted for parity;
  * the direction switch uses exact edge counts. */
 gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_array,
                      const unsigned* out_degree_list, const unsigned* in_degree_list,

@@ -11,9 +11,10 @@ if ROOT not in sys.path:
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA path)")
     # build the library and the oracle once per session if they are missing
-    from connectivity_gb300 import build as b
-    if not os.path.exists(b.LIB) or not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
-        b.build()
+    import __graft_entry__
+    if not os.path.exists(os.path.join(ROOT, "connectivity_gb300", "libgbconn.so")) or \
+            not os.path.exists(os.path.join(ROOT, "oracle", "liboracle.so")):
+        __graft_entry__.build()
 
 
 @pytest.fixture(scope="session")

@@ -66,7 +66,7 @@ def test_reference_golden_vector(ctx):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "trim2", "tiers", "small_grid"])
+@pytest.mark.parametrize("variant", ["default", "trim2", "tiers", "pull_early", "small_grid"])
 def test_rmat_scc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -76,10 +76,11 @@ def test_rmat_scc(ctx, scale, ef, variant):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (14, 16), (16, 16), (18, 8)])
-def test_rmat_wcc(ctx, scale, ef):
+@pytest.mark.parametrize("variant", ["default", "pull_early"])
+def test_rmat_wcc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(g, o=gb.opts(**VARIANTS[variant])), _wcc_want(n, s, d))
 
 
 @pytest.mark.parametrize("side", [16, 64, 128])
