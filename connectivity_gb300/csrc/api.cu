@@ -37,6 +37,8 @@ struct gb_graph {
   int32_t* out_adj = nullptr;
   int64_t* in_off = nullptr;
   int32_t* in_adj = nullptr;
+  int32_t* hint_out = nullptr;  // pull hints (null for the drop-in staging graph)
+  int32_t* hint_in = nullptr;
 };
 
 namespace {
@@ -147,8 +149,22 @@ void graph_free(gb_graph* g) {
   cudaFree(g->out_adj);
   cudaFree(g->in_off);
   cudaFree(g->in_adj);
+  cudaFree(g->hint_out);
+  cudaFree(g->hint_in);
   g->out_off = g->in_off = nullptr;
   g->out_adj = g->in_adj = nullptr;
+  g->hint_out = g->hint_in = nullptr;
+}
+
+// Builds the pull hints of a graph whose CSR is complete on the device.
+gb_status graph_hints(gb_ctx* c, gb_graph* g) {
+  const size_t hb = (size_t)(g->n > 0 ? g->n : 1) * 4;
+  CK(cudaMalloc(&g->hint_out, hb), "hint allocation");
+  if (!g->symmetric) CK(cudaMalloc(&g->hint_in, hb), "hint allocation");
+  CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
+                     c->stream),
+     "hints");
+  return GB_OK;
 }
 
 gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
@@ -254,12 +270,12 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   gb::GraphView gv;
   gv.n = g->n;
   gv.m = g->m;
-  gv.out = {g->out_off, g->out_adj};
+  gv.out = {g->out_off, g->out_adj, g->hint_out};
   if (g->symmetric) {
     // a symmetric graph is its own reverse
-    gv.in = kind == gb::kSCC ? gv.out : gb::Csr{nullptr, nullptr};
+    gv.in = kind == gb::kSCC ? gv.out : gb::Csr{nullptr, nullptr, nullptr};
   } else {
-    gv.in = {g->in_off, g->in_adj};
+    gv.in = {g->in_off, g->in_adj, g->hint_in};
   }
   cudaStream_t sm = c->stream;
   CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
@@ -413,6 +429,11 @@ gb_status gb_ctx_phase_times(gb_ctx* c, int32_t count, double* ms) {
 }
 
 int32_t gb_ctx_reach_trace(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mode, int32_t cap) {
+  return gb_ctx_reach_trace2(c, t_ns, count, mode, nullptr, cap);
+}
+
+int32_t gb_ctx_reach_trace2(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mode,
+                            int64_t* extra, int32_t cap) {
   if (!c || cap < 0) return 0;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return 0;
   const gb::Ctl& h = *c->h_ctl;
@@ -424,6 +445,11 @@ int32_t gb_ctx_reach_trace(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mo
     if (t_ns) t_ns[i] = (int64_t)e.t;
     if (count) count[i] = e.count;
     if (mode) mode[i] = e.mode;
+    if (extra) {
+      extra[3 * i] = e.t_mid ? (int64_t)(e.t_mid - e.t) : 0;
+      extra[3 * i + 1] = e.nwarp;
+      extra[3 * i + 2] = e.nblock;
+    }
   }
   return k;
 }
@@ -462,6 +488,7 @@ gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* sr
   }
   cudaFree(ts);
   cudaFree(tt);
+  if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
     delete g;
@@ -510,6 +537,7 @@ gb_status gb_graph_from_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* out_
   if (s == GB_OK && !g->symmetric) s = upload(c, g->in_adj, in_adj, (size_t)m * 4);
   if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
   if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
+  if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
     delete g;
@@ -553,6 +581,7 @@ gb_status gb_graph_from_csr32(gb_ctx* c, int32_t n, uint32_t m, const int32_t* o
   g->symmetric = idl == nullptr;
   gb_status s = graph_alloc(g, !g->symmetric);
   if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl);
+  if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
     delete g;

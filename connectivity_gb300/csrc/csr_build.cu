@@ -115,6 +115,41 @@ __global__ void k_latch(const Ctl* c, int* sticky) {
   }
 }
 
+__global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t* in_off,
+                               int32_t* deg) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    long long d = out_off[v + 1] - out_off[v];
+    if (in_off) d += in_off[v + 1] - in_off[v];
+    deg[v] = (int32_t)(d < 0x7fffffffll ? d : 0x7fffffffll);
+  }
+}
+
+// One warp per vertex: the neighbour of largest degree, first one on ties.
+__global__ void k_hint(int32_t n, const int64_t* off, const int32_t* adj, const int32_t* deg,
+                       int32_t* hint) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+    const int64_t s = off[v], d = off[v + 1] - s;
+    int32_t best_d = -1;
+    int64_t best_e = -1;
+    for (int64_t e = lane; e < d; e += 32) {
+      const int32_t dd = deg[adj[s + e]];
+      if (dd > best_d) { best_d = dd; best_e = e; }
+    }
+    for (int o = 16; o; o >>= 1) {
+      const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
+      const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
+      if (d2 > best_d || (d2 == best_d && e2 >= 0 && (best_e < 0 || e2 < best_e))) {
+        best_d = d2;
+        best_e = e2;
+      }
+    }
+    if (lane == 0) hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
+  }
+}
+
 int bits_for(int32_t n) {
   int b = 1;
   while (b < 32 && (1ll << b) < (long long)n) ++b;
@@ -217,6 +252,24 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s) {
   k_latch<<<1, 1, 0, s>>>(ctl, sticky);
   return cudaGetLastError();
+}
+
+cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+                        const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
+                        int32_t* hint_in, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int32_t* deg = nullptr;
+  cudaError_t e = cudaMallocAsync(&deg, (size_t)n * 4, s);
+  if (e != cudaSuccess) return e;
+  k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
+  const int warp_grid = grid_for((int64_t)n * 32);
+  k_hint<<<warp_grid, 256, 0, s>>>(n, out_off, out_adj, deg, hint_out);
+  if (in_off != nullptr && hint_in != nullptr)
+    k_hint<<<warp_grid, 256, 0, s>>>(n, in_off, in_adj, deg, hint_in);
+  cudaFreeAsync(deg, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
 }
 
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s) {

@@ -8,8 +8,9 @@
 
 namespace gb {
 
-constexpr int kBlock = 512;               // threads per block, cooperative kernels
-constexpr int kWarps = kBlock / 32;
+constexpr int kBlock = 1024;              // threads per block, cooperative kernels
+constexpr int kMinBlocks = 1024 / kBlock; // resident blocks per SM (64 registers)
+constexpr int kWarps = kBlock / 32;       // <= 32 (block scans use one warp)
 constexpr int kBlkList = 128;             // per-block list of large vertices
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -24,6 +25,8 @@ enum : int {
 struct Csr {
   const int64_t* off;   // n + 1 offsets
   const int32_t* adj;   // neighbour ids
+  const int32_t* hint;  // per vertex, the neighbour of largest total degree
+                        // (-1: none), or null
 };
 
 // Counters filled during one step and read by every block after the
@@ -78,8 +81,11 @@ struct Ctl {
   // time at the end of the step, vertices appended, mode (1 = pull).
   struct Trace {
     unsigned long long t;
+    unsigned long long t_mid;   // pull steps: end of the thread tier
     int32_t count;
     int32_t mode;
+    int32_t nwarp;              // pull steps: warp-tier candidates
+    int32_t nblock;             // pull steps: block-tier candidates
   } trace[128];
   int32_t ntrace;
   int32_t pad2;
@@ -170,6 +176,11 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
 // unless an earlier one is already there.
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
+// Pull hints: for every vertex, its neighbour of largest total degree in
+// each CSR (hint_in may be null when in_off is).  Synchronises the stream.
+cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+                        const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
+                        int32_t* hint_in, cudaStream_t s);
 // Seeded R-MAT edge list on the device, sorted by (src, dst), without
 // self-loops and duplicates; *d_src / *d_dst are cudaMallocAsync'd.
 cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat_thr thr,

@@ -62,6 +62,19 @@ __device__ __forceinline__ bool bit_claim(uint32_t* bm, int32_t v) {
   const uint32_t b = 1u << (v & 31);
   return (atomicOr(bm + (v >> 5), b) & b) == 0u;
 }
+// L1-cacheable read for checks that tolerate a value from earlier in the
+// same step (a stale "not set" only costs work: the atomic that follows, or
+// the next step, settles it).  Values written before the last grid barrier
+// are seen: the barrier's acquire by the block's first thread invalidates
+// the SM's L1.
+__device__ __forceinline__ bool bit_get_l1(const uint32_t* bm, int32_t v) {
+  return (bm[v >> 5] >> (v & 31)) & 1u;
+}
+// Fire-and-forget set (RED): for bits only one thread can be setting.
+__device__ __forceinline__ void bit_set_red(uint32_t* bm, int32_t v) {
+  asm volatile("red.relaxed.gpu.global.or.b32 [%0], %1;" ::"l"(bm + (v >> 5)), "r"(1u << (v & 31))
+               : "memory");
+}
 __device__ __forceinline__ bool bit_release(uint32_t* bm, int32_t v) {
   const uint32_t b = 1u << (v & 31);
   return (atomicAnd(bm + (v >> 5), ~b) & b) != 0u;
@@ -582,8 +595,8 @@ struct ReachVisit {
   __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
   __device__ __forceinline__ bool edge(int32_t, int32_t w, int, bool act) const {
     if (!act) return false;
-    if (bit_get(vis, w)) return false;
-    if (!bit_get(allow, w)) return false;
+    if (bit_get_l1(vis, w)) return false;
+    if (!bit_get_l1(allow, w)) return false;
     return bit_claim(vis, w);
   }
   __device__ __forceinline__ unsigned long long weight(int32_t w) const {
@@ -725,7 +738,7 @@ __device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsign
   return k2 > k || (k2 == k && v2 >= 0 && (v < 0 || v2 < v));
 }
 
-__global__ void __launch_bounds__(kBlock, 2) k_trim(Args A) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   __shared__ Smem sm;
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -1008,26 +1021,38 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
       v[j] = i < ncur ? __ldcg(cand_cur + i) : -1;
     }
 #pragma unroll
-    for (int j = 0; j < kPullU; ++j) unv[j] = v[j] >= 0 && !bit_get(R.vis, v[j]);
+    for (int j = 0; j < kPullU; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
+    // the hint (the neighbour of largest degree) settles most candidates
+    // without touching the CSR
+    bool hinted[kPullU];
+#pragma unroll
+    for (int j = 0; j < kPullU; ++j) {
+      int32_t h0 = -1, h1 = -1;
+      if (unv[j] && R.pull.c[0].hint != nullptr) h0 = __ldg(R.pull.c[0].hint + v[j]);
+      if constexpr (NC > 1) {
+        if (unv[j] && R.pull.c[1].hint != nullptr) h1 = __ldg(R.pull.c[1].hint + v[j]);
+      }
+      hinted[j] = (h0 >= 0 && bit_get_l1(R.vis, h0)) || (h1 >= 0 && bit_get_l1(R.vis, h1));
+    }
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) {
       s0[j] = d0[j] = s1[j] = d1[j] = 0;
-      if (unv[j]) rec_load<NC>(R.pull, v[j], s0[j], d0[j], s1[j], d1[j]);
+      if (unv[j] && !hinted[j]) rec_load<NC>(R.pull, v[j], s0[j], d0[j], s1[j], d1[j]);
     }
     // first edge of every candidate, then the next kt-1 of those still open
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) {
       u[j][0] = -1;
-      if (unv[j] && d0[j] + d1[j] > 0) {
+      if (unv[j] && !hinted[j] && d0[j] + d1[j] > 0) {
         int k;
         u[j][0] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], 0, k);
       }
     }
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) {
-      found[j] = u[j][0] >= 0 && bit_get(R.vis, u[j][0]);
+      found[j] = hinted[j] || (u[j][0] >= 0 && bit_get_l1(R.vis, u[j][0]));
       if (v[j] >= 0) ty.list++;
-      if (unv[j]) {
+      if (unv[j] && !hinted[j]) {
         ty.vtx += NC;
         if (u[j][0] >= 0) ty.edges++;
       }
@@ -1050,7 +1075,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
       for (int e = 1; e < kPullThread; ++e) {
         if (u[j][e] >= 0) {
           ty.edges++;
-          if (!found[j] && bit_get(R.vis, u[j][e])) found[j] = true;
+          if (!found[j] && bit_get_l1(R.vis, u[j][e])) found[j] = true;
         }
       }
       const long long d = d0[j] + d1[j];
@@ -1061,8 +1086,9 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
     }
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) {
-      const bool f = found[j] && bit_claim(R.vis, v[j]);
-      stage_push(sf, f, v[j], 0ull, of, c);
+      // a pull candidate has one owner: its bit is set without a reply
+      if (found[j]) bit_set_red(R.vis, v[j]);
+      stage_push(sf, found[j], v[j], 0ull, of, c);
       stage_push(sk, keep[j], v[j], 0ull, ok, c);
       list_append(to_warp[j], v[j], wl, &lc[0], w.n, c, 204);
       list_append(to_block[j], v[j], bl, &lc[1], w.n, c, 205);
@@ -1071,6 +1097,12 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   // the warp and block tiers need the complete lists
   if (!grid_barrier(c, 206)) return false;
   const int32_t nwl = __ldcg(&lc[0]), nbl = __ldcg(&lc[1]);
+  if (b == 0 && t == 0 && c->ntrace > 0) {
+    auto& tr = c->trace[(c->ntrace - 1) % kTrace];
+    tr.t_mid = gtimer();
+    tr.nwarp = nwl;
+    tr.nblock = nbl;
+  }
   for (long long j = (long long)b * (T >> 5) + warp; j < nwl; j += nw) {
     const int32_t v = __ldcg(wl + j);
     long long s0, d0, s1, d1;
@@ -1084,15 +1116,15 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
         int k;
         const int32_t x = adj_at<NC>(R.pull, s0, d0, s1, e, k);
         ty.edges++;
-        hit = bit_get(R.vis, x);
+        hit = bit_get_l1(R.vis, x);
       }
       if (__any_sync(kFull, hit)) {
         found = true;
         break;
       }
     }
-    const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
-    stage_push(sf, f, v, 0ull, of, c);
+    if (found && lane == 0) bit_set_red(R.vis, v);
+    stage_push(sf, found && lane == 0, v, 0ull, of, c);
     stage_push(sk, !found && lane == 0, v, 0ull, ok, c);
   }
   for (long long j = b; j < nbl; j += G) {
@@ -1108,7 +1140,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
         int k;
         const int32_t x = adj_at<NC>(R.pull, s0, d0, s1, e, k);
         ty.edges++;
-        hit = bit_get(R.vis, x);
+        hit = bit_get_l1(R.vis, x);
       }
       if (__syncthreads_or(hit)) {
         found = true;
@@ -1116,8 +1148,8 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
       }
     }
     if (warp == 0) {
-      const bool f = (found && lane == 0) ? bit_claim(R.vis, v) : false;
-      stage_push(sf, f, v, 0ull, of, c);
+      if (found && lane == 0) bit_set_red(R.vis, v);
+      stage_push(sf, found && lane == 0, v, 0ull, of, c);
       stage_push(sk, !found && lane == 0, v, 0ull, ok, c);
     }
   }
@@ -1178,6 +1210,9 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
     if (b == 0 && t == 0) {
       const int ti = c->ntrace % kTrace;
       c->trace[ti].t = gtimer();
+      c->trace[ti].t_mid = 0;
+      c->trace[ti].nwarp = 0;
+      c->trace[ti].nblock = 0;
       c->trace[ti].count = in.count;
       c->trace[ti].mode = (pull ? 1 : 0) | (in.huge > 0 ? 2 : 0) | (R.stat_slot == kStBwSteps ? 4 : 0);
       c->ntrace++;
@@ -1209,7 +1244,7 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
 // adjacency (cc_bfs, cc_bfs.cpp:217-291).
 // ------------------------------------------------------------------------
 template <int NC>
-__global__ void __launch_bounds__(kBlock, 2) k_reach(Args A) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   __shared__ Smem sm;
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -1431,7 +1466,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   steps_close(c, st);
 }
 
-__global__ void __launch_bounds__(kBlock, 2) k_colour(Args A) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_colour(Args A) {
   __shared__ Smem sm;
   if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
   else colour_rounds<2>(A, sm);

@@ -128,6 +128,11 @@ gb_status gb_ctx_phase_times(gb_ctx* ctx, int32_t count, double* ms);
  * (1: pull step, 2: heavy vertices pending, 4: backward search).  Writes up
  * to cap entries and returns how many were written (0 on error). */
 int32_t gb_ctx_reach_trace(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* mode, int32_t cap);
+/* As gb_ctx_reach_trace, plus three values per step in extra (3 x cap):
+ * for pull steps, ns from the step's start to the end of its thread tier,
+ * and the lengths of its warp- and block-tier candidate lists. */
+int32_t gb_ctx_reach_trace2(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* mode,
+                            int64_t* extra, int32_t cap);
 
 /* ---- graphs: create_csr (multistep/scc_main.cpp:127-191) --------------- */
 /* Device CSR build from an edge list (host or device arrays, m entries

@@ -1,0 +1,138 @@
+"""Host side of libgbconn without a GPU: the C ABI loads and exports every
+declared symbol, the reader / writer / verify / generator functions behave,
+and the compute entry points fail loudly instead of falling back to the CPU."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import connectivity_gb300 as gb
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gbconn.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(gb.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings():
+    lib = ctypes.CDLL(gb.LIB_PATH)
+    lib.gb_status_string.restype = ctypes.c_char_p
+    assert lib.gb_status_string(0) == b"ok"
+    assert lib.gb_status_string(4) == b"device wait timed out"
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU behaviour")
+def test_no_cpu_fallback_without_gpu():
+    with pytest.raises(gb.GBError) as e:
+        gb.Context(0)
+    assert e.value.status in (2, 7, 8)
+
+
+def test_read_edge_and_errors(tmp_path):
+    p = tmp_path / "g.txt"
+    p.write_text("4 3\n0 1\n1  2\n3 0\n")
+    n, s, d = gb.read_edge(str(p))
+    assert n == 4 and s.tolist() == [0, 1, 3] and d.tolist() == [1, 2, 0]
+    p.write_text("4 3\n0 1\n1 9\n3 0\n")
+    with pytest.raises(gb.GBError) as e:
+        gb.read_edge(str(p))
+    assert e.value.status == 1  # id out of range
+    p.write_text("4 3\n0 1\n")
+    with pytest.raises(gb.GBError) as e:
+        gb.read_edge(str(p))
+    assert e.value.status == 6  # truncated
+    with pytest.raises(gb.GBError) as e:
+        gb.read_edge(str(tmp_path / "missing.txt"))
+    assert e.value.status == 6
+
+
+def test_output_labels(tmp_path):
+    p = tmp_path / "out.txt"
+    gb.output_labels(str(p), np.array([0, 0, 2, -1], np.int32))
+    assert p.read_text() == "0\n0\n2\n-1\n"
+
+
+def test_verify_lines():
+    lab = np.array([0, 0, 2, 3, 3, 3, -1], np.int32)
+    assert gb.scc_verify(lab) == "Num SCCs: 3, Nontrivial: 2, Max SCC: 3, Unassigned 1\n"
+    assert gb.cc_verify(lab) == "Num CCs: 3, Max CC: 3, Unassigned 1\n"
+    assert oracle.stats(lab) == (3, 2, 3, 1)
+
+
+def test_canonicalize():
+    lab = np.array([5, 5, 2, 5, 2, 7, 7, 7], np.int32)
+    assert gb.canonicalize(lab).tolist() == [0, 0, 2, 0, 2, 5, 5, 5]
+
+
+def test_rmat_generator_properties():
+    n, s, d = gb.rmat_edges(12, 16, 1)
+    assert n == 4096
+    n2, s2, d2 = gb.rmat_edges(12, 16, 1)
+    assert np.array_equal(s, s2) and np.array_equal(d, d2)
+    assert not np.any(s == d)
+    key = s.astype(np.int64) * n + d
+    assert np.all(np.diff(key) > 0)  # sorted by (src, dst), no duplicates
+    assert s.size > 0.7 * 16 * n
+    # seed changes the graph
+    _, s3, _ = gb.rmat_edges(12, 16, 2)
+    assert s3.size != s.size or not np.array_equal(s3, s)
+
+
+def test_grid_generator_properties():
+    side = 50
+    n, s, d = gb.grid_edges(side, 250, 64, 2)
+    assert n == side * side + 250
+    lattice = (s < side * side) & (d < side * side)
+    # lattice edges join horizontal or vertical neighbours only
+    ds = np.abs(s[lattice].astype(np.int64) - d[lattice])
+    assert set(np.unique(ds)) <= {1, side}
+    # every chain vertex has exactly one in- or one out-edge to the rest
+    assert s.size == np.count_nonzero(lattice) + 250
+    # about 3/4 of the 2*side*(side-1) lattice pairs carry 1.33 arcs on average
+    pairs = 2 * side * (side - 1)
+    assert 0.8 * pairs < np.count_nonzero(lattice) < 1.2 * pairs
+
+
+def test_batch_sizes_deterministic_and_clipped():
+    ns, efs, seeds = gb.batch_sizes(20000, seed=4)
+    ns2, efs2, seeds2 = gb.batch_sizes(20000, seed=4)
+    assert np.array_equal(ns, ns2) and np.array_equal(efs, efs2) and np.array_equal(seeds, seeds2)
+    assert ns.min() >= 64 and ns.max() <= 500_000
+    assert efs.min() >= 4 and efs.max() <= 32
+    med = np.median(ns)
+    assert 1500 < med < 2700
+    assert 0.10 < np.mean(ns > 10_000) < 0.20
+
+
+def test_cli_usage_without_arguments():
+    for tool in ("scc", "cc"):
+        exe = os.path.join(ROOT, "connectivity_gb300", "bin", tool)
+        r = subprocess.run([exe], capture_output=True, text=True)
+        assert r.returncode == 0
+        assert r.stdout == f"Usage: {exe} [graph] [optional: output file]\n"

@@ -1,0 +1,103 @@
+"""The oracle (oracle/multistep.c) pinned against the reference: its golden
+vector, the golden fixtures produced by the unmodified reference code
+(tests/golden/, see make_golden.py), and -- where the reference tree is
+present -- the reference harness itself.  CPU only."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+import connectivity_gb300 as gb
+import oracle
+from tests import graphs
+from tests.golden.make_golden import cases, digest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+INDEX = json.load(open(os.path.join(GOLD, "index.json")))
+CASES = list(cases())
+
+
+def test_reference_golden_vector():
+    # multistep/test.graph: SCC {0,1},{2}, CC one component; canonical labels
+    # 0 0 2 and 0 0 0 (the reference prints exactly these)
+    n, s, d = graphs.test_graph()
+    assert oracle.scc(oracle.CpuGraph(n, s, d)).tolist() == [0, 0, 2]
+    assert oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)).tolist() == [0, 0, 0]
+    assert INDEX["test_graph_text"]["scc"] == [0, 0, 2]
+    assert INDEX["test_graph_text"]["cc"] == [0, 0, 0]
+
+
+def test_text_reader_on_reference_fixture():
+    n, s, d = gb.read_edge(os.path.join(GOLD, "test_graph.txt"))
+    n2, s2, d2 = graphs.test_graph()
+    assert n == n2 and s.tolist() == s2.tolist() and d.tolist() == d2.tolist()
+    lab = oracle.scc(oracle.CpuGraph(n, s, d))
+    assert gb.scc_verify(lab) == INDEX["test_graph_text"]["scc_verify"]
+    assert gb.cc_verify(oracle.cc(oracle.CpuGraph(n, s, d, mirror=True))) == \
+        INDEX["test_graph_text"]["cc_verify"]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_oracle_matches_reference_fixture(case):
+    name, (n, s, d) = case
+    ent = INDEX[name]
+    assert digest(n, s, d) == ent["digest"], "generator output changed"
+    gold = np.load(os.path.join(GOLD, f"{name}.npz"))
+    scc = oracle.scc(oracle.CpuGraph(n, s, d))
+    assert np.array_equal(scc, gold["scc"])
+    assert gb.scc_verify(scc) == ent["scc_verify"]
+    cc = oracle.cc(oracle.CpuGraph(n, s, d, mirror=True))
+    assert np.array_equal(cc, gold["cc"])
+    assert gb.cc_verify(cc) == ent["cc_verify"]
+
+
+@pytest.mark.parametrize("case", CASES[:9], ids=[c[0] for c in CASES[:9]])
+def test_oracle_variants_agree(case):
+    name, (n, s, d) = case
+    g = oracle.CpuGraph(n, s, d)
+    base = oracle.scc(g)
+    # fixed-point trim, no serial step, and an independent Tarjan
+    assert np.array_equal(oracle.scc(g, trim_level=2), base)
+    assert np.array_equal(oracle.scc(g, vert_cutoff=0), base)
+    assert np.array_equal(oracle.tarjan(g), base)
+
+
+@pytest.mark.parametrize("case", CASES[:9], ids=[c[0] for c in CASES[:9]])
+def test_oracle_against_scipy(case):
+    sp = pytest.importorskip("scipy.sparse")
+    csg = pytest.importorskip("scipy.sparse.csgraph")
+    name, (n, s, d) = case
+    a = sp.csr_matrix((np.ones(s.size, np.int8), (s, d)), shape=(n, n))
+    _, lab = csg.connected_components(a, directed=True, connection="strong")
+    assert np.array_equal(oracle.canonical(lab.astype(np.int32)),
+                          oracle.scc(oracle.CpuGraph(n, s, d)))
+    _, lab = csg.connected_components(a, directed=True, connection="weak")
+    assert np.array_equal(oracle.canonical(lab.astype(np.int32)),
+                          oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)))
+
+
+def test_pivot_rules():
+    # SCC pivot: lowest id of maximum out*in (scc_main.cpp:169-182)
+    n, s, d = 4, np.array([0, 1, 1, 2, 3, 3, 0], np.int32), np.array([1, 0, 2, 1, 0, 1, 3], np.int32)
+    g = oracle.CpuGraph(n, s, d)
+    # out: 0:2 1:2 2:1 3:2; in: 0:2 1:3 2:1 3:1 -> products 4 6 1 2
+    assert g.pivot_scc()[0] == 1
+    # cc pivot: lowest id of maximum mirrored degree (cc_main.cpp:148-160)
+    gm = oracle.CpuGraph(n, s, d, mirror=True)
+    assert gm.pivot_cc()[0] == 1
+    # no positive product -> no pivot
+    g0 = oracle.CpuGraph(3, np.array([0, 0], np.int32), np.array([1, 2], np.int32))
+    assert g0.pivot_scc()[0] == -1
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("seed", [5, 6])
+def test_oracle_against_live_reference(seed):
+    n, s, d = gb.rmat_edges(13, 8, seed)
+    raw, line, _ = oracle.ref_run("scc", n, s, d, threads=4)
+    assert np.array_equal(oracle.canonical(raw), oracle.scc(oracle.CpuGraph(n, s, d)))
+    raw, line, _ = oracle.ref_run("cc", n, s, d, threads=4)
+    assert np.array_equal(oracle.canonical(raw), oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)))
