@@ -97,6 +97,7 @@ _sig("gb_ctx_sync", C.c_int32, [_P])
 _sig("gb_ctx_phase_times", C.c_int32, [_P, C.c_int32, _P])
 _sig("gb_ctx_reach_trace", C.c_int32, [_P, _P, _P, _P, C.c_int32])
 _sig("gb_ctx_reach_trace2", C.c_int32, [_P, _P, _P, _P, _P, C.c_int32])
+_sig("gb_ctx_block_times", C.c_int32, [_P, _P, C.c_int32])
 _sig("gb_graph_from_edges", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, C.POINTER(_P)])
 _sig("gb_graph_from_csr", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, _P, _P, C.POINTER(_P)])
 _sig("gb_graph_from_csr32", C.c_int32, [_P, C.c_int32, C.c_uint32, _P, _P, _P, _P, C.POINTER(_P)])
@@ -283,6 +284,13 @@ class Context:
         k = _lib.gb_ctx_reach_trace2(self._h, _ptr(t), _ptr(cnt), _ptr(mode), _ptr(ex), cap)
         return [(int(t[i]), int(cnt[i]), int(mode[i]), int(ex[3 * i]), int(ex[3 * i + 1]),
                  int(ex[3 * i + 2])) for i in range(k)]
+
+    def block_times(self) -> np.ndarray:
+        """Per block, device ns at which it finished the thread tier of the
+        first pull step of the last run."""
+        t = np.zeros(256, np.int64)
+        k = _lib.gb_ctx_block_times(self._h, _ptr(t), 256)
+        return t[:k]
 
     def phase_times(self, count: int) -> np.ndarray:
         """(count, 5) ms of the last runs: trim, reach, colour, canon, total."""

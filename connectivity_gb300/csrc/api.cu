@@ -432,6 +432,14 @@ int32_t gb_ctx_reach_trace(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mo
   return gb_ctx_reach_trace2(c, t_ns, count, mode, nullptr, cap);
 }
 
+int32_t gb_ctx_block_times(gb_ctx* c, int64_t* t_ns, int32_t cap) {
+  if (!c || !t_ns || cap < 0) return 0;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return 0;
+  const int k = cap < gb::kBlkTimes ? cap : gb::kBlkTimes;
+  for (int i = 0; i < k; ++i) t_ns[i] = (int64_t)c->h_ctl->blk_t[i];
+  return k;
+}
+
 int32_t gb_ctx_reach_trace2(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* mode,
                             int64_t* extra, int32_t cap) {
   if (!c || cap < 0) return 0;

@@ -89,8 +89,12 @@ struct Ctl {
   } trace[128];
   int32_t ntrace;
   int32_t pad2;
+  // Diagnostic: device time at which each block finished the thread tier of
+  // the first pull step of the run.
+  unsigned long long blk_t[256];
 };
 constexpr int kTrace = 128;
+constexpr int kBlkTimes = 256;
 
 enum KernelId : int { kKTrim = 0, kKReach = 1, kKColour = 2, kKCanon = 3 };
 

@@ -318,7 +318,10 @@ __device__ __forceinline__ Adj adj_undirected(const GraphView& g) {
 // moves them to the global list in one atomic + coalesced copy per kWB
 // entries, which keeps the step counters (a single L2 word) cool.
 // ------------------------------------------------------------------------
-constexpr int kWB = 128;
+constexpr int kWB = 512;
+// Dynamic shared memory of the cooperative kernels: two staging buffers per
+// warp.
+constexpr int kDynSmem = kWarps * 2 * kWB * 4;
 
 // A global output list.
 struct Out {
@@ -418,8 +421,12 @@ struct Smem {
   int warp_tmp[kWarps + 1];
   long long red_l[kWarps];
   int red_i[kWarps];
-  int32_t stage[kWarps][2][kWB];
+  int32_t* stage_base;  // dynamic shared memory, kWarps x 2 x kWB entries
+  __device__ __forceinline__ int32_t* stage(int warp, int k) {
+    return stage_base + (warp * 2 + k) * kWB;
+  }
 };
+extern __shared__ __align__(16) int32_t g_dyn_smem[];
 
 // Output of one expansion step: the main list and the heavy list.
 struct Sink {
@@ -474,7 +481,7 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
                        Ctl* c, Tally& ty) {
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
-  Stage st = stage_make(sm.stage[warp][0]);
+  Stage st = stage_make(sm.stage(warp, 0));
   const bool small = nfront <= kSmallFront;
   // (1) heavy vertices deferred by the previous step, and a small frontier:
   // block b takes slice b of each vertex's edges
@@ -740,6 +747,7 @@ __device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsign
 
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   __shared__ Smem sm;
+  sm.stage_base = g_dyn_smem;
   Work& w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -757,7 +765,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   unsigned long long mc = 0ull;
   int removed = 0;
   const TrimVisit tv{w.vbits, w.live_in, w.live_out, w.label};
-  Stage rs = stage_make(sm.stage[warp][0]);
+  Stage rs = stage_make(sm.stage(warp, 0));
   Out ro;
   ro.arr = w.x0;
   ro.base = 0;
@@ -1004,13 +1012,17 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   ok.edges = nullptr;
   ok.minv = nullptr;
   ok.where = 203;
-  Stage sf = stage_make(sm.stage[warp][0]);
-  Stage sk = stage_make(sm.stage[warp][1]);
+  Stage sf = stage_make(sm.stage(warp, 0));
+  Stage sk = stage_make(sm.stage(warp, 1));
   int32_t* wl = w.x1;  // warp-tier list
   int32_t* bl = w.h1;  // block-tier list
   const long long nw = (long long)G * (T >> 5);
-  for (long long base = ((long long)b * (T >> 5) + warp) * 32 * kPullU; base < ncur;
-       base += nw * 32 * kPullU) {
+  // block b streams through its own contiguous share of the candidates
+  constexpr long long kGroup = 32 * kPullU;
+  const long long chunk = ((ncur + G - 1) / G + kGroup - 1) / kGroup * kGroup;
+  const long long clo = chunk * b < ncur ? chunk * b : ncur;
+  const long long chi = clo + chunk < ncur ? clo + chunk : ncur;
+  for (long long base = clo + warp * kGroup; base < chi; base += (T >> 5) * kGroup) {
     int32_t v[kPullU];
     bool unv[kPullU], found[kPullU];
     long long s0[kPullU], d0[kPullU], s1[kPullU], d1[kPullU];
@@ -1018,7 +1030,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) {
       const long long i = base + j * 32 + lane;
-      v[j] = i < ncur ? __ldcg(cand_cur + i) : -1;
+      v[j] = i < chi ? __ldcg(cand_cur + i) : -1;
     }
 #pragma unroll
     for (int j = 0; j < kPullU; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
@@ -1094,6 +1106,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
       list_append(to_block[j], v[j], bl, &lc[1], w.n, c, 205);
     }
   }
+  if (pp == 0 && t == 0 && b < kBlkTimes) c->blk_t[b] = gtimer();
   // the warp and block tiers need the complete lists
   if (!grid_barrier(c, 206)) return false;
   const int32_t nwl = __ldcg(&lc[0]), nbl = __ldcg(&lc[1]);
@@ -1246,6 +1259,7 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
 template <int NC>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   __shared__ Smem sm;
+  sm.stage_base = g_dyn_smem;
   Work& w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -1409,7 +1423,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
       ro.edges = nullptr;
       ro.minv = nullptr;
       ro.where = 302;
-      Stage rs = stage_make(sm.stage[warp][0]);
+      Stage rs = stage_make(sm.stage(warp, 0));
       for (long long base = gt - (t & 31); base < nl; base += gstride) {
         const long long i = base + (t & 31);
         bool root = false;
@@ -1468,6 +1482,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
 
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_colour(Args A) {
   __shared__ Smem sm;
+  sm.stage_base = g_dyn_smem;
   if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
   else colour_rounds<2>(A, sm);
 }
@@ -1490,7 +1505,8 @@ __global__ void k_count_unassigned(Args A) {
 template <class K>
 cudaError_t coop(K kern, int grid, const Args& a, cudaStream_t s) {
   void* params[] = {const_cast<Args*>(&a)};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kBlock), params, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kBlock), params,
+                                     (size_t)kDynSmem, s);
 }
 
 }  // namespace
@@ -1502,8 +1518,12 @@ int max_coop_grid(int device) {
   const void* ks[] = {(const void*)k_trim, (const void*)k_reach<1>, (const void*)k_reach<2>,
                       (const void*)k_colour};
   for (const void* k : ks) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem) !=
+        cudaSuccess)
+      return 0;
     int per = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, 0) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, kDynSmem) != cudaSuccess)
+      return 0;
     if (per < best) best = per;
   }
   if (best < 1) return 0;

@@ -133,6 +133,10 @@ int32_t gb_ctx_reach_trace(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* 
  * and the lengths of its warp- and block-tier candidate lists. */
 int32_t gb_ctx_reach_trace2(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* mode,
                             int64_t* extra, int32_t cap);
+/* Diagnostic: device time (ns) at which each block of the last completed run
+ * finished the thread tier of its first pull step (0 for blocks that did
+ * not run one).  Returns the number of entries written (<= 256). */
+int32_t gb_ctx_block_times(gb_ctx* ctx, int64_t* t_ns, int32_t cap);
 
 /* ---- graphs: create_csr (multistep/scc_main.cpp:127-191) --------------- */
 /* Device CSR build from an edge list (host or device arrays, m entries
