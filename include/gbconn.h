@@ -195,6 +195,24 @@ gb_status gb_cc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts* 
 gb_status gb_scc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, const gb_opts* opts);
 gb_status gb_wcc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, const gb_opts* opts);
 
+/* SCC labels without any device allocation.  No counterpart in the
+ * reference.  For callers that may not call cudaMalloc (code inside a
+ * framework's memory pool, plug-ins whose host process has reserved or capped
+ * device memory, loops that cannot take an allocation's latency or failure):
+ * the run's scratch is a fixed static device array inside the library (about
+ * 15 MB, held by every GPU that loads the library until exit).  The CSR
+ * (out_off/in_off n+1 entries, out_adj/in_adj m entries) and labels (n
+ * entries, canonical minimum member ids) are device memory owned by the
+ * caller; the work goes on `stream` (NULL: the legacy default stream) and
+ * the call returns after it completes.  At most 262144 vertices (more:
+ * GB_ERR_CAPACITY, nothing queued).  All calls share the scratch: calls that
+ * overlap on the GPU race and must be serialised.  The first call on a
+ * device sets that device up (symbol address, kernel attributes); make it
+ * before any stream capture. */
+gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
+                         const int64_t* in_off, const int32_t* in_adj, int32_t* labels,
+                         void* stream);
+
 /* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
