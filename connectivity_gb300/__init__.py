@@ -103,7 +103,19 @@ _sig("gb_graph_from_csr", C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, _P, _P, 
 _sig("gb_graph_from_csr32", C.c_int32, [_P, C.c_int32, C.c_uint32, _P, _P, _P, _P, C.POINTER(_P)])
 _sig("gb_graph_rmat", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
                                   C.c_double, C.POINTER(_P)])
+_sig("gb_graph_rmat_n", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                    C.c_double, C.POINTER(_P)])
 _sig("gb_graph_info", C.c_int32, [_P, _I32P, _I64P, _I32P])
+_sig("gb_batch_from_edges", C.c_int32, [_P, C.c_int32, _P, C.c_int64, _P, _P, C.POINTER(_P)])
+_sig("gb_batch_rmat", C.c_int32, [_P, C.c_int32, _P, _P, _P, C.c_double, C.c_double, C.c_double,
+                                  C.POINTER(_P)])
+_sig("gb_batch_info", C.c_int32, [_P, _I32P, _I64P, _I64P])
+_sig("gb_batch_vbase", C.c_int32, [_P, _P])
+_sig("gb_batch_graph", C.c_int32, [_P, C.POINTER(_P)])
+for _n in ("gb_batch_scc", "gb_batch_wcc"):
+    _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
+_sig("gb_batch_scc_async", C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
+_sig("gb_batch_destroy", C.c_int32, [_P])
 _sig("gb_graph_csr_to_host", C.c_int32, [_P, _P, _P, _P, _P])
 _sig("gb_graph_device_csr", C.c_int32, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
                                         C.POINTER(_P)])
@@ -123,6 +135,8 @@ _sig("gb_cc_verify", C.c_int32, [C.c_int32, _P, C.c_char_p, C.c_size_t, _I64P])
 _sig("gb_canonicalize", C.c_int32, [C.c_int32, _P])
 _sig("gb_rmat_edges_host", C.c_int32, [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
                                        C.c_double, _I64P, C.POINTER(_P), C.POINTER(_P)])
+_sig("gb_rmat_edges_host_n", C.c_int32, [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                         C.c_double, _I64P, C.POINTER(_P), C.POINTER(_P)])
 _sig("gb_grid_edges_host", C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _I32P, _I64P,
                                        C.POINTER(_P), C.POINTER(_P)])
 _sig("gb_batch_sizes", C.c_int32, [C.c_int32, C.c_uint64, C.c_double, C.c_double, C.c_int32,
@@ -208,6 +222,17 @@ def rmat_edges(scale: int, edge_factor: int = 16, seed: int = 1,
     _check(_lib.gb_rmat_edges_host(scale, edge_factor, seed, abc[0], abc[1], abc[2], C.byref(m),
                                    C.byref(s), C.byref(d)), "rmat_edges")
     return 1 << scale, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
+
+
+def rmat_edges_n(n: int, edge_factor: int, seed: int,
+                 abc: tuple[float, float, float] = RMAT_ABC) -> tuple[int, np.ndarray, np.ndarray]:
+    """R-MAT on any n (the batch rule): edge_factor*n candidates at scale
+    ceil(log2 n), ids >= n dropped.  Returns (n, src, dst)."""
+    m = C.c_int64()
+    s, d = C.c_void_p(), C.c_void_p()
+    _check(_lib.gb_rmat_edges_host_n(n, edge_factor, seed, abc[0], abc[1], abc[2], C.byref(m),
+                                     C.byref(s), C.byref(d)), "rmat_edges_n")
+    return n, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
 
 
 def grid_edges(side: int, extra: int | None = None, max_chain: int = 64,
@@ -298,7 +323,7 @@ class Context:
         _check(_lib.gb_ctx_phase_times(self._h, count, _ptr(out)), "gb_ctx_phase_times")
         return out
 
-    def _run(self, fn, name, g: "Graph", labels, o: Opts | None, want_stats: bool):
+    def _run(self, fn, name, g, labels, o: Opts | None, want_stats: bool):
         st = Stats()
         if labels is None:
             labels = np.empty(g.n, np.int32)
@@ -324,6 +349,17 @@ class Context:
         _check(_lib.gb_wcc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),
                "gb_wcc_async")
 
+    def batch_scc(self, b: "Batch", labels=None, o: Opts | None = None, stats: bool = False):
+        """SCC of every graph of a batch: labels (total_n) local to each graph."""
+        return self._run(_lib.gb_batch_scc, "gb_batch_scc", b, labels, o, stats)
+
+    def batch_wcc(self, b: "Batch", labels=None, o: Opts | None = None, stats: bool = False):
+        return self._run(_lib.gb_batch_wcc, "gb_batch_wcc", b, labels, o, stats)
+
+    def batch_scc_async(self, b: "Batch", labels_dev: int, o: Opts | None = None) -> None:
+        _check(_lib.gb_batch_scc_async(self._h, b._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+               "gb_batch_scc_async")
+
     def pivot(self, g: "Graph", kind: int = 0) -> tuple[int, float]:
         p, a = C.c_int32(), C.c_double()
         _check(_lib.gb_graph_pivot(self._h, g._h, kind, C.byref(p), C.byref(a)), "gb_graph_pivot")
@@ -333,8 +369,9 @@ class Context:
 class Graph:
     """A device-resident graph: out- and in-CSR (gb_graph)."""
 
-    def __init__(self, handle: C.c_void_p):
+    def __init__(self, handle: C.c_void_p, owned: bool = True):
         self._h = handle
+        self._owned = owned
         n, m, sym = C.c_int32(), C.c_int64(), C.c_int32()
         _check(_lib.gb_graph_info(handle, C.byref(n), C.byref(m), C.byref(sym)), "gb_graph_info")
         self.n, self.m, self.symmetric = n.value, m.value, bool(sym.value)
@@ -372,6 +409,14 @@ class Graph:
                                   C.byref(h)), "gb_graph_rmat")
         return cls(h)
 
+    @classmethod
+    def rmat_n(cls, ctx: Context, n: int, edge_factor: int, seed: int,
+               abc: tuple[float, float, float] = RMAT_ABC) -> "Graph":
+        h = C.c_void_p()
+        _check(_lib.gb_graph_rmat_n(ctx._h, n, edge_factor, seed, abc[0], abc[1], abc[2],
+                                    C.byref(h)), "gb_graph_rmat_n")
+        return cls(h)
+
     def to_host(self) -> tuple[np.ndarray, np.ndarray, np.ndarray | None, np.ndarray | None]:
         oo = np.empty(self.n + 1, np.int64)
         oa = np.empty(self.m, np.int32)
@@ -387,8 +432,61 @@ class Graph:
         return tuple(p.value or 0 for p in ps)
 
     def close(self) -> None:
-        if self._h:
+        if self._h and self._owned:
             _lib.gb_graph_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent graphs stored as one disjoint union (gb_batch)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        cnt, tn, tm = C.c_int32(), C.c_int64(), C.c_int64()
+        _check(_lib.gb_batch_info(handle, C.byref(cnt), C.byref(tn), C.byref(tm)), "gb_batch_info")
+        self.count, self.n, self.m = cnt.value, tn.value, tm.value
+        self.vbase = np.zeros(self.count + 1, np.int64)
+        _check(_lib.gb_batch_vbase(handle, _ptr(self.vbase)), "gb_batch_vbase")
+
+    @classmethod
+    def rmat(cls, ctx: Context, ns, efs, seeds,
+             abc: tuple[float, float, float] = RMAT_ABC) -> "Batch":
+        ns = np.ascontiguousarray(ns, np.int32)
+        efs = np.ascontiguousarray(efs, np.int32)
+        seeds = np.ascontiguousarray(seeds, np.uint64)
+        h = C.c_void_p()
+        _check(_lib.gb_batch_rmat(ctx._h, ns.size, _ptr(ns), _ptr(efs), _ptr(seeds), abc[0],
+                                  abc[1], abc[2], C.byref(h)), "gb_batch_rmat")
+        return cls(h)
+
+    @classmethod
+    def from_edges(cls, ctx: Context, vbase, src, dst) -> "Batch":
+        vb = np.ascontiguousarray(vbase, np.int64)
+        s = np.ascontiguousarray(src, np.int32)
+        d = np.ascontiguousarray(dst, np.int32)
+        h = C.c_void_p()
+        _check(_lib.gb_batch_from_edges(ctx._h, vb.size - 1, _ptr(vb), s.size, _ptr(s), _ptr(d),
+                                        C.byref(h)), "gb_batch_from_edges")
+        return cls(h)
+
+    def graph(self) -> Graph:
+        """The union as a Graph (owned by the batch)."""
+        h = C.c_void_p()
+        _check(_lib.gb_batch_graph(self._h, C.byref(h)), "gb_batch_graph")
+        return Graph(h, owned=False)
+
+    def split(self, labels: np.ndarray) -> list[np.ndarray]:
+        return [labels[self.vbase[i]:self.vbase[i + 1]] for i in range(self.count)]
+
+    def close(self) -> None:
+        if self._h:
+            _lib.gb_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):
@@ -431,5 +529,5 @@ class Info:
 __all__ = [
     "Context", "Graph", "GBError", "Opts", "Stats", "opts", "read_edge", "output_labels",
     "scc_verify", "cc_verify", "canonicalize", "rmat_edges", "grid_edges", "batch_sizes",
-    "csr_from_edges", "run_scc_ref", "run_cc_ref", "LIB_PATH",
+    "csr_from_edges", "run_scc_ref", "run_cc_ref", "LIB_PATH", "Batch", "rmat_edges_n",
 ]

@@ -8,40 +8,11 @@
 #include <new>
 
 #include "../../include/gbconn.h"
+#include "api_internal.h"
 #include "gb_internal.cuh"
 #include "host_internal.h"
 
-struct gb_ctx {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  int grid = 0;                 // cooperative grid (all resident blocks)
-  int32_t cap_n = -1;           // workspace capacity in vertices
-  void* ws = nullptr;
-  gb::Work w{};
-  gb::Ctl* d_ctl = nullptr;
-  gb::Ctl* h_ctl = nullptr;     // pinned
-  int* d_sticky = nullptr;      // first error of any run since the last sync
-  int* h_sticky = nullptr;      // pinned
-  static constexpr int kRing = 64;
-  cudaEvent_t ev[kRing][5] = {};  // phase events of the last kRing runs
-  long long runs = 0;             // runs issued on this context
-};
-
-struct gb_graph {
-  int device = 0;
-  int32_t n = 0;
-  int64_t m = 0;
-  int symmetric = 0;
-  int64_t* out_off = nullptr;
-  int32_t* out_adj = nullptr;
-  int64_t* in_off = nullptr;
-  int32_t* in_adj = nullptr;
-  int32_t* hint_out = nullptr;  // pull hints (null for the drop-in staging graph)
-  int32_t* hint_in = nullptr;
-};
-
-namespace {
+namespace gb {
 
 gb_status cuda_fail(cudaError_t e, const char* where) {
   char buf[256];
@@ -66,6 +37,12 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+
+}  // namespace gb
+
+namespace {
+using gb::cuda_fail;
+using gb::is_device_ptr;
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -132,6 +109,10 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
   p.tune.max_steps = o->max_steps > 0 ? o->max_steps : (1 << 30);
 }
 
+}  // namespace
+
+namespace gb {
+
 gb_status graph_alloc(gb_graph* g, bool with_in) {
   const size_t offb = (size_t)(g->n + 1) * 8, adjb = (size_t)(g->m > 0 ? g->m : 1) * 4;
   CK(cudaMalloc(&g->out_off, offb), "graph allocation");
@@ -166,6 +147,13 @@ gb_status graph_hints(gb_ctx* c, gb_graph* g) {
      "hints");
   return GB_OK;
 }
+
+}  // namespace gb
+
+namespace {
+using gb::graph_alloc;
+using gb::graph_free;
+using gb::graph_hints;
 
 gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
   CK(cudaStreamSynchronize(c->stream), "run");
@@ -234,8 +222,8 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
   return GB_OK;
 }
 
-gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
-              const gb_opts* o, gb_stats* st, bool wait) {
+gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
+                         const gb_opts* o, gb_stats* st, bool wait, const gb::BatchView* bv) {
   if (!c || !g) {
     gb_set_error("run: null context or graph%s", "");
     return GB_ERR_INVALID;
@@ -262,12 +250,12 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   w.nwords = (g->n + 31) / 32;
   w.m = g->m;
   if (dev_labels) w.label = labels;
-  gb::RunParams p;
+  gb::RunParams p{};
   fill_params(o, p);
   p.count_unassigned = st != nullptr ? 1 : 0;
   int grid = c->grid;
   if (o && o->grid_blocks > 0 && o->grid_blocks < grid) grid = o->grid_blocks;
-  gb::GraphView gv;
+  gb::GraphView gv{};
   gv.n = g->n;
   gv.m = g->m;
   gv.out = {g->out_off, g->out_adj, g->hint_out};
@@ -277,7 +265,13 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   } else {
     gv.in = {g->in_off, g->in_adj, g->hint_in};
   }
+  gv.batch = gb::BatchView{};
   cudaStream_t sm = c->stream;
+  if (bv != nullptr) {
+    gv.batch = *bv;
+    CK(cudaMemsetAsync(bv->pkey, 0, (size_t)bv->count * 8, sm), "memset");
+    CK(cudaMemsetAsync(bv->gmin, 0x7f, (size_t)bv->count * 4, sm), "memset");
+  }
   CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
   CK(cudaMemsetAsync(w.fvis, 0, (size_t)w.nwords * 4, sm), "memset");
   CK(cudaMemsetAsync(w.bvis, 0, (size_t)w.nwords * 4, sm), "memset");
@@ -287,12 +281,23 @@ gb_status run(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
   c->runs++;
   CK(gb::launch_run(gv, kind, p, w, grid, sm, ev), "kernel launch");
   CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
+  if (bv != nullptr) CK(gb::launch_localize(w.label, g->n, bv->gid, bv->vbase, sm), "localize");
   if (!dev_labels)
     CK(cudaMemcpyAsync(labels, w.label, (size_t)g->n * 4, cudaMemcpyDeviceToHost, sm), "labels copy");
   CK(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(gb::Ctl), cudaMemcpyDeviceToHost, sm), "status copy");
   if (!wait) return GB_OK;
   return finish_run(c, g, st);
 }
+
+}  // namespace
+
+gb_status gb::run_graph(gb_ctx* c, const gb_graph* g, RunKind kind, int32_t* labels,
+                        const gb_opts* o, gb_stats* st, bool wait, const BatchView* bv) {
+  return run_graph_impl(c, g, kind, labels, o, st, wait, bv);
+}
+
+namespace {
+using gb::validate_csr;
 
 std::mutex g_default_mu;
 gb_ctx* g_default_ctx = nullptr;
@@ -508,7 +513,10 @@ gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* sr
 
 // Validates CSR arrays already on the device: off[0] == 0, off[n] == m,
 // offsets non-decreasing, ids in [0, n).
-static gb_status validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off, const int32_t* adj) {
+}  // extern "C"
+
+gb_status gb::validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off,
+                           const int32_t* adj) {
   int bad = 0;
   cudaError_t e = gb::check_csr(n, m, off, adj, c->stream, &bad);
   if (e != cudaSuccess) return cuda_fail(e, "CSR check");
@@ -518,6 +526,8 @@ static gb_status validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* of
   }
   return GB_OK;
 }
+
+extern "C" {
 
 static gb_status upload(gb_ctx* c, void* dst, const void* src, size_t bytes) {
   if (bytes == 0) return GB_OK;
@@ -606,8 +616,26 @@ gb_status gb_graph_rmat(gb_ctx* c, int32_t scale, int32_t ef, uint64_t seed, dou
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   int32_t *s = nullptr, *d = nullptr;
   int64_t m = 0;
-  CK(gb::rmat_edges_device(scale, ef, seed, gb_rmat_thresholds(a, b, cc), &s, &d, &m, c->stream), "R-MAT");
+  CK(gb::rmat_edges_device((int32_t)(1 << scale), ef, seed, gb_rmat_thresholds(a, b, cc), &s, &d, &m,
+                           c->stream),
+     "R-MAT");
   gb_status st = gb_graph_from_edges(c, (int32_t)(1 << scale), m, s, d, out);
+  cudaFreeAsync(s, c->stream);
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return st;
+}
+
+gb_status gb_graph_rmat_n(gb_ctx* c, int32_t n, int32_t ef, uint64_t seed, double a, double b,
+                          double cc, gb_graph** out) {
+  if (!c || !out || n < 1 || ef < 1) return GB_ERR_INVALID;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  int32_t *s = nullptr, *d = nullptr;
+  int64_t m = 0;
+  CK(gb::rmat_edges_device(n, ef, seed, gb_rmat_thresholds(a, b, cc), &s, &d, &m, c->stream),
+     "R-MAT");
+  gb_status st = gb_graph_from_edges(c, n, m, s, d, out);
   cudaFreeAsync(s, c->stream);
   cudaFreeAsync(d, c->stream);
   cudaStreamSynchronize(c->stream);
@@ -669,19 +697,19 @@ gb_status gb_graph_destroy(gb_graph* g) {
 }
 
 gb_status gb_scc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
-  return run(c, g, gb::kSCC, labels, o, st, true);
+  return gb::run_graph(c, g, gb::kSCC, labels, o, st, true, nullptr);
 }
 gb_status gb_wcc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
-  return run(c, g, gb::kWCC, labels, o, st, true);
+  return gb::run_graph(c, g, gb::kWCC, labels, o, st, true, nullptr);
 }
 gb_status gb_cc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
-  return run(c, g, gb::kWCC, labels, o, st, true);
+  return gb::run_graph(c, g, gb::kWCC, labels, o, st, true, nullptr);
 }
 gb_status gb_scc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o) {
-  return run(c, g, gb::kSCC, labels, o, nullptr, false);
+  return gb::run_graph(c, g, gb::kSCC, labels, o, nullptr, false, nullptr);
 }
 gb_status gb_wcc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o) {
-  return run(c, g, gb::kWCC, labels, o, nullptr, false);
+  return gb::run_graph(c, g, gb::kWCC, labels, o, nullptr, false, nullptr);
 }
 
 // Drop-ins with the reference's signatures: a library-owned context on

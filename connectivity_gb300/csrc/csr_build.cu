@@ -45,14 +45,87 @@ __global__ void k_widen(const uint32_t* in, int64_t* out, int64_t count) {
     out[i] = (int64_t)in[i];
 }
 
-__global__ void k_rmat_keys(uint64_t seed, int64_t m0, int scale, gb_rmat_thr thr, uint64_t self,
-                            uint64_t* keys) {
+__global__ void k_rmat_keys(uint64_t seed, int64_t m0, int scale, uint32_t n, gb_rmat_thr thr,
+                            uint64_t self, uint64_t* keys) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m0;
        i += (int64_t)gridDim.x * blockDim.x) {
     uint32_t s, d;
     gb_rmat_edge(seed, (uint64_t)i, scale, thr, &s, &d);
-    keys[i] = s == d ? self : (((uint64_t)s << scale) | d);
+    keys[i] = (s == d || s >= n || d >= n) ? self : (((uint64_t)s << scale) | d);
   }
+}
+
+// Batch generator: edge index i of the concatenation of every graph's ef*n
+// candidate edges.  Each thread walks a run of kRun consecutive indices,
+// locating its graph once.  Keys hold global ids.
+constexpr int kRun = 64;
+__global__ void k_batch_keys(int64_t etotal, const int64_t* ebase, const int64_t* vbase,
+                             const int32_t* nv, const int32_t* scale, const uint64_t* seeds,
+                             int32_t count, gb_rmat_thr thr, int id_bits, uint64_t* keys) {
+  const uint64_t self = (1ull << (2 * id_bits)) - 1ull;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r * kRun < etotal;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = r * kRun;
+    const int64_t end = i + kRun < etotal ? i + kRun : etotal;
+    int lo = 0, hi = count;  // last graph with ebase[g] <= i
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (ebase[mid] <= i) lo = mid; else hi = mid;
+    }
+    int gr = lo;
+    for (; i < end; ++i) {
+      while (gr + 1 < count && ebase[gr + 1] <= i) ++gr;
+      uint32_t s, d;
+      gb_rmat_edge(seeds[gr], (uint64_t)(i - ebase[gr]), scale[gr], thr, &s, &d);
+      const uint32_t n = (uint32_t)nv[gr];
+      if (s == d || s >= n || d >= n) {
+        keys[i] = self;
+      } else {
+        const uint64_t vb = (uint64_t)vbase[gr];
+        keys[i] = ((vb + s) << id_bits) | (vb + d);
+      }
+    }
+  }
+}
+
+__global__ void k_split_bits(const uint64_t* keys, int64_t m, int id_bits, int32_t* src,
+                             int32_t* dst) {
+  const uint64_t mask = (1ull << id_bits) - 1ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    src[i] = (int32_t)(keys[i] >> id_bits);
+    dst[i] = (int32_t)(keys[i] & mask);
+  }
+}
+
+__global__ void k_fill_gid(int32_t n, const int64_t* vbase, int32_t count, int32_t* gid) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = count;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (vbase[mid] <= v) lo = mid; else hi = mid;
+    }
+    gid[v] = lo;
+  }
+}
+
+// Every edge must stay inside its graph.
+__global__ void k_check_within(const int32_t* s, const int32_t* d, int64_t m, const int32_t* gid,
+                               int* bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (gid[s[i]] != gid[d[i]]) atomicOr(bad, 1);
+}
+
+__global__ void k_max_degree(int32_t n, const int64_t* off, unsigned long long* out) {
+  unsigned long long best = 0;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long d = (unsigned long long)(off[v + 1] - off[v]);
+    if (d > best) best = d;
+  }
+  if (best) atomicMax(out, best);
 }
 
 __global__ void k_split(const uint64_t* keys, int64_t m, int scale, int32_t* src, int32_t* dst) {
@@ -249,6 +322,114 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
   return cudaSuccess;
 }
 
+cudaError_t batch_edges_device(int32_t count, const int32_t* h_n, const int32_t* h_ef,
+                               const uint64_t* h_seeds, gb_rmat_thr thr, int id_bits,
+                               const int64_t* h_vbase, int32_t** d_src, int32_t** d_dst,
+                               int64_t* m_out, cudaStream_t s) {
+  // per graph: scale, candidate edge base
+  int32_t* hs = new int32_t[count];
+  int64_t* heb = new int64_t[count + 1];
+  heb[0] = 0;
+  for (int g = 0; g < count; ++g) {
+    int sc = 1;
+    while (sc < 31 && (1ll << sc) < (long long)h_n[g]) ++sc;
+    hs[g] = sc;
+    heb[g + 1] = heb[g] + (int64_t)h_ef[g] * h_n[g];
+  }
+  const int64_t etotal = heb[count];
+  int64_t *d_eb = nullptr, *d_vb = nullptr, *nsel = nullptr;
+  int32_t *d_nv = nullptr, *d_sc = nullptr;
+  uint64_t *d_seed = nullptr, *a = nullptr, *b = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_eb, (count + 1) * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_vb, (count + 1) * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_nv, count * 4, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_sc, count * 4, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_seed, count * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&nsel, 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&a, (size_t)(etotal > 0 ? etotal : 1) * 8, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&b, (size_t)(etotal > 0 ? etotal : 1) * 8, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_eb, heb, (count + 1) * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_vb, h_vbase, (count + 1) * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_nv, h_n, count * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_sc, hs, count * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seed, h_seeds, count * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  delete[] hs;
+  delete[] heb;
+  int64_t k = 0;
+  if (e == cudaSuccess && etotal > 0) {
+    k_batch_keys<<<grid_for((etotal + kRun - 1) / kRun), 256, 0, s>>>(
+        etotal, d_eb, d_vb, d_nv, d_sc, d_seed, count, thr, id_bits, a);
+    size_t bytes = 0, bytes2 = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, bytes, a, b, etotal, 0, 2 * id_bits, s);
+    cub::DeviceSelect::Unique(nullptr, bytes2, b, a, nsel, etotal, s);
+    if (bytes2 > bytes) bytes = bytes2;
+    void* temp = nullptr;
+    e = cudaMallocAsync(&temp, bytes ? bytes : 16, s);
+    if (e == cudaSuccess) e = cub::DeviceRadixSort::SortKeys(temp, bytes, a, b, etotal, 0, 2 * id_bits, s);
+    if (e == cudaSuccess) e = cub::DeviceSelect::Unique(temp, bytes, b, a, nsel, etotal, s);
+    cudaFreeAsync(temp, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&k, nsel, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && k > 0) {
+      uint64_t last = 0;
+      e = cudaMemcpyAsync(&last, a + (k - 1), 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (last == (1ull << (2 * id_bits)) - 1ull) --k;  // the dropped-edge marker
+    }
+  }
+  int32_t *src = nullptr, *dst = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&src, (size_t)(k > 0 ? k : 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dst, (size_t)(k > 0 ? k : 1) * 4, s);
+  if (e == cudaSuccess && k > 0) k_split_bits<<<grid_for(k), 256, 0, s>>>(a, k, id_bits, src, dst);
+  cudaFreeAsync(a, s);
+  cudaFreeAsync(b, s);
+  cudaFreeAsync(d_eb, s);
+  cudaFreeAsync(d_vb, s);
+  cudaFreeAsync(d_nv, s);
+  cudaFreeAsync(d_sc, s);
+  cudaFreeAsync(d_seed, s);
+  cudaFreeAsync(nsel, s);
+  if (e != cudaSuccess) return e;
+  *d_src = src;
+  *d_dst = dst;
+  *m_out = k;
+  return cudaGetLastError();
+}
+
+cudaError_t batch_gid(int32_t n, const int64_t* d_vbase, int32_t count, int32_t* gid,
+                      cudaStream_t s) {
+  if (n > 0) k_fill_gid<<<grid_for(n), 256, 0, s>>>(n, d_vbase, count, gid);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_check_within(const int32_t* src, const int32_t* dst, int64_t m,
+                               const int32_t* gid, cudaStream_t s, int* bad) {
+  int* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(d, 0, sizeof(int), s);
+  if (m > 0) k_check_within<<<grid_for(m), 256, 0, s>>>(src, dst, m, gid, d);
+  cudaMemcpyAsync(bad, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
+}
+
+cudaError_t max_degree(int32_t n, const int64_t* off, cudaStream_t s, unsigned long long* out) {
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, 8, s);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(d, 0, 8, s);
+  if (n > 0) k_max_degree<<<grid_for(n), 256, 0, s>>>(n, off, d);
+  cudaMemcpyAsync(out, d, 8, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
+}
+
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s) {
   k_latch<<<1, 1, 0, s>>>(ctl, sticky);
   return cudaGetLastError();
@@ -277,9 +458,11 @@ cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat_thr thr,
+cudaError_t rmat_edges_device(int32_t n, int edge_factor, uint64_t seed, gb_rmat_thr thr,
                               int32_t** d_src, int32_t** d_dst, int64_t* m_out, cudaStream_t s) {
-  const int64_t m0 = (int64_t)edge_factor << scale;
+  int scale = 1;
+  while (scale < 31 && (1ll << scale) < (long long)n) ++scale;
+  const int64_t m0 = (int64_t)edge_factor * n;
   const uint64_t self = (1ull << (2 * scale)) - 1ull;
   uint64_t *a = nullptr, *b = nullptr;
   int64_t* nsel = nullptr;
@@ -287,7 +470,7 @@ cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat
   if (e == cudaSuccess) e = cudaMallocAsync(&b, (size_t)m0 * 8, s);
   if (e == cudaSuccess) e = cudaMallocAsync(&nsel, sizeof(int64_t), s);
   if (e != cudaSuccess) return e;
-  k_rmat_keys<<<grid_for(m0), 256, 0, s>>>(seed, m0, scale, thr, self, a);
+  k_rmat_keys<<<grid_for(m0), 256, 0, s>>>(seed, m0, scale, (uint32_t)n, thr, self, a);
   size_t bytes = 0, bytes2 = 0;
   cub::DeviceRadixSort::SortKeys(nullptr, bytes, a, b, m0, 0, 2 * scale, s);
   cub::DeviceSelect::Unique(nullptr, bytes2, b, a, nsel, m0, s);

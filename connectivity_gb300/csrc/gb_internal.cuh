@@ -69,6 +69,7 @@ struct Ctl {
   int32_t unassigned;
   int32_t ncolour;        // vertices labelled by the colour rounds
   int32_t minv[2];        // smallest vertex reached forward / backward
+  int32_t nroots;         // batch: pivots in BatchView::roots
   int32_t lcount[2][2];   // pull steps: warp- and block-tier list lengths
                           // (two sets, used by alternate pull steps)
   int32_t pad1;
@@ -136,12 +137,26 @@ struct Work {
   Ctl* ctl;
 };
 
-// One graph as the kernels see it.  `in` is null for a symmetric CSR.
+// A batch of independent graphs stored as one disjoint union: graph g owns
+// vertices [vbase[g], vbase[g+1]).  gid == null for a single graph.
+struct BatchView {
+  const int32_t* gid;          // vertex -> graph
+  const int64_t* vbase;        // count + 1 entries
+  int32_t count;
+  int32_t id_bits;             // pivot keys: (score << id_bits) | (mask - v)
+  unsigned long long* pkey;    // per graph pivot key (zeroed per run)
+  int32_t* gmin;               // per graph smallest FW-BW member (INT_MAX per run)
+  int32_t* roots;              // per run: the pivots of all graphs
+};
+
+// One graph (or a batch union) as the kernels see it.  `in` is null for a
+// symmetric CSR.
 struct GraphView {
   int32_t n;
   int64_t m;
   Csr out;
   Csr in;
+  BatchView batch;
 };
 
 // Kind of run.
@@ -180,14 +195,31 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
 // unless an earlier one is already there.
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
+// Batch labels: global ids -> ids local to each graph.
+cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
+                            cudaStream_t s);
 // Pull hints: for every vertex, its neighbour of largest total degree in
 // each CSR (hint_in may be null when in_off is).  Synchronises the stream.
 cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s);
-// Seeded R-MAT edge list on the device, sorted by (src, dst), without
-// self-loops and duplicates; *d_src / *d_dst are cudaMallocAsync'd.
-cudaError_t rmat_edges_device(int scale, int edge_factor, uint64_t seed, gb_rmat_thr thr,
+// Seeded R-MAT edge list on the device for n vertices: edge_factor * n
+// candidate edges at scale ceil(log2 n), ids >= n, self-loops and duplicates
+// dropped, sorted by (src, dst); *d_src / *d_dst are cudaMallocAsync'd.
+cudaError_t rmat_edges_device(int32_t n, int edge_factor, uint64_t seed, gb_rmat_thr thr,
                               int32_t** d_src, int32_t** d_dst, int64_t* m_out, cudaStream_t s);
+// The same for a batch: graph g (h_n[g] vertices, h_ef[g], h_seeds[g]) gets
+// global ids from h_vbase[g]; id_bits >= bits of the total vertex count.
+cudaError_t batch_edges_device(int32_t count, const int32_t* h_n, const int32_t* h_ef,
+                               const uint64_t* h_seeds, gb_rmat_thr thr, int id_bits,
+                               const int64_t* h_vbase, int32_t** d_src, int32_t** d_dst,
+                               int64_t* m_out, cudaStream_t s);
+cudaError_t batch_gid(int32_t n, const int64_t* d_vbase, int32_t count, int32_t* gid,
+                      cudaStream_t s);
+// Sets *bad if an edge joins two graphs.  Synchronises the stream.
+cudaError_t batch_check_within(const int32_t* src, const int32_t* dst, int64_t m,
+                               const int32_t* gid, cudaStream_t s, int* bad);
+// Largest degree of a CSR.  Synchronises the stream.
+cudaError_t max_degree(int32_t n, const int64_t* off, cudaStream_t s, unsigned long long* out);
 
 }  // namespace gb

@@ -289,19 +289,26 @@ static void radix_sort_u64(std::vector<uint64_t>& keys, int bits) {
   if (src != keys.data()) std::memcpy(keys.data(), src, n * sizeof(uint64_t));
 }
 
-extern "C" gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint64_t seed,
-                                        double a, double b, double c, int64_t* m, int32_t** src,
-                                        int32_t** dst) {
-  if (scale < 1 || scale > 30 || edge_factor < 1 || !m || !src || !dst) return GB_ERR_INVALID;
-  const long long m0 = (long long)edge_factor << scale;
+// R-MAT graph on n vertices: edge_factor * n candidate edges drawn at scale
+// ceil(log2 n); ids >= n, self-loops and duplicates dropped; sorted by
+// (src, dst).  For n a power of two nothing is dropped but self-loops and
+// duplicates.  The device generator follows the same rule.
+static gb_status rmat_host(int32_t n, int32_t edge_factor, uint64_t seed, double a, double b,
+                           double c, int64_t* m, int32_t** src, int32_t** dst) {
+  if (n < 1 || edge_factor < 1 || !m || !src || !dst) return GB_ERR_INVALID;
+  int scale = 1;
+  while (scale < 31 && (1ll << scale) < (long long)n) ++scale;
+  const long long m0 = (long long)edge_factor * n;
   const gb_rmat_thr thr = gb_rmat_thresholds(a, b, c);
-  const uint64_t self = (1ull << (2 * scale)) - 1ull;  // key of (n-1, n-1)
+  const uint64_t self = (1ull << (2 * scale)) - 1ull;  // marker of a dropped edge
   std::vector<uint64_t> keys((size_t)m0);
 #pragma omp parallel for schedule(static)
   for (long long i = 0; i < m0; ++i) {
     uint32_t s, d;
     gb_rmat_edge(seed, (uint64_t)i, scale, thr, &s, &d);
-    keys[(size_t)i] = s == d ? self : (((uint64_t)s << scale) | d);
+    keys[(size_t)i] = (s == d || s >= (uint32_t)n || d >= (uint32_t)n)
+                          ? self
+                          : (((uint64_t)s << scale) | d);
   }
   radix_sort_u64(keys, 2 * scale);
   size_t k = 0;
@@ -327,6 +334,19 @@ extern "C" gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint
   *src = s;
   *dst = d;
   return GB_OK;
+}
+
+extern "C" gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint64_t seed,
+                                        double a, double b, double c, int64_t* m, int32_t** src,
+                                        int32_t** dst) {
+  if (scale < 1 || scale > 30) return GB_ERR_INVALID;
+  return rmat_host((int32_t)(1 << scale), edge_factor, seed, a, b, c, m, src, dst);
+}
+
+extern "C" gb_status gb_rmat_edges_host_n(int32_t n, int32_t edge_factor, uint64_t seed, double a,
+                                          double b, double c, int64_t* m, int32_t** src,
+                                          int32_t** dst) {
+  return rmat_host(n, edge_factor, seed, a, b, c, m, src, dst);
 }
 
 extern "C" gb_status gb_grid_edges_host(int32_t side, int32_t extra, int32_t max_chain,

@@ -758,6 +758,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   Tally ty;
   if (ld_vol(&c->err)) return;
   Steps st = steps_open(c);
+  // the FW-BW minima are folded with atomicMin later (read after this
+  // kernel ends)
+  if (b == 0 && t == 0) {
+    c->minv[0] = 0x7fffffff;
+    c->minv[1] = 0x7fffffff;
+  }
 
   // Pass 1: warp k of the grid takes the 32-vertex word k.
   unsigned long long best_key = 0ull;  // out*in (SCC) or degree (WCC)
@@ -799,6 +805,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
       const long long wd = wd0 + j;
       const long long vv = wd * 32 + lane;
       bool keep = false, gone = false;
+      unsigned long long score = 0ull;
       if (vv < g.n) {
         const int32_t v = (int32_t)vv;
         const long long dout = o1[j] - o0[j];
@@ -810,6 +817,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
             const unsigned long long prod = (unsigned long long)dout * (unsigned long long)din;
             if (prod > best_key) { best_key = prod; best_v = v; }
             mc += (unsigned long long)dout;
+            score = prod;
           }
         } else {
           const long long deg = dout + din;
@@ -817,6 +825,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
           if (keep) {
             if ((unsigned long long)deg > best_key) { best_key = (unsigned long long)deg; best_v = v; }
             mc += (unsigned long long)deg;
+            score = (unsigned long long)deg;
           }
         }
         gone = !keep;
@@ -830,6 +839,24 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
       const unsigned bits = __ballot_sync(kFull, keep);
       if (wd < w.nwords && lane == 0) w.vbits[wd] = bits;
       if (level2) stage_push(rs, gone, (int32_t)vv, 0ull, ro, c);
+      // batch: per-graph pivot, the packed key (score, lowest id) is maxed
+      if (g.batch.gid != nullptr) {
+        const unsigned long long mask = (1ull << g.batch.id_bits) - 1ull;
+        const unsigned long long key =
+            score ? ((score << g.batch.id_bits) | (mask - (unsigned long long)vv)) : 0ull;
+        const int32_t gg = vv < g.n ? __ldg(g.batch.gid + vv) : -1;
+        const int32_t g0 = __shfl_sync(kFull, gg, 0);
+        if (__all_sync(kFull, gg == g0)) {
+          unsigned long long kmax = key;
+          for (int o = 16; o; o >>= 1) {
+            const unsigned long long k2 = __shfl_xor_sync(kFull, kmax, o);
+            kmax = k2 > kmax ? k2 : kmax;
+          }
+          if (lane == 0 && kmax && kmax > __ldcg(g.batch.pkey + g0)) atomicMax(g.batch.pkey + g0, kmax);
+        } else if (key && gg >= 0 && key > __ldcg(g.batch.pkey + gg)) {
+          atomicMax(g.batch.pkey + gg, key);
+        }
+      }
     }
   }
   if (level2) stage_flush(rs, ro, c);
@@ -938,6 +965,22 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
     if (pv >= 0 && !bit_get(w.vbits, pv)) pv = -1;
     c->pivot = pv;
   }
+  // batch: every graph's pivot that survived trim is a root
+  if (g.batch.gid != nullptr) {
+    const unsigned long long mask = (1ull << g.batch.id_bits) - 1ull;
+    for (long long gi0 = (long long)b * T; gi0 < g.batch.count; gi0 += (long long)G * T) {
+      const long long gi = gi0 + t;
+      int32_t v = -1;
+      if (gi < g.batch.count) {
+        const unsigned long long key = __ldcg(g.batch.pkey + gi);
+        if (key) {
+          v = (int32_t)(mask - (key & mask));
+          if (!bit_get(w.vbits, v)) v = -1;
+        }
+      }
+      list_append(v >= 0, v, g.batch.roots, &c->nroots, g.batch.count, c, 6);
+    }
+  }
   tally_flush(ty, c, kKTrim);
   steps_close(c, st);
 }
@@ -960,7 +1003,8 @@ struct ReachSpec {
   const int32_t* cand;
   int32_t ncand;
   unsigned long long m_cand;
-  int32_t root;
+  const int32_t* roots;   // sources (distinct, allowed)
+  int32_t nroots;
   int32_t* q;
   int32_t* minv;
   int stat_slot;
@@ -1179,14 +1223,29 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
   const int warp = t >> 5, lane = t & 31;
   const Tune& tn = A.p.tune;
   const ReachVisit<NC> rv{R.allow, R.vis, R.push};
-  if (b == 0 && t == 0) {
-    if (bit_claim(R.vis, R.root)) {
-      R.q[0] = R.root;
-      Slot* o = step_out(c, st.s);
-      o->count = 1;
-      o->edges = adj_degree<NC>(R.push, R.root);
-      *R.minv = R.root;
+  // the sources are the first step's frontier
+  {
+    Out ro;
+    ro.arr = R.q;
+    ro.base = 0;
+    ro.cap = w.n;
+    ro.counter = &step_out(c, st.s)->count;
+    ro.edges = &step_out(c, st.s)->edges;
+    ro.minv = R.minv;
+    ro.where = 207;
+    Stage rs = stage_make(sm.stage(warp, 0));
+    for (long long base = (long long)b * T + (t & ~31); base < R.nroots;
+         base += (long long)G * T) {
+      const long long i = base + lane;
+      bool take = false;
+      int32_t r = 0;
+      if (i < R.nroots) {
+        r = __ldcg(R.roots + i);
+        take = bit_claim(R.vis, r);
+      }
+      stage_push(rs, take, r, take ? adj_degree<NC>(R.push, r) : 0ull, ro, c);
     }
+    stage_flush(rs, ro, c);
   }
   if (!step_sync(c, st, 20)) return -1;
   long long qlo = 0, qhi = 0;
@@ -1266,9 +1325,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   Tally ty;
   if (ld_vol(&c->err)) return;
+  const bool batch = g.batch.gid != nullptr;
   const int32_t pivot = __ldcg(&c->pivot);
   const int32_t nvalid = __ldcg(&c->nvalid);
-  if (pivot < 0 || nvalid == 0) return;
+  const int32_t* roots = batch ? g.batch.roots : &c->pivot;
+  const int32_t nroots = batch ? __ldcg(&c->nroots) : (pivot >= 0 ? 1 : 0);
+  if (nroots == 0 || nvalid == 0) return;
   Steps st = steps_open(c);
   const bool scc = A.kind == kSCC;
   const uint32_t* hit;
@@ -1281,9 +1343,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   F.cand = w.listA;
   F.ncand = nvalid;
   F.m_cand = __ldcg(&c->m_cand);
-  F.root = pivot;
+  F.roots = roots;
+  F.nroots = nroots;
   F.q = w.q;
-  F.minv = &c->minv[0];
+  F.minv = batch ? nullptr : &c->minv[0];
   F.stat_slot = kStFwSteps;
   int pp = 0;  // pull steps so far (selects the long-list counters)
   const int nf = reach<NC>(F, A, w, sm, st, ty, pp);
@@ -1299,9 +1362,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
     B.cand = w.q;
     B.ncand = nf;
     B.m_cand = F.m_cand;
-    B.root = pivot;
+    B.roots = roots;
+    B.nroots = nroots;
     B.q = w.x0;
-    B.minv = &c->minv[1];
+    B.minv = batch ? nullptr : &c->minv[1];
     B.stat_slot = kStBwSteps;
     const int nb = reach<1>(B, A, w, sm, st, ty, pp);
     if (nb < 0) return;
@@ -1313,7 +1377,25 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
     hit = w.fvis;
     hit_min = &c->minv[0];
   }
-  const int32_t lab = A.p.canonical ? __ldcg(hit_min) : pivot;
+  // batch: the smallest member of each graph's component labels it
+  if (batch) {
+    for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
+      unsigned x = __ldcg(hit + wd);
+      int32_t gprev = -1;
+      while (x) {
+        const int bit = __ffs(x) - 1;
+        x &= x - 1;
+        const int32_t v = (int32_t)(wd * 32 + bit);
+        const int32_t gg = __ldg(g.batch.gid + v);
+        if (gg != gprev) {  // bits rise, so v is the smallest of its graph here
+          if (v < __ldcg(g.batch.gmin + gg)) atomicMin(g.batch.gmin + gg, v);
+          gprev = gg;
+        }
+      }
+    }
+    if (!step_sync(c, st, 25)) return;
+  }
+  const int32_t lab = A.p.canonical ? (batch ? -1 : __ldcg(hit_min)) : pivot;
   // label the component and take it out of the valid set (update_valid,
   // scc_fwbw.cpp:425-433)
   for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
@@ -1324,7 +1406,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
       while (x) {
         const int bit = __ffs(x) - 1;
         x &= x - 1;
-        w.label[wd * 32 + bit] = lab;
+        const int32_t v = (int32_t)(wd * 32 + bit);
+        w.label[v] = batch ? (A.p.canonical ? __ldcg(g.batch.gmin + __ldg(g.batch.gid + v))
+                                            : v)
+                           : lab;
       }
     }
   }
@@ -1502,6 +1587,14 @@ __global__ void k_count_unassigned(Args A) {
   if (lane_id() == 0 && un) atomicAdd(&w.ctl->unassigned, un);
 }
 
+__global__ void k_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int32_t l = labels[v];
+    if (l >= 0) labels[v] = (int32_t)(l - vbase[gid[v]]);
+  }
+}
+
 template <class K>
 cudaError_t coop(K kern, int grid, const Args& a, cudaStream_t s) {
   void* params[] = {const_cast<Args*>(&a)};
@@ -1530,9 +1623,18 @@ int max_coop_grid(int device) {
   return best * sms;
 }
 
+cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
+                            cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  long long blocks = ((long long)n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_localize<<<(int)blocks, 256, 0, s>>>(labels, n, gid, vbase);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p, const Work& w,
                        int grid, cudaStream_t stream, cudaEvent_t* ev) {
-  Args a;
+  Args a{};
   a.g = g;
   a.p = p;
   a.w = w;

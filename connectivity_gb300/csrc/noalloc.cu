@@ -150,14 +150,14 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
     gb_set_error("gb_scc_noalloc: %s", cudaGetErrorString(e));
     return GB_ERR_CUDA;
   }
-  gb::GraphView gv;
+  gb::GraphView gv{};
   gv.n = n;
   gv.m = m;
   gv.out = {out_off, out_adj, nullptr};
   gv.in = {in_off, in_adj, nullptr};
   gb_opts o;
   gb_opts_default(&o);
-  gb::RunParams prm;
+  gb::RunParams prm{};
   prm.trim_level = o.trim_level;
   prm.canonical = 1;
   prm.pivot_hint = -1;

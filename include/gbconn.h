@@ -161,6 +161,11 @@ gb_status gb_graph_from_csr32(gb_ctx* ctx, int32_t n, uint32_t m, const int32_t*
  * duplicates removed.  Same edges as gb_rmat_edges_host. */
 gb_status gb_graph_rmat(gb_ctx* ctx, int32_t scale, int32_t edge_factor, uint64_t seed, double a,
                         double b, double c, gb_graph** g);
+/* R-MAT graph on any n: edge_factor * n candidate edges at scale
+ * ceil(log2 n), ids >= n dropped (the batch rule).  Same edges as
+ * gb_rmat_edges_host_n. */
+gb_status gb_graph_rmat_n(gb_ctx* ctx, int32_t n, int32_t edge_factor, uint64_t seed, double a,
+                          double b, double c, gb_graph** g);
 gb_status gb_graph_info(const gb_graph* g, int32_t* n, int64_t* m, int32_t* symmetric);
 /* Copies the CSR to host arrays (n+1 offsets, m entries; in_* ignored when
  * NULL). */
@@ -213,6 +218,38 @@ gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off, const int
                          const int64_t* in_off, const int32_t* in_adj, int32_t* labels,
                          void* stream);
 
+/* ---- batches: many independent graphs per run ------------------------- */
+/* No counterpart in the reference, whose equivalent is a loop of run_scc /
+ * run_cc (multistep/scc_main.cpp:210, cc_main.cpp:184) per graph.  A batch
+ * is one disjoint union: graph g owns vertices [vbase[g], vbase[g+1]) and its
+ * edges use those global ids.  A run advances every graph in the same
+ * kernels (each phase one cooperative launch), with each graph's pivot chosen
+ * by the reference rule within the graph, and returns labels local to each
+ * graph (its smallest member's local id), identical to running the graph
+ * alone. */
+typedef struct gb_batch gb_batch;
+/* From a concatenated edge list (host or device, m entries, global ids);
+ * vbase has count + 1 entries starting at 0.  An edge that joins two graphs
+ * is rejected (GB_ERR_INVALID). */
+gb_status gb_batch_from_edges(gb_ctx* ctx, int32_t count, const int64_t* vbase, int64_t m,
+                              const int32_t* src, const int32_t* dst, gb_batch** b);
+/* count seeded R-MAT graphs built on the device: graph g has n[g] vertices,
+ * edge factor ef[g], seed seeds[g] (the gb_graph_rmat_n rule per graph). */
+gb_status gb_batch_rmat(gb_ctx* ctx, int32_t count, const int32_t* n, const int32_t* ef,
+                        const uint64_t* seeds, double a, double b, double c, gb_batch** batch);
+gb_status gb_batch_info(const gb_batch* b, int32_t* count, int64_t* total_n, int64_t* total_m);
+gb_status gb_batch_vbase(const gb_batch* b, int64_t* vbase);
+/* The union as a graph (owned by the batch). */
+gb_status gb_batch_graph(const gb_batch* b, const gb_graph** g);
+/* labels: total_n entries (host or device), local ids per graph. */
+gb_status gb_batch_scc(gb_ctx* ctx, const gb_batch* b, int32_t* labels, const gb_opts* opts,
+                       gb_stats* stats);
+gb_status gb_batch_wcc(gb_ctx* ctx, const gb_batch* b, int32_t* labels, const gb_opts* opts,
+                       gb_stats* stats);
+gb_status gb_batch_scc_async(gb_ctx* ctx, const gb_batch* b, int32_t* labels_dev,
+                             const gb_opts* opts);
+gb_status gb_batch_destroy(gb_batch* b);
+
 /* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
@@ -254,6 +291,9 @@ gb_status gb_canonicalize(int32_t n, int32_t* labels);
  * R-MAT: as gb_graph_rmat; *src/*dst malloc'd, sorted by (src, dst). */
 gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint64_t seed, double a,
                              double b, double c, int64_t* m, int32_t** src, int32_t** dst);
+/* R-MAT on any n (the batch rule, see gb_graph_rmat_n). */
+gb_status gb_rmat_edges_host_n(int32_t n, int32_t edge_factor, uint64_t seed, double a, double b,
+                               double c, int64_t* m, int32_t** src, int32_t** dst);
 /* side x side lattice, every lattice edge u->v, v->u, both or none with
  * probability 1/4 each, plus `extra` vertices hung off random lattice
  * vertices in chains of length 1..max_chain (half feeding in from an
