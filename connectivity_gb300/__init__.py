@@ -34,6 +34,8 @@ if not os.path.exists(LIB_PATH):
 _lib = C.CDLL(LIB_PATH)
 
 GB_OK = 0
+(GB_ERR_INVALID, GB_ERR_CUDA, GB_ERR_OOM, GB_ERR_TIMEOUT, GB_ERR_ITER_LIMIT, GB_ERR_IO,
+ GB_ERR_NO_DEVICE, GB_ERR_UNSUPPORTED, GB_ERR_CAPACITY) = range(1, 10)
 STATUS_NAMES = {
     0: "GB_OK", 1: "GB_ERR_INVALID", 2: "GB_ERR_CUDA", 3: "GB_ERR_OOM",
     4: "GB_ERR_TIMEOUT", 5: "GB_ERR_ITER_LIMIT", 6: "GB_ERR_IO",
@@ -116,6 +118,23 @@ for _n in ("gb_batch_scc", "gb_batch_wcc"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
 _sig("gb_batch_scc_async", C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
 _sig("gb_batch_destroy", C.c_int32, [_P])
+
+
+class ServerStats(C.Structure):
+    """gb_server_stats."""
+    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("mean_batch", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("graphs_per_s", C.c_double)]
+
+
+_sig("gb_server_create", C.c_int32, [_P, C.c_int64, C.c_int32, C.POINTER(_P)])
+_sig("gb_server_start", C.c_int32, [_P])
+_sig("gb_server_submit", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int64, _P, _P, _P, C.c_int64,
+                                     _I64P])
+_sig("gb_server_wait", C.c_int32, [_P, C.c_int64, _I64P])
+_sig("gb_server_drain", C.c_int32, [_P])
+_sig("gb_server_stats_get", C.c_int32, [_P, C.POINTER(ServerStats)])
+_sig("gb_server_destroy", C.c_int32, [_P])
 _sig("gb_graph_csr_to_host", C.c_int32, [_P, _P, _P, _P, _P])
 _sig("gb_graph_device_csr", C.c_int32, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
                                         C.POINTER(_P)])
@@ -488,6 +507,71 @@ class Batch:
         if self._h:
             _lib.gb_batch_destroy(self._h)
             self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A request loop with continuous batching (gb_server) over one Context.
+
+    submit() takes host edge arrays and returns a request id; the labels
+    land in the array returned by result() once wait() has returned.  The
+    arrays passed to submit() are kept alive here until the request is done.
+    """
+
+    SCC, WCC = 0, 1
+
+    def __init__(self, ctx: Context, budget_bytes: int = 0, max_graphs: int = 4096):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(_lib.gb_server_create(ctx._h, int(budget_bytes), int(max_graphs), C.byref(h)),
+               "gb_server_create")
+        self._h = h
+        self._keep: dict[int, tuple] = {}
+
+    def start(self) -> None:
+        _check(_lib.gb_server_start(self._h), "gb_server_start")
+
+    def submit(self, kind: int, n: int, src, dst, arrival_ns: int = -1,
+               out: np.ndarray | None = None) -> int:
+        s = np.ascontiguousarray(src, np.int32)
+        d = np.ascontiguousarray(dst, np.int32)
+        if s.shape != d.shape:
+            raise ValueError("src and dst differ in length")
+        lab = out if out is not None else np.empty(n, np.int32)
+        if lab.dtype != np.int32 or lab.size < n or not lab.flags.c_contiguous:
+            raise ValueError("out must be a contiguous int32 array of n entries")
+        rid = C.c_int64()
+        _check(_lib.gb_server_submit(self._h, int(kind), int(n), s.size, _ptr(s), _ptr(d),
+                                     _ptr(lab), int(arrival_ns), C.byref(rid)), "gb_server_submit")
+        self._keep[rid.value] = (s, d, lab)
+        return rid.value
+
+    def wait(self, rid: int) -> tuple[np.ndarray, float]:
+        """Labels and latency (ms) of request rid."""
+        lat = C.c_int64()
+        st = _lib.gb_server_wait(self._h, int(rid), C.byref(lat))
+        keep = self._keep.pop(rid, None)
+        _check(st, "gb_server_wait")
+        return keep[2], lat.value / 1e6
+
+    def drain(self) -> None:
+        _check(_lib.gb_server_drain(self._h), "gb_server_drain")
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(_lib.gb_server_stats_get(self._h, C.byref(s)), "gb_server_stats_get")
+        return s
+
+    def close(self) -> None:
+        if self._h:
+            _lib.gb_server_destroy(self._h)
+            self._h = C.c_void_p()
+            self._keep.clear()
 
     def __del__(self):
         try:

@@ -113,25 +113,37 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
 
 namespace gb {
 
+cudaError_t dev_alloc(void** p, size_t bytes, bool pooled, cudaStream_t s) {
+  return pooled ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+}
+
+void dev_free(void* p, bool pooled, cudaStream_t s) {
+  if (!p) return;
+  if (pooled) cudaFreeAsync(p, s);
+  else cudaFree(p);
+}
+
 gb_status graph_alloc(gb_graph* g, bool with_in) {
   const size_t offb = (size_t)(g->n + 1) * 8, adjb = (size_t)(g->m > 0 ? g->m : 1) * 4;
-  CK(cudaMalloc(&g->out_off, offb), "graph allocation");
-  CK(cudaMalloc(&g->out_adj, adjb), "graph allocation");
+  cudaStream_t s = g->pool_stream;
+  CK(dev_alloc((void**)&g->out_off, offb, g->pooled, s), "graph allocation");
+  CK(dev_alloc((void**)&g->out_adj, adjb, g->pooled, s), "graph allocation");
   if (with_in) {
-    CK(cudaMalloc(&g->in_off, offb), "graph allocation");
-    CK(cudaMalloc(&g->in_adj, adjb), "graph allocation");
+    CK(dev_alloc((void**)&g->in_off, offb, g->pooled, s), "graph allocation");
+    CK(dev_alloc((void**)&g->in_adj, adjb, g->pooled, s), "graph allocation");
   }
   return GB_OK;
 }
 
 void graph_free(gb_graph* g) {
   if (!g) return;
-  cudaFree(g->out_off);
-  cudaFree(g->out_adj);
-  cudaFree(g->in_off);
-  cudaFree(g->in_adj);
-  cudaFree(g->hint_out);
-  cudaFree(g->hint_in);
+  cudaStream_t s = g->pool_stream;
+  dev_free(g->out_off, g->pooled, s);
+  dev_free(g->out_adj, g->pooled, s);
+  dev_free(g->in_off, g->pooled, s);
+  dev_free(g->in_adj, g->pooled, s);
+  dev_free(g->hint_out, g->pooled, s);
+  dev_free(g->hint_in, g->pooled, s);
   g->out_off = g->in_off = nullptr;
   g->out_adj = g->in_adj = nullptr;
   g->hint_out = g->hint_in = nullptr;
@@ -140,14 +152,13 @@ void graph_free(gb_graph* g) {
 // Builds the pull hints of a graph whose CSR is complete on the device.
 gb_status graph_hints(gb_ctx* c, gb_graph* g) {
   const size_t hb = (size_t)(g->n > 0 ? g->n : 1) * 4;
-  CK(cudaMalloc(&g->hint_out, hb), "hint allocation");
-  if (!g->symmetric) CK(cudaMalloc(&g->hint_in, hb), "hint allocation");
+  CK(dev_alloc((void**)&g->hint_out, hb, g->pooled, g->pool_stream), "hint allocation");
+  if (!g->symmetric) CK(dev_alloc((void**)&g->hint_in, hb, g->pooled, g->pool_stream), "hint allocation");
   CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
                      c->stream),
      "hints");
   return GB_OK;
 }
-
 }  // namespace gb
 
 namespace {
@@ -467,8 +478,10 @@ int32_t gb_ctx_reach_trace2(gb_ctx* c, int64_t* t_ns, int32_t* count, int32_t* m
   return k;
 }
 
-gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
-                              const int32_t* dst, gb_graph** out) {
+}  // extern "C"
+
+gb_status gb::graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
+                               const int32_t* dst, bool pooled, gb_graph** out) {
   if (!c || !out || n < 0 || m < 0 || (m > 0 && (!src || !dst))) return GB_ERR_INVALID;
   *out = nullptr;
   CK(cudaSetDevice(c->device), "cudaSetDevice");
@@ -477,12 +490,14 @@ gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* sr
   g->device = c->device;
   g->n = n;
   g->m = m;
+  g->pooled = pooled;
+  g->pool_stream = c->stream;
   gb_status s = graph_alloc(g, true);
   const int32_t *ds = src, *dd = dst;
   int32_t *ts = nullptr, *tt = nullptr;
   if (s == GB_OK && m > 0 && !is_device_ptr(src)) {
-    cudaError_t e = cudaMalloc(&ts, (size_t)m * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&tt, (size_t)m * 4);
+    cudaError_t e = gb::dev_alloc((void**)&ts, (size_t)m * 4, pooled, c->stream);
+    if (e == cudaSuccess) e = gb::dev_alloc((void**)&tt, (size_t)m * 4, pooled, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ts, src, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(tt, dst, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) s = cuda_fail(e, "edge upload");
@@ -499,8 +514,8 @@ gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* sr
       s = GB_ERR_INVALID;
     }
   }
-  cudaFree(ts);
-  cudaFree(tt);
+  gb::dev_free(ts, pooled, c->stream);
+  gb::dev_free(tt, pooled, c->stream);
   if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
@@ -511,9 +526,18 @@ gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* sr
   return GB_OK;
 }
 
+extern "C" {
+
+gb_status gb_graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
+                              const int32_t* dst, gb_graph** out) {
+  return gb::graph_from_edges(c, n, m, src, dst, false, out);
+}
+
 // Validates CSR arrays already on the device: off[0] == 0, off[n] == m,
 // offsets non-decreasing, ids in [0, n).
 }  // extern "C"
+
+gb_status gb::reserve_workspace(gb_ctx* c, int32_t n) { return ensure_ws(c, n); }
 
 gb_status gb::validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off,
                            const int32_t* adj) {

@@ -34,13 +34,23 @@ struct gb_graph {
   int32_t* in_adj = nullptr;
   int32_t* hint_out = nullptr;  // pull hints (null for the drop-in staging graph)
   int32_t* hint_in = nullptr;
+  bool pooled = false;          // arrays from the stream-ordered pool
+  cudaStream_t pool_stream = nullptr;
 };
 
 
+struct gb_batch;
+
 namespace gb {
+// Device allocation from cudaMalloc, or from the stream-ordered pool on
+// stream s (pooled); the matching free.
+cudaError_t dev_alloc(void** p, size_t bytes, bool pooled, cudaStream_t s);
+void dev_free(void* p, bool pooled, cudaStream_t s);
 // Records a CUDA failure for gb_last_error and maps it to a status.
 gb_status cuda_fail(cudaError_t e, const char* where);
 bool is_device_ptr(const void* p);
+// Grows the context workspace to at least n vertices.
+gb_status reserve_workspace(gb_ctx* c, int32_t n);
 gb_status graph_alloc(gb_graph* g, bool with_in);
 void graph_free(gb_graph* g);
 gb_status graph_hints(gb_ctx* c, gb_graph* g);
@@ -49,4 +59,14 @@ gb_status validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off, cons
 // local to each graph.
 gb_status run_graph(gb_ctx* c, const gb_graph* g, RunKind kind, int32_t* labels,
                     const gb_opts* o, gb_stats* st, bool wait, const BatchView* bv);
+// Graph from an edge list; pooled graphs take their arrays from the
+// context stream's pool and free them on that stream.
+gb_status graph_from_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src,
+                           const int32_t* dst, bool pooled, gb_graph** out);
+// Batch from a concatenated global-id edge list (host or device).
+gb_status batch_create(gb_ctx* c, int32_t count, const int64_t* vbase, int64_t m,
+                       const int32_t* src, const int32_t* dst, bool check_edges, bool pooled,
+                       gb_batch** out);
+gb_status batch_run(gb_ctx* c, const gb_batch* b, RunKind kind, int32_t* labels,
+                    const gb_opts* o, gb_stats* st, bool wait);
 }  // namespace gb

@@ -32,6 +32,8 @@ struct gb_batch {
   int32_t id_bits = 1;
   int32_t score_bits_scc = 0;   // bits of the largest out*in product
   int32_t score_bits_wcc = 0;   // bits of the largest total degree
+  bool pooled = false;
+  cudaStream_t pool_stream = nullptr;
 };
 
 namespace {
@@ -55,11 +57,11 @@ void batch_free(gb_batch* b) {
     delete b->g;
     b->g = nullptr;
   }
-  cudaFree(b->d_vbase);
-  cudaFree(b->d_gid);
-  cudaFree(b->d_pkey);
-  cudaFree(b->d_gmin);
-  cudaFree(b->d_roots);
+  gb::dev_free(b->d_vbase, b->pooled, b->pool_stream);
+  gb::dev_free(b->d_gid, b->pooled, b->pool_stream);
+  gb::dev_free(b->d_pkey, b->pooled, b->pool_stream);
+  gb::dev_free(b->d_gmin, b->pooled, b->pool_stream);
+  gb::dev_free(b->d_roots, b->pooled, b->pool_stream);
   b->d_vbase = nullptr;
   b->d_gid = nullptr;
   b->d_pkey = nullptr;
@@ -73,13 +75,16 @@ gb_status batch_finish(gb_ctx* c, gb_batch* b, const int32_t* d_src, const int32
                        bool check_edges) {
   const int32_t n = b->g->n;
   const int32_t count = b->count;
-  CKB(cudaMalloc(&b->d_vbase, (size_t)(count + 1) * 8), "batch allocation");
-  CKB(cudaMemcpy(b->d_vbase, b->vbase.data(), (size_t)(count + 1) * 8, cudaMemcpyHostToDevice),
+  const bool pl = b->pooled;
+  cudaStream_t ps = b->pool_stream;
+  CKB(gb::dev_alloc((void**)&b->d_vbase, (size_t)(count + 1) * 8, pl, ps), "batch allocation");
+  CKB(cudaMemcpyAsync(b->d_vbase, b->vbase.data(), (size_t)(count + 1) * 8, cudaMemcpyHostToDevice,
+                      c->stream),
       "batch upload");
-  CKB(cudaMalloc(&b->d_gid, (size_t)(n > 0 ? n : 1) * 4), "batch allocation");
-  CKB(cudaMalloc(&b->d_pkey, (size_t)(count > 0 ? count : 1) * 8), "batch allocation");
-  CKB(cudaMalloc(&b->d_gmin, (size_t)(count > 0 ? count : 1) * 4), "batch allocation");
-  CKB(cudaMalloc(&b->d_roots, (size_t)(count > 0 ? count : 1) * 4), "batch allocation");
+  CKB(gb::dev_alloc((void**)&b->d_gid, (size_t)(n > 0 ? n : 1) * 4, pl, ps), "batch allocation");
+  CKB(gb::dev_alloc((void**)&b->d_pkey, (size_t)(count > 0 ? count : 1) * 8, pl, ps), "batch allocation");
+  CKB(gb::dev_alloc((void**)&b->d_gmin, (size_t)(count > 0 ? count : 1) * 4, pl, ps), "batch allocation");
+  CKB(gb::dev_alloc((void**)&b->d_roots, (size_t)(count > 0 ? count : 1) * 4, pl, ps), "batch allocation");
   CKB(gb::batch_gid(n, b->d_vbase, count, b->d_gid, c->stream), "batch gid");
   if (check_edges && b->g->m > 0) {
     int bad = 0;
@@ -101,7 +106,7 @@ gb_status batch_finish(gb_ctx* c, gb_batch* b, const int32_t* d_src, const int32
 
 gb_status batch_from_union(gb_ctx* c, int32_t count, const int64_t* vbase, int64_t m,
                            const int32_t* src, const int32_t* dst, bool check_edges,
-                           gb_batch** out) {
+                           bool pooled, gb_batch** out) {
   if (!c || !out || count < 1 || !vbase || m < 0 || (m > 0 && (!src || !dst))) {
     gb_set_error("batch: %s", "bad argument");
     return GB_ERR_INVALID;
@@ -117,25 +122,28 @@ gb_status batch_from_union(gb_ctx* c, int32_t count, const int64_t* vbase, int64
   gb_batch* b = new (std::nothrow) gb_batch();
   if (!b) return GB_ERR_OOM;
   b->count = count;
+  b->pooled = pooled;
+  b->pool_stream = c->stream;
   b->vbase.assign(vbase, vbase + count + 1);
-  gb_status s = gb_graph_from_edges(c, (int32_t)vbase[count], m, src, dst, &b->g);
+  gb_status s = gb::graph_from_edges(c, (int32_t)vbase[count], m, src, dst, pooled, &b->g);
   if (s == GB_OK) {
     // the checks need device copies of the edges; from_edges already
     // validated ids against n, so only the within-graph rule remains
     const int32_t *ds = src, *dd = dst;
     int32_t *ts = nullptr, *tt = nullptr;
     if (check_edges && m > 0 && !gb::is_device_ptr(src)) {
-      if (cudaMalloc(&ts, (size_t)m * 4) != cudaSuccess || cudaMalloc(&tt, (size_t)m * 4) != cudaSuccess ||
-          cudaMemcpy(ts, src, (size_t)m * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-          cudaMemcpy(tt, dst, (size_t)m * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+      if (gb::dev_alloc((void**)&ts, (size_t)m * 4, pooled, c->stream) != cudaSuccess ||
+          gb::dev_alloc((void**)&tt, (size_t)m * 4, pooled, c->stream) != cudaSuccess ||
+          cudaMemcpyAsync(ts, src, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+          cudaMemcpyAsync(tt, dst, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
         s = GB_ERR_OOM;
       }
       ds = ts;
       dd = tt;
     }
     if (s == GB_OK) s = batch_finish(c, b, ds, dd, check_edges);
-    cudaFree(ts);
-    cudaFree(tt);
+    gb::dev_free(ts, pooled, c->stream);
+    gb::dev_free(tt, pooled, c->stream);
   }
   if (s != GB_OK) {
     batch_free(b);
@@ -146,8 +154,8 @@ gb_status batch_from_union(gb_ctx* c, int32_t count, const int64_t* vbase, int64
   return GB_OK;
 }
 
-gb_status batch_run(gb_ctx* c, const gb_batch* b, gb::RunKind kind, int32_t* labels,
-                    const gb_opts* o, gb_stats* st, bool wait) {
+gb_status batch_run_impl(gb_ctx* c, const gb_batch* b, gb::RunKind kind, int32_t* labels,
+                         const gb_opts* o, gb_stats* st, bool wait) {
   if (!b) return GB_ERR_INVALID;
   const int sb = kind == gb::kSCC ? b->score_bits_scc : b->score_bits_wcc;
   if (sb + b->id_bits > 63) {
@@ -167,11 +175,22 @@ gb_status batch_run(gb_ctx* c, const gb_batch* b, gb::RunKind kind, int32_t* lab
 
 }  // namespace
 
+gb_status gb::batch_create(gb_ctx* c, int32_t count, const int64_t* vbase, int64_t m,
+                           const int32_t* src, const int32_t* dst, bool check_edges, bool pooled,
+                           gb_batch** out) {
+  return batch_from_union(c, count, vbase, m, src, dst, check_edges, pooled, out);
+}
+
+gb_status gb::batch_run(gb_ctx* c, const gb_batch* b, RunKind kind, int32_t* labels,
+                        const gb_opts* o, gb_stats* st, bool wait) {
+  return batch_run_impl(c, b, kind, labels, o, st, wait);
+}
+
 extern "C" {
 
 gb_status gb_batch_from_edges(gb_ctx* c, int32_t count, const int64_t* vbase, int64_t m,
                               const int32_t* src, const int32_t* dst, gb_batch** out) {
-  return batch_from_union(c, count, vbase, m, src, dst, true, out);
+  return batch_from_union(c, count, vbase, m, src, dst, true, false, out);
 }
 
 gb_status gb_batch_rmat(gb_ctx* c, int32_t count, const int32_t* n, const int32_t* ef,
@@ -191,7 +210,7 @@ gb_status gb_batch_rmat(gb_ctx* c, int32_t count, const int32_t* n, const int32_
   CKB(gb::batch_edges_device(count, n, ef, seeds, gb_rmat_thresholds(a, bb, cc), id_bits, vb.data(),
                              &s, &d, &m, c->stream),
       "batch R-MAT");
-  gb_status st = batch_from_union(c, count, vb.data(), m, s, d, false, out);
+  gb_status st = batch_from_union(c, count, vb.data(), m, s, d, false, false, out);
   cudaFreeAsync(s, c->stream);
   cudaFreeAsync(d, c->stream);
   cudaStreamSynchronize(c->stream);
@@ -220,16 +239,16 @@ gb_status gb_batch_graph(const gb_batch* b, const gb_graph** g) {
 
 gb_status gb_batch_scc(gb_ctx* c, const gb_batch* b, int32_t* labels, const gb_opts* o,
                        gb_stats* st) {
-  return batch_run(c, b, gb::kSCC, labels, o, st, true);
+  return batch_run_impl(c, b, gb::kSCC, labels, o, st, true);
 }
 
 gb_status gb_batch_wcc(gb_ctx* c, const gb_batch* b, int32_t* labels, const gb_opts* o,
                        gb_stats* st) {
-  return batch_run(c, b, gb::kWCC, labels, o, st, true);
+  return batch_run_impl(c, b, gb::kWCC, labels, o, st, true);
 }
 
 gb_status gb_batch_scc_async(gb_ctx* c, const gb_batch* b, int32_t* labels_dev, const gb_opts* o) {
-  return batch_run(c, b, gb::kSCC, labels_dev, o, nullptr, false);
+  return batch_run_impl(c, b, gb::kSCC, labels_dev, o, nullptr, false);
 }
 
 gb_status gb_batch_destroy(gb_batch* b) {

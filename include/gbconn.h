@@ -250,6 +250,47 @@ gb_status gb_batch_scc_async(gb_ctx* ctx, const gb_batch* b, int32_t* labels_dev
                              const gb_opts* opts);
 gb_status gb_batch_destroy(gb_batch* b);
 
+/* ---- serving: a request stream with continuous batching --------------- */
+/* No counterpart in the reference, whose equivalent is one run_scc / run_cc
+ * call per request (multistep/scc_main.cpp:210, cc_main.cpp:184).  A server
+ * owns an engine thread over one context: it admits every request that has
+ * arrived and fits the device-memory budget (at most max_graphs per merged
+ * run), merges them into one SCC and one WCC batch, and delivers each
+ * request's labels -- identical to the graph's own gb_scc / gb_wcc labels --
+ * into the caller's host buffer.  The next requests' edges are copied to the
+ * device while the current merged runs compute.  Graph state comes from the
+ * stream-ordered device pool.  While a server runs, its context must not be
+ * used by other calls. */
+typedef struct gb_server gb_server;
+typedef struct gb_server_stats {
+  int64_t completed;   /* requests finished */
+  int64_t batches;     /* merged runs (an SCC and a WCC part count as one) */
+  double mean_batch;   /* requests per merged run */
+  double p50_ms;       /* latency = completion - arrival */
+  double p99_ms;
+  double max_ms;
+  double graphs_per_s; /* completed / (last completion - first arrival) */
+} gb_server_stats;
+/* budget_bytes <= 0: half the device's free memory at creation. */
+gb_status gb_server_create(gb_ctx* ctx, int64_t budget_bytes, int32_t max_graphs,
+                           gb_server** server);
+/* Starts the engine and the server clock (t = 0). */
+gb_status gb_server_start(gb_server* server);
+/* kind 0 = SCC, 1 = WCC.  src / dst / labels_out are host arrays that stay
+ * valid until the request completes.  arrival_ns: arrival time on the server
+ * clock; the engine does not admit the request before it (a negative value
+ * means now).  GB_ERR_CAPACITY: the request alone exceeds the budget. */
+gb_status gb_server_submit(gb_server* server, int32_t kind, int32_t n, int64_t m,
+                           const int32_t* src, const int32_t* dst, int32_t* labels_out,
+                           int64_t arrival_ns, int64_t* id);
+/* Blocks until request id completes; its status and latency. */
+gb_status gb_server_wait(gb_server* server, int64_t id, int64_t* latency_ns);
+/* Blocks until every submitted request completes; the first error seen. */
+gb_status gb_server_drain(gb_server* server);
+gb_status gb_server_stats_get(gb_server* server, gb_server_stats* stats);
+/* Finishes the requests in flight, stops the engine and frees everything. */
+gb_status gb_server_destroy(gb_server* server);
+
 /* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
