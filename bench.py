@@ -17,6 +17,16 @@ e2e   : the reference-shaped C-ABI call gb_run_scc (the run_scc signature
 For N > 1 (torchrun) every rank runs a replica on its own GPU ("replicas
 only": the path does not shard), barrier + max time over ranks.
 
+batched: 20,000 R-MAT graphs (vertex counts log-normal, median 2,000, sigma
+        1.5, clipped to 64..500,000; edge factor uniform in 4..32) resident
+        as one batch; graphs/s of one batched SCC run against back-to-back
+        per-graph runs of the same graphs (a sample), labels compared.
+served: a Poisson stream (20,000 requests/s, 80% SCC / 20% WCC) of graphs
+        from the same distribution through gb_server from pinned host
+        buffers; p50/p99 latency and graphs/s, against the same arrivals
+        served by launching each request alone (graph build + run + labels
+        to host, first come first served, measured service times).
+
 --impl reference times the reference algorithm on the host cores: the CPU
 restatement in oracle/ (OpenMP, all threads) on the same graph, each step
 one full run.
@@ -36,11 +46,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "SCC GTEPS on R-MAT-24 (1 GB300) vs host OpenMP; batched graphs/s and p99 ms"
 SCALE, EF, SEED = 24, 16, 1
+BATCH_COUNT = 20000
+BATCH_DIST = dict(seed=4, median=2000.0, sigma=1.5, n_min=64, n_max=500000, ef_min=4, ef_max=32)
 ABC = (0.57, 0.19, 0.19)
 
 
-def workload_name(n, m):
-    return (f"R-MAT scale {SCALE}, edge factor {EF}, a=0.57 b=0.19 c=0.19, seed {SEED}, "
+def workload_name(n, m, scale=SCALE):
+    return (f"R-MAT scale {scale}, edge factor {EF}, a=0.57 b=0.19 c=0.19, seed {SEED}, "
             f"self-loops and duplicates removed ({n:,} vertices, {m:,} edges); SCC")
 
 
@@ -53,6 +65,13 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--cpu-reps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--scale", type=int, default=SCALE,
+                   help="R-MAT scale of the headline graph (smaller only for profiling)")
+    p.add_argument("--sections", default="headline,batched,served",
+                   help="comma list of headline, batched, served")
+    p.add_argument("--serve-rate", type=float, default=20000.0)
+    p.add_argument("--serve-seconds", type=float, default=1.5)
+    p.add_argument("--serve-pool", type=int, default=400)
     return p.parse_args()
 
 
@@ -189,6 +208,144 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batched_section(gb, ctx, stream, steps, sample=400):
+    """graphs/s of one batched SCC run over BATCH_COUNT resident graphs,
+    against back-to-back per-graph runs of a sample of the same graphs."""
+    import numpy as np
+    import torch
+    ns, efs, seeds = gb.batch_sizes(BATCH_COUNT, **BATCH_DIST)
+    t0 = time.time()
+    b = gb.Batch.rmat(ctx, ns, efs, seeds)
+    build_s = time.time() - t0
+    labels = torch.empty(max(b.n, 1), dtype=torch.int32, device="cuda")
+    o = gb.opts()
+    for _ in range(3):
+        ctx.batch_scc_async(b, labels.data_ptr(), o)
+    ctx.sync()
+    K = max(1, steps)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        ctx.batch_scc_async(b, labels.data_ptr(), o)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    t_scc = e0.elapsed_time(e1) / 1e3 / K
+    batch_lab = labels[:b.n].cpu().numpy()
+    wl = torch.empty_like(labels)
+    ctx.batch_wcc(b, labels=wl.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        ctx.batch_wcc(b, labels=wl.data_ptr())
+    t_wcc = (time.perf_counter() - t0) / K
+    # per-graph launches: the first `sample` graphs, resident, one run each
+    S = min(sample, b.count)
+    gs = [gb.Graph.rmat_n(ctx, int(ns[i]), int(efs[i]), int(seeds[i])) for i in range(S)]
+    outs = [torch.empty(max(g.n, 1), dtype=torch.int32, device="cuda") for g in gs]
+    for g, lab in zip(gs[:20], outs[:20]):
+        ctx.scc_async(g, lab.data_ptr(), o)
+    ctx.sync()
+    e0.record(stream)
+    for g, lab in zip(gs, outs):
+        ctx.scc_async(g, lab.data_ptr(), o)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.sync()
+    t_alone = e0.elapsed_time(e1) / 1e3
+    same = all(np.array_equal(outs[i][:gs[i].n].cpu().numpy(),
+                              batch_lab[b.vbase[i]:b.vbase[i + 1]]) for i in range(S))
+    out = {
+        "workload": (f"{b.count:,} R-MAT graphs, vertex counts log-normal (median 2,000, sigma "
+                     f"1.5, clipped 64..500,000), edge factor uniform 4..32 ({b.n:,} vertices, "
+                     f"{b.m:,} edges), one disjoint-union CSR resident in HBM"),
+        "graphs_per_s": round(b.count / t_scc, 1), "ms_per_batch": round(t_scc * 1e3, 3),
+        "steps": K, "gteps": round(b.m / t_scc / 1e9, 2),
+        "wcc_graphs_per_s": round(b.count / t_wcc, 1),
+        "per_graph_graphs_per_s": round(S / t_alone, 1),
+        "per_graph_sample": f"first {S} graphs of the batch, resident, gb_scc_async back to back",
+        "speedup_vs_per_graph": round((b.count / t_scc) / (S / t_alone), 1),
+        "labels_equal_per_graph_runs": bool(same), "build_s": round(build_s, 2),
+    }
+    for g in gs:
+        g.close()
+    b.close()
+    return out
+
+
+def served_section(gb, device, rate, seconds, pool_size):
+    """gb_server under a Poisson stream; the same arrivals served by one
+    launch per request (FIFO over measured per-request service times)."""
+    import numpy as np
+    import torch
+    ns, efs, seeds = gb.batch_sizes(pool_size, **BATCH_DIST)
+    pool = []
+    for i in range(pool_size):
+        n, s, d = gb.rmat_edges_n(int(ns[i]), int(efs[i]), int(seeds[i]))
+        pool.append((n, torch.from_numpy(s).pin_memory().numpy(),
+                     torch.from_numpy(d).pin_memory().numpy()))
+    rng = np.random.default_rng(1)
+    cnt = int(max(200, rate * seconds))
+    kinds = (rng.random(cnt) < 0.2).astype(np.int32)
+    idx = rng.integers(0, pool_size, cnt)
+    arr = (np.cumsum(rng.exponential(1e9 / rate, cnt)) + 2e6).astype(np.int64)
+    ctx = gb.Context(device)
+
+    def alone(i, kind, out=None):
+        n, s, d = pool[i]
+        g = gb.Graph.from_edges(ctx, n, s, d)
+        lab = ctx.scc(g, labels=out) if kind == 0 else ctx.wcc(g, labels=out)
+        g.close()
+        return lab
+
+    for i in range(min(20, pool_size)):
+        alone(i, 0)
+    svc = np.zeros((pool_size, 2))
+    for i in range(pool_size):
+        for k in (0, 1):
+            t0 = time.perf_counter()
+            alone(i, k)
+            svc[i, k] = time.perf_counter() - t0
+    fin, lat = 0.0, np.zeros(cnt)
+    for j in range(cnt):
+        a = arr[j] / 1e9
+        fin = max(a, fin) + svc[idx[j], kinds[j]]
+        lat[j] = fin - a
+    alone_gps = cnt / (fin - arr[0] / 1e9)
+    outs = [np.empty(pool[i][0], np.int32) for i in idx]
+    sctx = gb.Context(device)
+    sv = gb.Server(sctx, budget_bytes=0, max_graphs=8192)
+    for j in range(cnt):
+        n, s, d = pool[idx[j]]
+        sv.submit(int(kinds[j]), n, s, d, arrival_ns=int(arr[j]), out=outs[j])
+    sv.start()
+    sv.drain()
+    st = sv.stats()
+    h2d = int(sum(pool[i][1].size * 8 for i in idx))
+    d2h = int(sum(pool[i][0] * 4 for i in idx))
+    sv.close()
+    sctx.close()
+    step = max(1, cnt // 200)
+    same = all(np.array_equal(outs[j], alone(idx[j], kinds[j])) for j in range(0, cnt, step))
+    ctx.close()
+    return {
+        "workload": (f"Poisson arrivals at {rate:,.0f} graphs/s for {seconds:g} s ({cnt:,} "
+                     f"requests, 80% SCC / 20% WCC), graphs drawn from {pool_size} of the batched "
+                     "size distribution, edges in pinned host memory, labels to host"),
+        "graphs_per_s": round(st.graphs_per_s, 1), "p50_ms": round(st.p50_ms, 3),
+        "p99_ms": round(st.p99_ms, 3), "max_ms": round(st.max_ms, 3),
+        "mean_merged": round(st.mean_batch, 1), "merged_runs": int(st.batches),
+        "h2d_bytes": h2d, "d2h_bytes": d2h,
+        "alone_graphs_per_s": round(alone_gps, 1),
+        "alone_p50_ms": round(float(np.median(lat)) * 1e3, 3),
+        "alone_p99_ms": round(float(np.quantile(lat, 0.99)) * 1e3, 3),
+        "alone_mean_service_ms": round(float(svc.mean()) * 1e3, 3),
+        "speedup_vs_alone": round(st.graphs_per_s / alone_gps, 1),
+        "labels_equal_alone": bool(same), "labels_checked": len(range(0, cnt, step)),
+    }
+
+
 def run_gbconn(args):
     import numpy as np
     import torch
@@ -198,6 +355,7 @@ def run_gbconn(args):
         __graft_entry__.build()
     import connectivity_gb300 as gb
 
+    sections = set(x.strip() for x in args.sections.split(",") if x.strip())
     ws, rank, local = dist()
     torch.cuda.set_device(local)
     if ws > 1:
@@ -218,15 +376,19 @@ def run_gbconn(args):
         return float(t.item())
 
     ctx = gb.Context(local)
-    stream = torch.cuda.current_stream()
+    # a stream of our own: the library runs on it and the CUDA events are
+    # recorded on it (torch's default stream is the legacy stream, handle 0,
+    # which the library reads as "use the context's own stream")
+    stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
-    g = gb.Graph.rmat(ctx, SCALE, EF, SEED, ABC)
+    g = gb.Graph.rmat(ctx, args.scale, EF, SEED, ABC)
     n, m = g.n, g.m
     labels = torch.empty(n, dtype=torch.int32, device="cuda")
     o = gb.opts()
 
     # warm-up
-    for _ in range(max(args.warmup, 3)):
+    W = max(args.warmup, 3)
+    for _ in range(W):
         ctx.scc_async(g, labels.data_ptr(), o)
     ctx.sync()
 
@@ -256,7 +418,7 @@ def run_gbconn(args):
     T = e0.elapsed_time(e1) / 1e3
     T = allmax(T)
     phases = ctx.phase_times(min(K, 64))
-    reach_ms = float(phases[:, 1].mean())
+    pm = phases.mean(axis=0)
     step_ms = T / K * 1e3
     value = ws * m / (T / K) / 1e9
 
@@ -283,12 +445,18 @@ def run_gbconn(args):
     d2h = n * 4
 
     peak, peak_kind = peaks()
-    achieved = st.bytes_reach / (reach_ms / 1e3) / 1e9
+
+    def roof(kernel, nbytes, ms):
+        a = nbytes / (ms / 1e3) / 1e9
+        return {"kernel": kernel, "achieved": round(a, 1), "frac": round(a / peak, 4),
+                "algorithmic_bytes_per_launch": int(nbytes), "launch_ms": round(ms, 4)}
+
+    reach = roof("k_reach", st.bytes_reach, float(pm[1]))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": K,
-        "warmup": max(args.warmup, 3), "ms_per_step": round(step_ms, 4), "higher_is_better": True,
+        "warmup": W, "ms_per_step": round(step_ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": workload_name(n, m),
+        "config": {"workload": workload_name(n, m, args.scale),
                    "l2": "inputs larger than L2 (2.1 GB CSR, 129 MB L2); no flush",
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "trim_level": 1, "labels": "canonical minimum member id, device memory"},
@@ -298,14 +466,17 @@ def run_gbconn(args):
                 "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers)",
                 "labels_match_device_run": e2e_ok},
         "roofline": {"bound": "hbm", "kernel": "k_reach (FW-BW reachability + commit)",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                     "achieved": reach["achieved"], "peak": peak, "unit": "GB/s",
+                     "frac": reach["frac"], "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
                      "traffic": profile_traffic(),
-                     "algorithmic_bytes_per_launch": int(st.bytes_reach),
-                     "launch_ms": round(reach_ms, 4)},
+                     "algorithmic_bytes_per_launch": reach["algorithmic_bytes_per_launch"],
+                     "launch_ms": reach["launch_ms"],
+                     "kernels": [roof("k_trim", st.bytes_trim, float(pm[0])), reach,
+                                 roof("k_colour", st.bytes_colour, float(pm[2]))]},
         "phases_ms": {k: round(float(v), 4) for k, v in
-                      zip(("trim", "reach", "colour", "canon", "total"), phases.mean(axis=0))},
-        "gpu_launches": 5 * K,
+                      zip(("trim", "reach", "colour", "tail", "total"), pm)},
+        "gpu_launches": 4 * K,
+        "gpu_launches_note": "k_trim, k_reach, k_colour and the status latch per step",
         "clocks": ck,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -316,10 +487,16 @@ def run_gbconn(args):
                       "(oracle/multistep.c, OpenMP restatement of run_scc)"}
         line["parity"] = {"labels_equal_oracle": bool(np.array_equal(gpu_labels, want)),
                           "verify_line": gb.scc_verify(gpu_labels).strip()}
+    g.close()
+    del labels
+    if "batched" in sections:
+        line["batched"] = batched_section(gb, ctx, stream, 5)
+    ctx.close()
+    if "served" in sections:
+        line["served"] = served_section(gb, local, args.serve_rate, args.serve_seconds,
+                                        args.serve_pool)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    g.close()
-    ctx.close()
     if ws > 1:
         import torch.distributed as tdist
         tdist.destroy_process_group()

@@ -319,9 +319,11 @@ __device__ __forceinline__ Adj adj_undirected(const GraphView& g) {
 // entries, which keeps the step counters (a single L2 word) cool.
 // ------------------------------------------------------------------------
 constexpr int kWB = 512;
-// Dynamic shared memory of the cooperative kernels: two staging buffers per
-// warp.
-constexpr int kDynSmem = kWarps * 2 * kWB * 4;
+// Per-warp backlog of pull candidates the hint did not settle (entries).
+constexpr int kTodo = 384;
+// Dynamic shared memory of the cooperative kernels: two staging buffers and
+// one pull backlog per warp.
+constexpr int kDynSmem = kWarps * (2 * kWB + kTodo) * 4;
 
 // A global output list.
 struct Out {
@@ -421,9 +423,12 @@ struct Smem {
   int warp_tmp[kWarps + 1];
   long long red_l[kWarps];
   int red_i[kWarps];
-  int32_t* stage_base;  // dynamic shared memory, kWarps x 2 x kWB entries
+  int32_t* stage_base;  // dynamic shared memory: kWarps x 2 x kWB, then kWarps x kTodo
   __device__ __forceinline__ int32_t* stage(int warp, int k) {
     return stage_base + (warp * 2 + k) * kWB;
+  }
+  __device__ __forceinline__ int32_t* todo(int warp) {
+    return stage_base + kWarps * 2 * kWB + warp * kTodo;
   }
 };
 extern __shared__ __align__(16) int32_t g_dyn_smem[];
@@ -691,43 +696,82 @@ struct Args {
 // Ordered compaction: in[0, nin) -> out, keeping the entries whose bit is
 // clear in `drop`, in list order.  Block b owns a contiguous chunk; one
 // barrier between counting and writing.  The survivor count goes to *total.
+template <class F>
 __device__ bool compact_ordered(const int32_t* in, int32_t nin, int32_t* out, const uint32_t* drop,
                                 Work& w, Smem& sm, Steps& st, int where, int32_t* total,
-                                Tally& ty) {
+                                Tally& ty, F on_drop) {
+  // Every warp owns a contiguous range (ranges follow the global warp
+  // order): pass 1 counts what stays and hands every dropped element to
+  // on_drop, one grid barrier publishes the block totals, pass 2 writes
+  // with warp ballots.  kCU elements per lane per iteration keep the loads
+  // overlapped.
+  constexpr int kCU = 8;
+  constexpr long long kCG = 32 * kCU;
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
-  const long long chunk = ((long long)nin + G - 1) / G;
-  const long long lo = chunk * b < nin ? chunk * b : nin;
-  const long long hi = lo + chunk < nin ? lo + chunk : nin;
-  int cnt = 0;
-  for (long long i = lo + t; i < hi; i += T) {
-    if (!bit_get(drop, __ldcg(in + i))) ++cnt;
-    ty.list++;
+  const int warp = t >> 5, lane = t & 31, nwarps = T >> 5;
+  const long long W = (long long)G * nwarps;
+  const long long gw = (long long)b * nwarps + warp;
+  const long long wchunk = (((long long)nin + W - 1) / W + 31) / 32 * 32;
+  const long long wlo = wchunk * gw < nin ? wchunk * gw : nin;
+  const long long whi = wlo + wchunk < nin ? wlo + wchunk : nin;
+  int cnt = 0;  // warp-uniform
+  for (long long base = wlo; base < whi; base += kCG) {
+    int32_t v[kCU];
+#pragma unroll
+    for (int j = 0; j < kCU; ++j) {
+      const long long i = base + j * 32 + lane;
+      v[j] = i < whi ? __ldcg(in + i) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < kCU; ++j) {
+      const bool d = v[j] >= 0 && bit_get(drop, v[j]);
+      if (d) on_drop(v[j]);
+      if (v[j] >= 0) ty.list++;
+      cnt += __popc(__ballot_sync(kFull, v[j] >= 0 && !d));
+    }
   }
-  int tot;
-  block_excl(cnt, tot, sm.warp_tmp);
-  if (t == 0) w.blk_i[b] = tot;
+  // warp offsets inside the block, block total
+  __syncthreads();
+  if (lane == 0) sm.warp_tmp[warp] = cnt;
+  __syncthreads();
+  if (warp == 0) {
+    const int x = lane < nwarps ? sm.warp_tmp[lane] : 0;
+    int incl = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += y;
+    }
+    if (lane < nwarps) sm.warp_tmp[lane] = incl - x;
+    if (lane == 31) w.blk_i[b] = incl;
+  }
+  __syncthreads();
+  const int woff = sm.warp_tmp[warp];
   if (!step_sync(w.ctl, st, where)) return false;
   int pre = 0;
   for (int j = t; j < b; j += T) pre += __ldcg(w.blk_i + j);
-  int boff;
+  const int tot = __ldcg(w.blk_i + b);
+  int boff;  // the block's offset: the sum of the earlier blocks' totals
   block_excl(pre, boff, sm.warp_tmp);
   if (b == G - 1 && t == 0) *total = boff + tot;
-  int run = boff;
-  for (long long i0 = lo; i0 < hi; i0 += T) {
-    const long long i = i0 + t;
-    int32_t v = -1;
-    bool k = false;
-    if (i < hi) {
-      v = __ldcg(in + i);
-      k = !bit_get(drop, v);
+  int run = boff + woff;
+  for (long long base = wlo; base < whi; base += kCG) {
+    int32_t v[kCU];
+#pragma unroll
+    for (int j = 0; j < kCU; ++j) {
+      const long long i = base + j * 32 + lane;
+      v[j] = i < whi ? __ldcg(in + i) : -1;
     }
-    int bt;
-    const int pos = block_excl(k ? 1 : 0, bt, sm.warp_tmp);
-    if (k) {
-      out[run + pos] = v;
-      ty.list++;
+#pragma unroll
+    for (int j = 0; j < kCU; ++j) {
+      const bool k = v[j] >= 0 && !bit_get(drop, v[j]);
+      const unsigned mask = __ballot_sync(kFull, k);
+      if (k) {
+        out[run + __popc(mask & lanemask_lt())] = v[j];
+        ty.list++;
+      }
+      run += __popc(mask);
     }
-    run += bt;
   }
   return true;
 }
@@ -1010,21 +1054,92 @@ struct ReachSpec {
   int stat_slot;
 };
 
-constexpr int kPullU = 4;  // candidates per thread per pull iteration
+constexpr int kPullU = 4;  // backlog candidates per thread per edge pass
+constexpr int kPullA = 8;  // candidates per thread per hint pass
 
 // One pull step: every unreached candidate looks for a reached
 // pull-neighbour (scc_fwbw.cpp:116-149, which scans until the first hit).
 // Three tiers keep the work balanced:
-//   thread: up to kPullThread edges, kPullU candidates per thread with
-//           their loads overlapped;
-//   warp  : candidates with more edges, one warp each, 32 edges per
-//           iteration, up to kPullWarpEdges edges;
+//   thread: a hint pass over kPullA candidates per thread (its loads do not
+//           depend on one another beyond the candidate id), then, for the
+//           candidates the hint did not settle, an edge pass of up to
+//           kPullThread edges, kPullU candidates per thread, run whenever a
+//           warp's backlog holds 32 * kPullU of them;
+//   warp  : candidates with more edges, one warp each, 32 * kPullWU edges
+//           per iteration, up to kPullWarpEdges edges;
 //   block : the rest, one block each, kBlock edges per iteration.
 // The warp and block tiers run after a grid barrier on lists the thread
 // tier filled, spread over the whole grid.  Found candidates are appended
 // to q; candidates with no reached neighbour are kept in cand_next.
 constexpr int kPullThread = 4;
-constexpr long long kPullWarpEdges = 2048;
+constexpr long long kPullWarpEdges = 1024;
+constexpr int kPullWU = 4;  // warp tier: edges per lane per iteration
+static_assert(kTodo >= 32 * kPullU - 1 + 32 * kPullA, "pull backlog too small");
+
+// Edge pass of the pull thread tier over todo[0, cnt) (cnt <= 32 * kPullU;
+// warp-uniform; every candidate is unreached and not settled by its hint).
+template <int NC>
+__device__ __forceinline__ void pull_edges(const ReachSpec& R, const int32_t* todo, int cnt,
+                                           int kt, Stage& sf, Stage& sk, const Out& of,
+                                           const Out& ok, int32_t* wl, int32_t* bl, int32_t* lc,
+                                           int32_t n, Ctl* c, Tally& ty) {
+  const int lane = lane_id();
+  int32_t v[kPullU];
+  bool found[kPullU];
+  long long s0[kPullU], d0[kPullU], s1[kPullU], d1[kPullU];
+  int32_t u[kPullU][kPullThread];
+#pragma unroll
+  for (int j = 0; j < kPullU; ++j) {
+    const int i = j * 32 + lane;
+    v[j] = i < cnt ? todo[i] : -1;
+  }
+#pragma unroll
+  for (int j = 0; j < kPullU; ++j) {
+    s0[j] = d0[j] = s1[j] = d1[j] = 0;
+    if (v[j] >= 0) {
+      rec_load<NC>(R.pull, v[j], s0[j], d0[j], s1[j], d1[j]);
+      ty.vtx += NC;
+    }
+  }
+  // the first kt edges of every candidate, loads overlapped
+#pragma unroll
+  for (int j = 0; j < kPullU; ++j) {
+#pragma unroll
+    for (int e = 0; e < kPullThread; ++e) {
+      u[j][e] = -1;
+      if (v[j] >= 0 && e < kt && e < d0[j] + d1[j]) {
+        int k;
+        u[j][e] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], e, k);
+      }
+    }
+  }
+  bool to_warp[kPullU], to_block[kPullU], keep[kPullU];
+#pragma unroll
+  for (int j = 0; j < kPullU; ++j) {
+    found[j] = false;
+#pragma unroll
+    for (int e = 0; e < kPullThread; ++e) {
+      if (u[j][e] >= 0) {
+        ty.edges++;
+        if (!found[j] && bit_get_l1(R.vis, u[j][e])) found[j] = true;
+      }
+    }
+    const long long d = d0[j] + d1[j];
+    const bool open = v[j] >= 0 && !found[j];
+    to_warp[j] = open && d > kt && d <= kt + kPullWarpEdges;
+    to_block[j] = open && d > kt + kPullWarpEdges;
+    keep[j] = open && d <= kt;
+  }
+#pragma unroll
+  for (int j = 0; j < kPullU; ++j) {
+    // a pull candidate has one owner: its bit is set without a reply
+    if (found[j]) bit_set_red(R.vis, v[j]);
+    stage_push(sf, found[j], v[j], 0ull, of, c);
+    stage_push(sk, keep[j], v[j], 0ull, ok, c);
+    list_append(to_warp[j], v[j], wl, &lc[0], n, c, 204);
+    list_append(to_block[j], v[j], bl, &lc[1], n, c, 205);
+  }
+}
 
 template <int NC>
 __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
@@ -1058,98 +1173,67 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   ok.where = 203;
   Stage sf = stage_make(sm.stage(warp, 0));
   Stage sk = stage_make(sm.stage(warp, 1));
+  int32_t* todo = sm.todo(warp);
+  int ntodo = 0;  // warp-uniform
   int32_t* wl = w.x1;  // warp-tier list
   int32_t* bl = w.h1;  // block-tier list
   const long long nw = (long long)G * (T >> 5);
+  const bool hints = R.pull.c[0].hint != nullptr;
   // block b streams through its own contiguous share of the candidates
-  constexpr long long kGroup = 32 * kPullU;
+  constexpr long long kGroup = 32 * kPullA;
+  constexpr int kEdgeBatch = 32 * kPullU;
   const long long chunk = ((ncur + G - 1) / G + kGroup - 1) / kGroup * kGroup;
   const long long clo = chunk * b < ncur ? chunk * b : ncur;
   const long long chi = clo + chunk < ncur ? clo + chunk : ncur;
   for (long long base = clo + warp * kGroup; base < chi; base += (T >> 5) * kGroup) {
-    int32_t v[kPullU];
-    bool unv[kPullU], found[kPullU];
-    long long s0[kPullU], d0[kPullU], s1[kPullU], d1[kPullU];
-    int32_t u[kPullU][kPullThread];
+    int32_t v[kPullA], h0[kPullA], h1[kPullA];
 #pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
+    for (int j = 0; j < kPullA; ++j) {
       const long long i = base + j * 32 + lane;
       v[j] = i < chi ? __ldcg(cand_cur + i) : -1;
     }
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
     // the hint (the neighbour of largest degree) settles most candidates
-    // without touching the CSR
-    bool hinted[kPullU];
+    // without touching the CSR; it is read before the candidate's own bit
+    // is known so that the two loads overlap
 #pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-      int32_t h0 = -1, h1 = -1;
-      if (unv[j] && R.pull.c[0].hint != nullptr) h0 = __ldg(R.pull.c[0].hint + v[j]);
+    for (int j = 0; j < kPullA; ++j) {
+      h0[j] = (v[j] >= 0 && hints) ? __ldg(R.pull.c[0].hint + v[j]) : -1;
+      h1[j] = -1;
       if constexpr (NC > 1) {
-        if (unv[j] && R.pull.c[1].hint != nullptr) h1 = __ldg(R.pull.c[1].hint + v[j]);
-      }
-      hinted[j] = (h0 >= 0 && bit_get_l1(R.vis, h0)) || (h1 >= 0 && bit_get_l1(R.vis, h1));
-    }
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-      s0[j] = d0[j] = s1[j] = d1[j] = 0;
-      if (unv[j] && !hinted[j]) rec_load<NC>(R.pull, v[j], s0[j], d0[j], s1[j], d1[j]);
-    }
-    // first edge of every candidate, then the next kt-1 of those still open
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-      u[j][0] = -1;
-      if (unv[j] && !hinted[j] && d0[j] + d1[j] > 0) {
-        int k;
-        u[j][0] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], 0, k);
+        if (v[j] >= 0 && R.pull.c[1].hint != nullptr) h1[j] = __ldg(R.pull.c[1].hint + v[j]);
       }
     }
+    bool unv[kPullA];
 #pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-      found[j] = hinted[j] || (u[j][0] >= 0 && bit_get_l1(R.vis, u[j][0]));
+    for (int j = 0; j < kPullA; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
+#pragma unroll
+    for (int j = 0; j < kPullA; ++j) {
+      const bool hinted = unv[j] && ((h0[j] >= 0 && bit_get_l1(R.vis, h0[j])) ||
+                                     (h1[j] >= 0 && bit_get_l1(R.vis, h1[j])));
       if (v[j] >= 0) ty.list++;
-      if (unv[j] && !hinted[j]) {
-        ty.vtx += NC;
-        if (u[j][0] >= 0) ty.edges++;
-      }
+      if (hinted) bit_set_red(R.vis, v[j]);
+      stage_push(sf, hinted, v[j], 0ull, of, c);
+      // the rest go to the warp's backlog
+      const bool open = unv[j] && !hinted;
+      const unsigned mask = __ballot_sync(kFull, open);
+      if (open) todo[ntodo + __popc(mask & lanemask_lt())] = v[j];
+      ntodo += __popc(mask);
     }
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-#pragma unroll
-      for (int e = 1; e < kPullThread; ++e) {
-        u[j][e] = -1;
-        if (unv[j] && !found[j] && e < kt && e < d0[j] + d1[j]) {
-          int k;
-          u[j][e] = adj_at<NC>(R.pull, s0[j], d0[j], s1[j], e, k);
-        }
+    __syncwarp();
+    if (ntodo >= kEdgeBatch) {
+      int done = 0;
+      while (ntodo - done >= kEdgeBatch) {
+        pull_edges<NC>(R, todo + done, kEdgeBatch, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
+        done += kEdgeBatch;
       }
-    }
-    bool to_warp[kPullU], to_block[kPullU], keep[kPullU];
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-#pragma unroll
-      for (int e = 1; e < kPullThread; ++e) {
-        if (u[j][e] >= 0) {
-          ty.edges++;
-          if (!found[j] && bit_get_l1(R.vis, u[j][e])) found[j] = true;
-        }
-      }
-      const long long d = d0[j] + d1[j];
-      const bool open = unv[j] && !found[j];
-      to_warp[j] = open && d > kt && d <= kt + kPullWarpEdges;
-      to_block[j] = open && d > kt + kPullWarpEdges;
-      keep[j] = open && d <= kt;
-    }
-#pragma unroll
-    for (int j = 0; j < kPullU; ++j) {
-      // a pull candidate has one owner: its bit is set without a reply
-      if (found[j]) bit_set_red(R.vis, v[j]);
-      stage_push(sf, found[j], v[j], 0ull, of, c);
-      stage_push(sk, keep[j], v[j], 0ull, ok, c);
-      list_append(to_warp[j], v[j], wl, &lc[0], w.n, c, 204);
-      list_append(to_block[j], v[j], bl, &lc[1], w.n, c, 205);
+      // move the remainder (< kEdgeBatch, from at or above kEdgeBatch) to the front
+      __syncwarp();
+      for (int i = lane; i < ntodo - done; i += 32) todo[i] = todo[done + i];
+      __syncwarp();
+      ntodo -= done;
     }
   }
+  if (ntodo > 0) pull_edges<NC>(R, todo, ntodo, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
   if (pp == 0 && t == 0 && b < kBlkTimes) c->blk_t[b] = gtimer();
   // the warp and block tiers need the complete lists
   if (!grid_barrier(c, 206)) return false;
@@ -1166,19 +1250,27 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
     rec_load<NC>(R.pull, v, s0, d0, s1, d1);
     const long long d = d0 + d1;
     bool found = false;
-    for (long long e0 = kt; e0 < d; e0 += 32) {
-      const long long e = e0 + lane;
+    // kPullWU edges per lane per iteration, loads overlapped
+    for (long long e0 = kt; e0 < d && !found; e0 += 32 * kPullWU) {
+      int32_t x[kPullWU];
+#pragma unroll
+      for (int q = 0; q < kPullWU; ++q) {
+        const long long e = e0 + q * 32 + lane;
+        x[q] = -1;
+        if (e < d) {
+          int k;
+          x[q] = adj_at<NC>(R.pull, s0, d0, s1, e, k);
+        }
+      }
       bool hit = false;
-      if (e < d) {
-        int k;
-        const int32_t x = adj_at<NC>(R.pull, s0, d0, s1, e, k);
-        ty.edges++;
-        hit = bit_get_l1(R.vis, x);
+#pragma unroll
+      for (int q = 0; q < kPullWU; ++q) {
+        if (x[q] >= 0) {
+          ty.edges++;
+          hit = hit || bit_get_l1(R.vis, x[q]);
+        }
       }
-      if (__any_sync(kFull, hit)) {
-        found = true;
-        break;
-      }
+      found = __any_sync(kFull, hit);
     }
     if (found && lane == 0) bit_set_red(R.vis, v);
     stage_push(sf, found && lane == 0, v, 0ull, of, c);
@@ -1396,24 +1488,17 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
     if (!step_sync(c, st, 25)) return;
   }
   const int32_t lab = A.p.canonical ? (batch ? -1 : __ldcg(hit_min)) : pivot;
-  // label the component and take it out of the valid set (update_valid,
-  // scc_fwbw.cpp:425-433)
+  // take the component out of the valid set (update_valid,
+  // scc_fwbw.cpp:425-433) and label it while the valid list is compacted
   for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
     const uint32_t h = __ldcg(hit + wd);
-    if (h) {
-      w.vbits[wd] = __ldcg(w.vbits + wd) & ~h;
-      unsigned x = h;
-      while (x) {
-        const int bit = __ffs(x) - 1;
-        x &= x - 1;
-        const int32_t v = (int32_t)(wd * 32 + bit);
-        w.label[v] = batch ? (A.p.canonical ? __ldcg(g.batch.gmin + __ldg(g.batch.gid + v))
-                                            : v)
-                           : lab;
-      }
-    }
+    if (h) w.vbits[wd] = __ldcg(w.vbits + wd) & ~h;
   }
-  if (!compact_ordered(w.listA, nvalid, w.listB, hit, w, sm, st, 26, &c->nvalid, ty)) return;
+  const bool canon = A.p.canonical != 0;
+  auto put = [&](int32_t v) {
+    w.label[v] = batch ? (canon ? __ldcg(g.batch.gmin + __ldg(g.batch.gid + v)) : v) : lab;
+  };
+  if (!compact_ordered(w.listA, nvalid, w.listB, hit, w, sm, st, 26, &c->nvalid, ty, put)) return;
   if (!step_sync(c, st, 27)) return;
   const int32_t nv = __ldcg(&c->nvalid);
   for (long long i = (long long)b * T + t; i < nv; i += (long long)G * T) w.listA[i] = __ldcg(w.listB + i);
@@ -1542,11 +1627,8 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
       }
     }
     // the labelled vertices leave the valid set; L is compacted into L2
-    for (long long i = gt; i < nl; i += gstride) {
-      const int32_t v = __ldcg(L + i);
-      if (bit_get(w.done, v)) bit_release(w.vbits, v);
-    }
-    if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 37, &c->nvalid, ty)) return;
+    auto release = [&](int32_t v) { bit_release(w.vbits, v); };
+    if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 37, &c->nvalid, ty, release)) return;
     if (!step_sync(c, st, 38)) return;
     const int32_t nn = __ldcg(&c->nvalid);
     labelled += nl - nn;
