@@ -59,7 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 14 * arr + 4 * bm + align256(G * 4) + align256(G * 8);
+  const size_t total = 14 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8);
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -87,7 +87,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.fvis = (uint32_t*)take(bm);
   w.bvis = (uint32_t*)take(bm);
   w.done = (uint32_t*)take(bm);
-  w.blk_i = (int32_t*)take(align256(G * 4));
+  w.blk_i = (int32_t*)take(align256(2 * G * 4));
   w.blk_l = (long long*)take(align256(G * 8));
   w.ctl = c->d_ctl;
   c->cap_n = n;

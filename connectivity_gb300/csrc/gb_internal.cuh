@@ -53,8 +53,9 @@ enum Stat : int {
 };
 
 struct Ctl {
-  unsigned int bar_count;
-  unsigned int bar_gen;
+  // grid barrier word: arrivals so far (low 32 bits, never reset within a
+  // run), bit 63 = an error was raised
+  unsigned long long bar;
   int err;
   int err_where;
   int step;               // step counter, continued by each kernel of a run
@@ -71,6 +72,7 @@ struct Ctl {
   int32_t minv[2];        // smallest vertex reached forward / backward
   int32_t nroots;         // batch: pivots in BatchView::roots
   int32_t lcount[2][2];   // pull steps: warp- and block-tier list lengths
+  long long pnext[2];     // pull steps: next unclaimed candidate of the thread tier
                           // (two sets, used by alternate pull steps)
   int32_t pad1;
   unsigned long long m_cand;   // push-degree sum of the valid list after trim
@@ -78,8 +80,11 @@ struct Ctl {
   // Algorithmic traffic per kernel (trim, reach, colour, canon): vertex
   // offset records read, adjacency entries read, list entries read/written.
   unsigned long long kst[4][3];
-  // Per-step trace of the reachability kernel (last kTrace steps): device
-  // time at the end of the step, vertices appended, mode (1 = pull).
+  // Per-step trace (last kTrace steps): device time at the start of the
+  // step and the step's input count.  Reachability steps: mode bit 0 =
+  // pull, bit 1 = heavy vertices pending, bit 2 = backward search.  Colour
+  // steps: mode 8 = colours reset, 9 = propagation, 10 = roots,
+  // 11 = same-colour marking, 12 = compaction; 15 = end of a kernel.
   struct Trace {
     unsigned long long t;
     unsigned long long t_mid;   // pull steps: end of the thread tier
@@ -132,7 +137,7 @@ struct Work {
   int32_t* candB;
   int32_t* h0;            // heavy-vertex lists
   int32_t* h1;
-  int32_t* blk_i;         // per-block scratch (grid size)
+  int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
   long long* blk_l;
   Ctl* ctl;
 };

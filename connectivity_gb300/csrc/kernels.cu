@@ -39,18 +39,13 @@ __device__ __forceinline__ uint64_t gtimer() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ int ld_vol(const int* p) { return *(volatile const int*)p; }
 
+constexpr unsigned long long kBarErrBit = 1ull << 63;
 __device__ __forceinline__ void set_err(Ctl* c, int code, int where) {
   if (atomicCAS(&c->err, 0, code) == 0) atomicExch(&c->err_where, where);
+  // the barrier word carries the error too, so a barrier needs no second read
+  atomicOr(&c->bar, kBarErrBit);
 }
 
 // Mutable arrays are read through L2 (ld.global.cg) so that a value written
@@ -126,38 +121,48 @@ __device__ int block_excl(int x, int& total, int* sm_warp /* kWarps + 1 */) {
 constexpr unsigned long long kBarrierTimeoutNs = 20ull * 1000ull * 1000ull * 1000ull;
 constexpr unsigned kBarrierMaxSpins = 1u << 28;
 
-// Grid-wide barrier for a cooperative launch.  Every wait is bounded by
-// time and by spin count; on expiry it sets the error flag, and any block
-// that sees the flag leaves its wait.  Returns false when the kernel must
-// stop.
+// Grid-wide barrier for a cooperative launch.  Thread 0 of every block adds
+// one arrival to the barrier word and waits until the arrivals reach the
+// next multiple of the grid size; the word's error bit ends every wait at
+// once.  Every wait is bounded by time and by spin count; on expiry it sets
+// the error.  Returns false when the kernel must stop.
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ bool grid_barrier(Ctl* c, int where) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned gen = ld_acquire(&c->bar_gen);
     __threadfence();
-    const unsigned arrived = atomicAdd(&c->bar_count, 1u) + 1u;
-    if (arrived == gridDim.x) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      st_release(&c->bar_gen, gen + 1u);
-    } else {
+    const unsigned G = gridDim.x;
+    const unsigned long long old = atomicAdd(&c->bar, 1ull);
+    const unsigned arrived = (unsigned)old + 1u;
+    const unsigned target = ((unsigned)old / G + 1u) * G;
+    bool ok = (old & kBarErrBit) == 0ull;
+    if (ok && arrived != target) {
       const uint64_t t0 = gtimer();
       unsigned spins = 0;
-      while (ld_acquire(&c->bar_gen) == gen) {
-        if (ld_vol(&c->err) != 0) break;
-        __nanosleep(64);
+      for (;;) {
+        const unsigned long long v = ld_acquire64(&c->bar);
+        if (v & kBarErrBit) { ok = false; break; }
+        if ((int)((unsigned)v - target) >= 0) break;
+        __nanosleep(32);
         ++spins;
         if (spins >= kBarrierMaxSpins ||
             ((spins & 1023u) == 0u && gtimer() - t0 > kBarrierTimeoutNs)) {
           set_err(c, kErrTimeout, where);
+          ok = false;
           break;
         }
       }
     }
     __threadfence();
+    s_ok = ok ? 1 : 0;
   }
   __syncthreads();
-  return ld_vol(&c->err) == 0;
+  return s_ok != 0;
 }
 
 // Step bookkeeping: step s reads ring[s%3], appends into ring[(s+1)%3] and
@@ -227,6 +232,19 @@ __device__ void tally_flush(const Tally& t, Ctl* c, int kernel) {
     if (a) atomicAdd(&c->kst[kernel][0], a);
     if (b) atomicAdd(&c->kst[kernel][1], b);
     if (d) atomicAdd(&c->kst[kernel][2], d);
+  }
+}
+// One trace record (block 0, thread 0).
+__device__ __forceinline__ void trace_rec(Ctl* c, int32_t count, int32_t mode) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    auto& e = c->trace[c->ntrace % kTrace];
+    e.t = gtimer();
+    e.t_mid = 0;
+    e.count = count;
+    e.mode = mode;
+    e.nwarp = 0;
+    e.nblock = 0;
+    c->ntrace++;
   }
 }
 __device__ __forceinline__ void stat_inc(Ctl* c, int slot) {
@@ -457,14 +475,23 @@ __device__ __forceinline__ Sink sink_make(int32_t* arr, long long base, long lon
   return k;
 }
 
-// Appends the far end of an edge when the visitor accepts it.
+// Visits kEU edges per lane at once: the visitor issues the loads of all of
+// them, then their atomics, so the memory latencies overlap; the far ends it
+// accepts are appended.
+constexpr int kEU = 4;
 template <class V>
-__device__ __forceinline__ void visit_edge(const V& vis, int32_t sv, int32_t w, int k, bool act,
-                                           Stage& st, const Sink& sk, Ctl* c) {
-  const bool app = vis.edge(sv, w, k, act);
-  unsigned long long wt = 0ull;
-  if (V::kWeighted && app && sk.out.edges != nullptr) wt = vis.weight(w);
-  stage_push(st, app, w, wt, sk.out, c);
+__device__ __forceinline__ void visit_edges(const V& vis, const int32_t (&sv)[kEU],
+                                            const int32_t (&w)[kEU], const int (&k)[kEU],
+                                            const bool (&act)[kEU], Stage& st, const Sink& sk,
+                                            Ctl* c) {
+  bool app[kEU];
+  vis.edges(sv, w, k, act, app);
+  unsigned long long wt[kEU];
+#pragma unroll
+  for (int q = 0; q < kEU; ++q)
+    wt[q] = (V::kWeighted && app[q] && sk.out.edges != nullptr) ? vis.weight(w[q]) : 0ull;
+#pragma unroll
+  for (int q = 0; q < kEU; ++q) stage_push(st, app[q], w[q], wt[q], sk.out, c);
 }
 
 constexpr int kSmallFront = 8;
@@ -488,27 +515,59 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
   const int warp = t >> 5, lane = t & 31;
   Stage st = stage_make(sm.stage(warp, 0));
   const bool small = nfront <= kSmallFront;
-  // (1) heavy vertices deferred by the previous step, and a small frontier:
-  // block b takes slice b of each vertex's edges
+  // (1) heavy vertices deferred by the previous step, and a small frontier.
+  // Their records are loaded in parallel, 32 at a time, into shared memory;
+  // a vertex of degree >= t_block is cut into one slice per block, a lighter
+  // one is walked by the single block (index mod grid size) that owns it.
   const int nsl = nheavy + (small ? nfront : 0);
-  for (int j = 0; j < nsl; ++j) {
-    const int32_t v = j < nheavy ? __ldcg(heavy + j) : __ldcg(front + (j - nheavy));
-    long long s0, d0, s1, d1;
-    rec_load<NC>(a, v, s0, d0, s1, d1);
-    const long long d = d0 + d1;
-    const long long lo = d * b / G, hi = d * (b + 1) / G;
-    const int32_t sv = vis.source(v);
-    if (t == 0) ty.vtx += NC;
-    for (long long e0 = lo; e0 < hi; e0 += T) {
-      const long long e = e0 + t;
-      const bool act = e < hi;
-      int32_t w = 0;
-      int k = 0;
-      if (act) {
-        w = adj_at<NC>(a, s0, d0, s1, e, k);
-        ty.edges++;
+  for (int j0 = 0; j0 < nsl; j0 += 32) {
+    __syncthreads();
+    if (warp == 0) {
+      const int j = j0 + lane;
+      if (j < nsl) {
+        const int32_t v = j < nheavy ? __ldcg(heavy + j) : __ldcg(front + (j - nheavy));
+        long long s0, d0, s1, d1;
+        rec_load<NC>(a, v, s0, d0, s1, d1);
+        sm.bl.v[lane] = v;
+        sm.bl.sval[lane] = vis.source(v);
+        sm.bl.s0[lane] = s0;
+        sm.bl.d0[lane] = d0;
+        sm.bl.s1[lane] = s1;
+        sm.bl.d1[lane] = d1;
       }
-      visit_edge(vis, sv, w, k, act, st, sk, c);
+    }
+    __syncthreads();
+    const int cnt = nsl - j0 < 32 ? nsl - j0 : 32;
+    for (int jj = 0; jj < cnt; ++jj) {
+      const long long s0 = sm.bl.s0[jj], d0 = sm.bl.d0[jj], s1 = sm.bl.s1[jj];
+      const long long d = d0 + sm.bl.d1[jj];
+      const int32_t sv = sm.bl.sval[jj];
+      long long lo = 0, hi = d;
+      if (d >= tn.t_block) {
+        lo = d * b / G;
+        hi = d * (b + 1) / G;
+      } else if ((j0 + jj) % G != b) {
+        continue;
+      }
+      if (t == 0 && (b == 0 || d < tn.t_block)) ty.vtx += NC;
+      for (long long e0 = lo; e0 < hi; e0 += (long long)T * kEU) {
+        int32_t svq[kEU], w[kEU];
+        int k[kEU];
+        bool act[kEU];
+#pragma unroll
+        for (int q = 0; q < kEU; ++q) {
+          const long long e = e0 + (long long)q * T + t;
+          act[q] = e < hi;
+          svq[q] = sv;
+          w[q] = 0;
+          k[q] = 0;
+          if (act[q]) {
+            w[q] = adj_at<NC>(a, s0, d0, s1, e, k[q]);
+            ty.edges++;
+          }
+        }
+        visit_edges(vis, svq, w, k, act, st, sk, c);
+      }
     }
   }
   if (small) {
@@ -549,26 +608,33 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
     const int32_t sv = mine ? vis.source(v) : 0;
     long long tot;
     const long long ex = warp_excl64(mine, tot);
-    for (long long eb = 0; eb < tot; eb += 32) {
-      const long long e = eb + lane;
-      const bool act = e < tot;
-      int j = 0;
+    for (long long eb = 0; eb < tot; eb += 32 * kEU) {
+      int32_t svq[kEU], w[kEU];
+      int k[kEU];
+      bool act[kEU];
 #pragma unroll
-      for (int stp = 16; stp; stp >>= 1) {
-        const int cnd = j + stp;
-        const long long exc = shfl64(ex, cnd);
-        if (exc <= e) j = cnd;
+      for (int q = 0; q < kEU; ++q) {
+        const long long e = eb + q * 32 + lane;
+        act[q] = e < tot;
+        // the owner of edge e: the last lane whose exclusive prefix is <= e
+        int j = 0;
+#pragma unroll
+        for (int stp = 16; stp; stp >>= 1) {
+          const int cnd = j + stp;
+          const long long exc = shfl64(ex, cnd);
+          if (exc <= e) j = cnd;
+        }
+        const long long ej = shfl64(ex, j);
+        svq[q] = __shfl_sync(kFull, sv, j);
+        const long long s0j = shfl64(s0, j), d0j = shfl64(d0, j), s1j = shfl64(s1, j);
+        w[q] = 0;
+        k[q] = 0;
+        if (act[q]) {
+          w[q] = adj_at<NC>(a, s0j, d0j, s1j, e - ej, k[q]);
+          ty.edges++;
+        }
       }
-      const long long ej = shfl64(ex, j);
-      const int32_t svj = __shfl_sync(kFull, sv, j);
-      const long long s0j = shfl64(s0, j), d0j = shfl64(d0, j), s1j = shfl64(s1, j);
-      int32_t w = 0;
-      int k = 0;
-      if (act) {
-        w = adj_at<NC>(a, s0j, d0j, s1j, e - ej, k);
-        ty.edges++;
-      }
-      visit_edge(vis, svj, w, k, act, st, sk, c);
+      visit_edges(vis, svq, w, k, act, st, sk, c);
     }
   }
   __syncthreads();
@@ -578,16 +644,23 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
     const int32_t sv = sm.bl.sval[j];
     const long long s0 = sm.bl.s0[j], d0 = sm.bl.d0[j], s1 = sm.bl.s1[j];
     const long long d = d0 + sm.bl.d1[j];
-    for (long long e0 = 0; e0 < d; e0 += T) {
-      const long long e = e0 + t;
-      const bool act = e < d;
-      int32_t w = 0;
-      int k = 0;
-      if (act) {
-        w = adj_at<NC>(a, s0, d0, s1, e, k);
-        ty.edges++;
+    for (long long e0 = 0; e0 < d; e0 += (long long)T * kEU) {
+      int32_t svq[kEU], w[kEU];
+      int k[kEU];
+      bool act[kEU];
+#pragma unroll
+      for (int q = 0; q < kEU; ++q) {
+        const long long e = e0 + (long long)q * T + t;
+        act[q] = e < d;
+        svq[q] = sv;
+        w[q] = 0;
+        k[q] = 0;
+        if (act[q]) {
+          w[q] = adj_at<NC>(a, s0, d0, s1, e, k[q]);
+          ty.edges++;
+        }
       }
-      visit_edge(vis, sv, w, k, act, st, sk, c);
+      visit_edges(vis, svq, w, k, act, st, sk, c);
     }
   }
   stage_flush(st, sk.out, c);
@@ -605,11 +678,18 @@ struct ReachVisit {
   uint32_t* vis;
   Adj push;
   __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
-  __device__ __forceinline__ bool edge(int32_t, int32_t w, int, bool act) const {
-    if (!act) return false;
-    if (bit_get_l1(vis, w)) return false;
-    if (!bit_get_l1(allow, w)) return false;
-    return bit_claim(vis, w);
+  __device__ __forceinline__ void edges(const int32_t (&)[kEU], const int32_t (&w)[kEU],
+                                        const int (&)[kEU], const bool (&act)[kEU],
+                                        bool (&out)[kEU]) const {
+    bool p[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) {
+      const bool seen = bit_get_l1(vis, w[q]);
+      const bool ok = bit_get_l1(allow, w[q]);
+      p[q] = act[q] && !seen && ok;
+    }
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && bit_claim(vis, w[q]);
   }
   __device__ __forceinline__ unsigned long long weight(int32_t w) const {
     return adj_degree<NC>(push, w);
@@ -628,12 +708,26 @@ struct ColourVisit {
   int32_t* stamp;
   int32_t iter;
   __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
-  __device__ __forceinline__ bool edge(int32_t cv, int32_t w, int, bool act) const {
-    if (!act) return false;
-    if (!bit_get(valid, w)) return false;
-    if (__ldcg(colour + w) <= cv) return false;
-    if (atomicMin(colour + w, cv) <= cv) return false;
-    return atomicExch(stamp + w, iter) != iter;
+  __device__ __forceinline__ void edges(const int32_t (&cv)[kEU], const int32_t (&w)[kEU],
+                                        const int (&)[kEU], const bool (&act)[kEU],
+                                        bool (&out)[kEU]) const {
+    bool p[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) {
+      const bool ok = bit_get(valid, w[q]);
+      const int32_t cw = __ldcg(colour + w[q]);
+      p[q] = act[q] && ok && cw > cv[q];
+    }
+    int32_t m[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) m[q] = p[q] ? atomicMin(colour + w[q], cv[q]) : cv[q];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) p[q] = p[q] && m[q] > cv[q];
+    int32_t x[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) x[q] = p[q] ? atomicExch(stamp + w[q], iter) : iter;
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && x[q] != iter;
   }
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
 };
@@ -648,14 +742,22 @@ struct MarkVisit {
   const int32_t* colour;
   int32_t* label;
   __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
-  __device__ __forceinline__ bool edge(int32_t cv, int32_t u, int, bool act) const {
-    if (!act) return false;
-    if (!bit_get(valid, u)) return false;
-    if (__ldcg(colour + u) != cv) return false;
-    if (bit_get(done, u)) return false;
-    if (!bit_claim(done, u)) return false;
-    label[u] = cv;
-    return true;
+  __device__ __forceinline__ void edges(const int32_t (&cv)[kEU], const int32_t (&u)[kEU],
+                                        const int (&)[kEU], const bool (&act)[kEU],
+                                        bool (&out)[kEU]) const {
+    bool p[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) {
+      const bool ok = bit_get(valid, u[q]);
+      const int32_t cu = __ldcg(colour + u[q]);
+      const bool dn = bit_get(done, u[q]);
+      p[q] = act[q] && ok && cu == cv[q] && !dn;
+    }
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && bit_claim(done, u[q]);
+#pragma unroll
+    for (int q = 0; q < kEU; ++q)
+      if (out[q]) label[u[q]] = cv[q];
   }
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
 };
@@ -671,14 +773,20 @@ struct TrimVisit {
   int32_t* live_out;
   int32_t* label;
   __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
-  __device__ __forceinline__ bool edge(int32_t, int32_t w, int k, bool act) const {
-    if (!act) return false;
-    if (!bit_get(valid, w)) return false;
-    int32_t* ctr = k == 0 ? live_in : live_out;
-    if (atomicSub(ctr + w, 1) != 1) return false;
-    if (!bit_release(valid, w)) return false;
-    label[w] = w;
-    return true;
+  __device__ __forceinline__ void edges(const int32_t (&)[kEU], const int32_t (&w)[kEU],
+                                        const int (&k)[kEU], const bool (&act)[kEU],
+                                        bool (&out)[kEU]) const {
+    bool p[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) p[q] = act[q] && bit_get(valid, w[q]);
+    int32_t r[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) r[q] = p[q] ? atomicSub((k[q] == 0 ? live_in : live_out) + w[q], 1) : 0;
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && r[q] == 1 && bit_release(valid, w[q]);
+#pragma unroll
+    for (int q = 0; q < kEU; ++q)
+      if (out[q]) label[w[q]] = w[q];
   }
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
 };
@@ -930,8 +1038,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
           bv = sm.red_i[i];
         }
       }
+      // the second half of blk_i: the first half may already be taking the
+      // valid-list counts of blocks that passed the next barrier
       w.blk_l[b] = (long long)bk;
-      w.blk_i[b] = bv;
+      w.blk_i[G + b] = bv;
     }
   }
   if (!step_sync(c, st, 1)) return;
@@ -940,7 +1050,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
     int32_t bv = -1;
     for (int i = 0; i < G; ++i) {
       const unsigned long long k2 = (unsigned long long)__ldcg(w.blk_l + i);
-      const int32_t v2 = __ldcg(w.blk_i + i);
+      const int32_t v2 = __ldcg(w.blk_i + G + i);
       if (better(k2, v2, bk, bv)) { bk = k2; bv = v2; }
     }
     c->pivot = bk > 0ull ? bv : -1;
@@ -1149,9 +1259,11 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
   int32_t* lc = c->lcount[pp & 1];
+  long long* pnext = &c->pnext[pp & 1];
   if (b == 0 && t == 0) {
     c->lcount[(pp + 1) & 1][0] = 0;
     c->lcount[(pp + 1) & 1][1] = 0;
+    c->pnext[(pp + 1) & 1] = 0;
   }
   const int kt = A.p.tune.k_pull < kPullThread ? (A.p.tune.k_pull > 0 ? A.p.tune.k_pull : 1)
                                                 : kPullThread;
@@ -1179,58 +1291,67 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   int32_t* bl = w.h1;  // block-tier list
   const long long nw = (long long)G * (T >> 5);
   const bool hints = R.pull.c[0].hint != nullptr;
-  // block b streams through its own contiguous share of the candidates
+  // warps claim runs of candidates from a shared counter, so a warp whose
+  // candidates settle quickly takes more of them; a run is about a quarter
+  // of a warp's even share (between 32 and 2 * kGroup)
   constexpr long long kGroup = 32 * kPullA;
   constexpr int kEdgeBatch = 32 * kPullU;
-  const long long chunk = ((ncur + G - 1) / G + kGroup - 1) / kGroup * kGroup;
-  const long long clo = chunk * b < ncur ? chunk * b : ncur;
-  const long long chi = clo + chunk < ncur ? clo + chunk : ncur;
-  for (long long base = clo + warp * kGroup; base < chi; base += (T >> 5) * kGroup) {
-    int32_t v[kPullA], h0[kPullA], h1[kPullA];
+  long long grab = (long long)ncur / (nw * 4) / 32 * 32;
+  grab = grab < 32 ? 32 : (grab > 2 * kGroup ? 2 * kGroup : grab);
+  for (;;) {
+    long long clo = 0;
+    if (lane == 0)
+      clo = (long long)atomicAdd((unsigned long long*)pnext, (unsigned long long)grab);
+    clo = shfl64(clo, 0);
+    if (clo >= ncur) break;
+    const long long chi = clo + grab < ncur ? clo + grab : ncur;
+    for (long long base = clo; base < chi; base += kGroup) {
+      int32_t v[kPullA], h0[kPullA], h1[kPullA];
 #pragma unroll
-    for (int j = 0; j < kPullA; ++j) {
-      const long long i = base + j * 32 + lane;
-      v[j] = i < chi ? __ldcg(cand_cur + i) : -1;
-    }
-    // the hint (the neighbour of largest degree) settles most candidates
-    // without touching the CSR; it is read before the candidate's own bit
-    // is known so that the two loads overlap
-#pragma unroll
-    for (int j = 0; j < kPullA; ++j) {
-      h0[j] = (v[j] >= 0 && hints) ? __ldg(R.pull.c[0].hint + v[j]) : -1;
-      h1[j] = -1;
-      if constexpr (NC > 1) {
-        if (v[j] >= 0 && R.pull.c[1].hint != nullptr) h1[j] = __ldg(R.pull.c[1].hint + v[j]);
+      for (int j = 0; j < kPullA; ++j) {
+        const long long i = base + j * 32 + lane;
+        v[j] = i < chi ? __ldcg(cand_cur + i) : -1;
       }
-    }
-    bool unv[kPullA];
+      // the hint (the neighbour of largest degree) settles most candidates
+      // without touching the CSR; it is read before the candidate's own bit
+      // is known so that the two loads overlap
 #pragma unroll
-    for (int j = 0; j < kPullA; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
-#pragma unroll
-    for (int j = 0; j < kPullA; ++j) {
-      const bool hinted = unv[j] && ((h0[j] >= 0 && bit_get_l1(R.vis, h0[j])) ||
-                                     (h1[j] >= 0 && bit_get_l1(R.vis, h1[j])));
-      if (v[j] >= 0) ty.list++;
-      if (hinted) bit_set_red(R.vis, v[j]);
-      stage_push(sf, hinted, v[j], 0ull, of, c);
-      // the rest go to the warp's backlog
-      const bool open = unv[j] && !hinted;
-      const unsigned mask = __ballot_sync(kFull, open);
-      if (open) todo[ntodo + __popc(mask & lanemask_lt())] = v[j];
-      ntodo += __popc(mask);
-    }
-    __syncwarp();
-    if (ntodo >= kEdgeBatch) {
-      int done = 0;
-      while (ntodo - done >= kEdgeBatch) {
-        pull_edges<NC>(R, todo + done, kEdgeBatch, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
-        done += kEdgeBatch;
+      for (int j = 0; j < kPullA; ++j) {
+        h0[j] = (v[j] >= 0 && hints) ? __ldg(R.pull.c[0].hint + v[j]) : -1;
+        h1[j] = -1;
+        if constexpr (NC > 1) {
+          if (v[j] >= 0 && R.pull.c[1].hint != nullptr) h1[j] = __ldg(R.pull.c[1].hint + v[j]);
+        }
       }
-      // move the remainder (< kEdgeBatch, from at or above kEdgeBatch) to the front
+      bool unv[kPullA];
+#pragma unroll
+      for (int j = 0; j < kPullA; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
+#pragma unroll
+      for (int j = 0; j < kPullA; ++j) {
+        const bool hinted = unv[j] && ((h0[j] >= 0 && bit_get_l1(R.vis, h0[j])) ||
+                                       (h1[j] >= 0 && bit_get_l1(R.vis, h1[j])));
+        if (v[j] >= 0) ty.list++;
+        if (hinted) bit_set_red(R.vis, v[j]);
+        stage_push(sf, hinted, v[j], 0ull, of, c);
+        // the rest go to the warp's backlog
+        const bool open = unv[j] && !hinted;
+        const unsigned mask = __ballot_sync(kFull, open);
+        if (open) todo[ntodo + __popc(mask & lanemask_lt())] = v[j];
+        ntodo += __popc(mask);
+      }
       __syncwarp();
-      for (int i = lane; i < ntodo - done; i += 32) todo[i] = todo[done + i];
-      __syncwarp();
-      ntodo -= done;
+      if (ntodo >= kEdgeBatch) {
+        int done = 0;
+        while (ntodo - done >= kEdgeBatch) {
+          pull_edges<NC>(R, todo + done, kEdgeBatch, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
+          done += kEdgeBatch;
+        }
+        // move the remainder (< kEdgeBatch, from at or above kEdgeBatch) to the front
+        __syncwarp();
+        for (int i = lane; i < ntodo - done; i += 32) todo[i] = todo[done + i];
+        __syncwarp();
+        ntodo -= done;
+      }
     }
   }
   if (ntodo > 0) pull_edges<NC>(R, todo, ntodo, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
@@ -1342,7 +1463,9 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
   if (!step_sync(c, st, 20)) return -1;
   long long qlo = 0, qhi = 0;
   bool pull = false, prev_pull = false;
-  unsigned long long edges_seen = 0ull;
+  // unreached candidates: exact after a pull step (the kept list), counted
+  // down by the frontier after a push step
+  long long remaining = R.ncand;
   const double avg = R.ncand > 0 ? (double)R.m_cand / (double)R.ncand : 0.0;
   const int32_t* cand_cur = R.cand;
   int32_t ncur = R.ncand;
@@ -1359,15 +1482,20 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
     // frontier edge count is estimated from the average degree
     const unsigned long long medges =
         prev_pull ? (unsigned long long)((double)in.count * avg) : in.edges;
-    edges_seen += medges;
     if (prev_pull) {
       cand_cur = cand_next;
       ncur = in.cand;
       cand_next = (cand_next == w.candA) ? w.candB : w.candA;
+      remaining = in.cand;
+    } else {
+      remaining = remaining > in.count ? remaining - in.count : 0;
     }
+    // push -> pull when the frontier's edges outweigh the unexplored edges
+    // (estimated from the unreached candidates); pull -> push when the
+    // frontier is small against the candidates
     if (!pull) {
-      const unsigned long long mu = R.m_cand > edges_seen ? R.m_cand - edges_seen : 0ull;
-      if ((double)medges * (double)tn.alpha > (double)mu) pull = true;
+      const double mu = (double)remaining * avg;
+      if ((double)medges * (double)tn.alpha > mu) pull = true;
     } else if ((double)in.count * (double)tn.beta < (double)R.ncand) {
       pull = false;
     }
@@ -1498,10 +1626,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   auto put = [&](int32_t v) {
     w.label[v] = batch ? (canon ? __ldcg(g.batch.gmin + __ldg(g.batch.gid + v)) : v) : lab;
   };
+  trace_rec(c, nvalid, 12);
   if (!compact_ordered(w.listA, nvalid, w.listB, hit, w, sm, st, 26, &c->nvalid, ty, put)) return;
   if (!step_sync(c, st, 27)) return;
   const int32_t nv = __ldcg(&c->nvalid);
   for (long long i = (long long)b * T + t; i < nv; i += (long long)G * T) w.listA[i] = __ldcg(w.listB + i);
+  trace_rec(c, nv, 15);
   tally_flush(ty, c, kKReach);
   steps_close(c, st);
 }
@@ -1544,6 +1674,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   const Tune& tn = A.p.tune;
   while (nl > 0) {
     if (rounds > g.n || st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 30); return; }
+    trace_rec(c, nl, 8);
     for (long long i = gt; i < nl; i += gstride) {
       const int32_t v = __ldcg(L + i);
       w.colour[v] = v;
@@ -1557,6 +1688,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
       int cur = 0, hs = 0;
       for (;;) {
         if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 32); return; }
+        trace_rec(c, nfront, 9);
         const ColourVisit cv{w.vbits, w.colour, w.stamp, iter++};
         const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, nullptr,
                                   hl[hs ^ 1], w.n, 301);
@@ -1584,6 +1716,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
     }
     // roots: colour == own id (scc_color_get_roots, scc_color.cpp:179-201)
     const MarkVisit mv{w.vbits, w.done, w.colour, w.label};
+    trace_rec(c, nl, 10);
     {
       Out ro;
       ro.arr = bufs[0];
@@ -1617,6 +1750,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
         if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 35); return; }
         const StepIn in = step_read(c, st.s);
         if (in.count == 0 && in.huge == 0) break;
+        trace_rec(c, in.count, 11);
         const Sink sk = sink_make(bufs[cur ^ 1], 0, w.n, step_out(c, st.s), false, nullptr,
                                   hl[hs ^ 1], w.n, 303);
         expand<1>(bufs[cur], in.count, hl[hs], in.huge, back, mv, sk, tn, sm, c, ty);
@@ -1627,6 +1761,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
       }
     }
     // the labelled vertices leave the valid set; L is compacted into L2
+    trace_rec(c, nl, 12);
     auto release = [&](int32_t v) { bit_release(w.vbits, v); };
     if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 37, &c->nvalid, ty, release)) return;
     if (!step_sync(c, st, 38)) return;
@@ -1643,6 +1778,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
     c->ncolour_rounds = rounds;
     c->ncolour = (int32_t)labelled;
   }
+  trace_rec(c, 0, 15);
   tally_flush(ty, c, kKColour);
   steps_close(c, st);
 }

@@ -41,7 +41,7 @@ constexpr size_t kWords = (size_t)(kNoAllocMaxVertices + 32) / 32 + 2;
 constexpr size_t kBm = al256(kWords * 4);
 constexpr size_t kCtl = al256(sizeof(gb::Ctl));
 constexpr size_t kScratchBytes =
-    kCtl + 14 * kArr + 4 * kBm + al256(kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8);
+    kCtl + 14 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8);
 
 // The scratch.  Host code must not pass this name to a kernel: on the host
 // it is a stand-in symbol, not a device address; its device address comes
@@ -133,7 +133,7 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.fvis = (uint32_t*)take(kBm);
   w.bvis = (uint32_t*)take(kBm);
   w.done = (uint32_t*)take(kBm);
-  w.blk_i = (int32_t*)take(al256(kNoAllocMaxGrid * 4));
+  w.blk_i = (int32_t*)take(al256(2 * kNoAllocMaxGrid * 4));
   w.blk_l = (long long*)take(al256(kNoAllocMaxGrid * 8));
   w.ctl = ctl;
   w.n = n;
