@@ -85,6 +85,8 @@ struct Ctl {
   // pull, bit 1 = heavy vertices pending, bit 2 = backward search.  Colour
   // steps: mode 8 = colours reset, 9 = propagation, 10 = roots,
   // 11 = same-colour marking, 12 = compaction; 15 = end of a kernel.
+  // Trim: 16 = start, 17 = degree pass done, 18 = list counted, 19 = list
+  // written.
   struct Trace {
     unsigned long long t;
     unsigned long long t_mid;   // pull steps: end of the thread tier

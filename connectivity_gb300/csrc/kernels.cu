@@ -75,6 +75,11 @@ __device__ __forceinline__ bool bit_release(uint32_t* bm, int32_t v) {
   return (atomicAnd(bm + (v >> 5), ~b) & b) != 0u;
 }
 
+// Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a
+// multiple of 16, the range inside one allocation).
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ long long shfl64(long long x, int src) {
   int lo = __shfl_sync(kFull, (int)(x & 0xffffffffll), src);
   int hi = __shfl_sync(kFull, (int)(x >> 32), src);
@@ -342,6 +347,8 @@ constexpr int kTodo = 384;
 // Dynamic shared memory of the cooperative kernels: two staging buffers and
 // one pull backlog per warp.
 constexpr int kDynSmem = kWarps * (2 * kWB + kTodo) * 4;
+// a warp's two staging buffers also hold the ids of 32 bitmap words
+static_assert(2 * kWB >= 32 * 32, "staging buffers too small for 32 words");
 
 // A global output list.
 struct Out {
@@ -910,6 +917,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   Tally ty;
   if (ld_vol(&c->err)) return;
   Steps st = steps_open(c);
+  trace_rec(c, g.n, 16);
   // the FW-BW minima are folded with atomicMin later (read after this
   // kernel ends)
   if (b == 0 && t == 0) {
@@ -932,21 +940,40 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
   ro.edges = nullptr;
   ro.minv = nullptr;
   ro.where = 103;
-  // Each warp takes kTrimU consecutive words per iteration and issues all
-  // their offset loads before using any.
+  // Block b owns the contiguous word range [wlo, whi) (ranges in block
+  // order, so the ordered valid list can be written per block); inside it
+  // the warps take kTrimU consecutive words at a time, interleaved, and
+  // issue all their offset loads before using any.  Each warp counts the
+  // valid vertices it saw.
   constexpr int kTrimU = 4;
-  const long long nwarps = (long long)G * (T >> 5);
-  for (long long wd0 = ((long long)b * (T >> 5) + warp) * kTrimU; wd0 < w.nwords;
-       wd0 += nwarps * kTrimU) {
+  const long long bchunk = ((long long)w.nwords + G - 1) / G;
+  const long long wlo = bchunk * b < w.nwords ? bchunk * b : w.nwords;
+  const long long whi = wlo + bchunk < w.nwords ? wlo + bchunk : w.nwords;
+  int wvalid = 0;  // warp-uniform
+  // The L2 is asked ahead (a bulk prefetch of the warp's next words of both
+  // offset arrays) while this iteration's loads are outstanding.
+  const bool has_in = g.in.off != nullptr;
+  constexpr long long kTrimAhead = 2;  // iterations ahead
+  // (caller-supplied CSRs need not be 16-byte aligned: no prefetch then)
+  const bool pf_ok = ((reinterpret_cast<uintptr_t>(g.out.off) |
+                       (has_in ? reinterpret_cast<uintptr_t>(g.in.off) : 0u)) & 15u) == 0u;
+  for (long long wd0 = wlo + warp * kTrimU; wd0 < whi; wd0 += (T >> 5) * kTrimU) {
+    {
+      const long long pw = wd0 + kTrimAhead * (T >> 5) * kTrimU;
+      if (pf_ok && lane == 0 && pw + kTrimU <= whi && (pw + kTrimU) * 32 <= (long long)g.n + 1) {
+        prefetch_l2(g.out.off + pw * 32, kTrimU * 32 * 8);
+        if (has_in) prefetch_l2(g.in.off + pw * 32, kTrimU * 32 * 8);
+      }
+    }
     long long o0[kTrimU], o1[kTrimU], i0[kTrimU], i1[kTrimU];
 #pragma unroll
     for (int j = 0; j < kTrimU; ++j) {
       const long long vv = (wd0 + j) * 32 + lane;
       o0[j] = o1[j] = i0[j] = i1[j] = 0;
-      if (vv < g.n) {
+      if (wd0 + j < whi && vv < g.n) {
         o0[j] = __ldg(g.out.off + vv);
         o1[j] = __ldg(g.out.off + vv + 1);
-        if (g.in.off != nullptr) {
+        if (has_in) {
           i0[j] = __ldg(g.in.off + vv);
           i1[j] = __ldg(g.in.off + vv + 1);
         }
@@ -958,7 +985,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
       const long long vv = wd * 32 + lane;
       bool keep = false, gone = false;
       unsigned long long score = 0ull;
-      if (vv < g.n) {
+      if (wd < whi && vv < g.n) {
         const int32_t v = (int32_t)vv;
         const long long dout = o1[j] - o0[j];
         const long long din = i1[j] - i0[j];
@@ -989,14 +1016,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
         if (gone) ++removed;
       }
       const unsigned bits = __ballot_sync(kFull, keep);
-      if (wd < w.nwords && lane == 0) w.vbits[wd] = bits;
+      if (wd < whi && lane == 0) w.vbits[wd] = bits;
+      wvalid += __popc(bits);
       if (level2) stage_push(rs, gone, (int32_t)vv, 0ull, ro, c);
       // batch: per-graph pivot, the packed key (score, lowest id) is maxed
       if (g.batch.gid != nullptr) {
         const unsigned long long mask = (1ull << g.batch.id_bits) - 1ull;
         const unsigned long long key =
             score ? ((score << g.batch.id_bits) | (mask - (unsigned long long)vv)) : 0ull;
-        const int32_t gg = vv < g.n ? __ldg(g.batch.gid + vv) : -1;
+        const int32_t gg = (wd < whi && vv < g.n) ? __ldg(g.batch.gid + vv) : -1;
         const int32_t g0 = __shfl_sync(kFull, gg, 0);
         if (__all_sync(kFull, gg == g0)) {
           unsigned long long kmax = key;
@@ -1012,6 +1040,24 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
     }
   }
   if (level2) stage_flush(rs, ro, c);
+  // Valid-list layout: block b writes the valid vertices of its word range
+  // after those of the earlier blocks (blk_i[0, b)).
+  int btot = 0;
+  auto block_total = [&]() {
+    __syncthreads();
+    if (lane == 0) sm.warp_tmp[warp] = wvalid;
+    __syncthreads();
+    if (t == 0) {
+      int s2 = 0;
+      for (int i = 0; i < (T >> 5); ++i) s2 += sm.warp_tmp[i];
+      sm.warp_tmp[kWarps] = s2;
+      w.blk_i[b] = s2;
+    }
+    __syncthreads();
+    btot = sm.warp_tmp[kWarps];
+  };
+  if (!level2) block_total();
+  // block reduction of the pivot candidates
   {
     unsigned long long k = best_key;
     int32_t v = best_v;
@@ -1038,25 +1084,31 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
           bv = sm.red_i[i];
         }
       }
-      // the second half of blk_i: the first half may already be taking the
-      // valid-list counts of blocks that passed the next barrier
+      // the second half of blk_i: the first half holds the list counts
       w.blk_l[b] = (long long)bk;
       w.blk_i[G + b] = bv;
     }
   }
   if (!step_sync(c, st, 1)) return;
-  if (b == 0 && t == 0) {
+  trace_rec(c, 0, 17);
+  if (b == 0 && warp == 0) {
     unsigned long long bk = 0ull;
     int32_t bv = -1;
-    for (int i = 0; i < G; ++i) {
+    for (int i = lane; i < G; i += 32) {
       const unsigned long long k2 = (unsigned long long)__ldcg(w.blk_l + i);
       const int32_t v2 = __ldcg(w.blk_i + G + i);
       if (better(k2, v2, bk, bv)) { bk = k2; bv = v2; }
     }
-    c->pivot = bk > 0ull ? bv : -1;
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long k2 = __shfl_xor_sync(kFull, bk, o);
+      const int32_t v2 = __shfl_xor_sync(kFull, bv, o);
+      if (better(k2, v2, bk, bv)) { bk = k2; bv = v2; }
+    }
+    if (lane == 0) c->pivot = bk > 0ull ? bv : -1;
   }
 
-  // Level 2: propagate removals to the fixed point.
+  // Level 2: propagate removals to the fixed point, then count the warp's
+  // share of the block's range again.
   if (level2) {
     const Adj both = adj2(g.out, g.in);
     int32_t* bufs[2] = {w.x0, w.x1};
@@ -1072,45 +1124,72 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
       if (!step_sync(c, st, 3)) return;
       cur ^= 1;
     }
-  }
-
-  // Ordered valid list from the bitmap: block b owns a contiguous word range.
-  {
-    const long long chunk = ((long long)w.nwords + G - 1) / G;
-    const long long lo = chunk * b < w.nwords ? chunk * b : w.nwords;
-    const long long hi = lo + chunk < w.nwords ? lo + chunk : w.nwords;
-    int cnt = 0;
-    for (long long wd = lo + t; wd < hi; wd += T) cnt += __popc(__ldcg(w.vbits + wd));
-    int tot;
-    block_excl(cnt, tot, sm.warp_tmp);
-    if (t == 0) w.blk_i[b] = tot;
+    wvalid = 0;
+    for (long long wd0 = wlo + warp * 32; wd0 < whi; wd0 += (long long)T) {
+      const long long wd = wd0 + lane;
+      int x = wd < whi ? __popc(__ldcg(w.vbits + wd)) : 0;
+      for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+      wvalid += x;
+    }
+    block_total();
     if (!step_sync(c, st, 4)) return;
+  }
+  trace_rec(c, 0, 18);
+
+  // Ordered valid list: per iteration warp k of the block takes the k-th
+  // group of 32 words; the warps' counts are scanned in shared memory and
+  // each warp writes the ids of its words with coalesced stores.
+  {
     int pre = 0;
     for (int j = t; j < b; j += T) pre += __ldcg(w.blk_i + j);
     int boff;
     block_excl(pre, boff, sm.warp_tmp);
     if (b == G - 1 && t == 0) {
-      c->nvalid = boff + tot;
-      if (level2) c->ntrim = g.n - (boff + tot);
+      c->nvalid = boff + btot;
+      if (level2) c->ntrim = g.n - (boff + btot);
     }
-    int run = boff;
-    for (long long wd0 = lo; wd0 < hi; wd0 += T) {
-      const long long wd = wd0 + t;
-      const unsigned bits = wd < hi ? __ldcg(w.vbits + wd) : 0u;
-      int bt;
-      const int pos = block_excl(__popc(bits), bt, sm.warp_tmp);
-      unsigned x = bits;
-      int o = run + pos;
-      while (x) {
-        const int bit = __ffs(x) - 1;
-        x &= x - 1;
-        w.listA[o++] = (int32_t)(wd * 32 + bit);
+    long long run = boff;
+    for (long long base = wlo; base < whi; base += (long long)T) {
+      const long long wd0 = base + warp * 32;
+      const long long wd = wd0 + lane;
+      const unsigned x = wd < whi ? __ldcg(w.vbits + wd) : 0u;
+      int tot;
+      const int ex = warp_excl(__popc(x), tot);
+      if (lane == 0) sm.warp_tmp[warp] = tot;
+      __syncthreads();
+      if (warp == 0) {
+        const int y = lane < (T >> 5) ? sm.warp_tmp[lane] : 0;
+        int incl = y;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int z = __shfl_up_sync(kFull, incl, d);
+          if (lane >= d) incl += z;
+        }
+        if (lane < (T >> 5)) sm.warp_tmp[lane] = incl - y;
+        if (lane == 31) sm.warp_tmp[kWarps] = incl;
       }
-      ty.list += __popc(bits);
-      run += bt;
+      __syncthreads();
+      const long long o = run + sm.warp_tmp[warp];
+      run += sm.warp_tmp[kWarps];
+      // each lane puts its word's ids at their ranks in the warp's staging
+      // buffer (visiting its bits from bit `lane` on, so that the lanes of
+      // dense words hit different banks), then the warp copies the buffer out
+      int32_t* buf = sm.stage(warp, 0);  // 2 * kWB >= 1024 entries
+      unsigned y = (x >> lane) | (lane ? x << (32 - lane) : 0u);
+      while (y) {
+        const int p = __ffs(y) - 1;
+        y &= y - 1;
+        const int bit = (p + lane) & 31;
+        buf[ex + __popc(x & ((1u << bit) - 1u))] = (int32_t)(wd * 32 + bit);
+      }
+      __syncwarp();
+      for (int k = lane; k < tot; k += 32) w.listA[o + k] = buf[k];
+      ty.list += __popc(x);
+      __syncthreads();
     }
   }
   if (!step_sync(c, st, 5)) return;
+  trace_rec(c, 0, 19);
   // A hint replaces the pivot; level 2 may have trimmed the pivot, in which
   // case FW-BW is skipped and the colour rounds label what is left.
   if (b == 0 && t == 0) {
