@@ -84,13 +84,13 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the reach kernel from the committed ncu
-    summary (profiles/traffic.json), or None."""
+def profile_traffic(kernel="k_reach"):
+    """DRAM bytes per launch of a kernel from the committed ncu summary
+    (profiles/traffic.json, R-MAT scale 24), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             d = json.load(f)
-        return d.get("k_reach_bytes_per_launch")
+        return d.get(f"{kernel}_bytes_per_launch")
     except Exception:
         return None
 
@@ -446,12 +446,25 @@ def run_gbconn(args):
 
     peak, peak_kind = peaks()
 
-    def roof(kernel, nbytes, ms):
+    # algorithmic bytes per launch, from the per-unit figures (O = 8 B per
+    # int64 offset, I = 4 B per id or label):
+    #   trim pass: 2*O*(n+1) + I*n + n/8
+    #   traversal, per direction: O*(n+1) + I*m_visited + 2*n/8, plus per pull
+    #   step O*(n+1), plus I per adjacency entry the pull steps scanned
+    O, I = 8, 4
+    trim8d = 2 * O * (n + 1) + I * n + n // 8
+    dirs = (1 if st.fw_steps else 0) + (1 if st.bw_steps else 0)
+    reach8d = (dirs * (O * (n + 1) + 2 * n // 8) + I * (st.m_visit_fw + st.m_visit_bw)
+               + st.pull_steps * O * (n + 1) + I * st.pull_edges)
+
+    def roof(kernel, nbytes, ms, touched):
         a = nbytes / (ms / 1e3) / 1e9
         return {"kernel": kernel, "achieved": round(a, 1), "frac": round(a / peak, 4),
-                "algorithmic_bytes_per_launch": int(nbytes), "launch_ms": round(ms, 4)}
+                "algorithmic_bytes_per_launch": int(nbytes), "launch_ms": round(ms, 4),
+                "touched_bytes_per_launch": int(touched),
+                "touched_gbs": round(touched / (ms / 1e3) / 1e9, 1)}
 
-    reach = roof("k_reach", st.bytes_reach, float(pm[1]))
+    reach = roof("k_reach", reach8d, float(pm[1]), st.bytes_reach)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": round(step_ms, 4), "higher_is_better": True,
@@ -468,11 +481,20 @@ def run_gbconn(args):
         "roofline": {"bound": "hbm", "kernel": "k_reach (FW-BW reachability + commit)",
                      "achieved": reach["achieved"], "peak": peak, "unit": "GB/s",
                      "frac": reach["frac"], "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "traffic": profile_traffic(),
+                     "traffic": profile_traffic() if args.scale == SCALE else None,
+                     "traffic_source": "profiles/traffic.json (ncu, one capture at scale 24)",
+                     "dram_gbs_at_traffic": (round(profile_traffic() / (float(pm[1]) / 1e3) / 1e9, 1)
+                                             if profile_traffic() and args.scale == SCALE
+                                             else None),
                      "algorithmic_bytes_per_launch": reach["algorithmic_bytes_per_launch"],
                      "launch_ms": reach["launch_ms"],
-                     "kernels": [roof("k_trim", st.bytes_trim, float(pm[0])), reach,
-                                 roof("k_colour", st.bytes_colour, float(pm[2]))]},
+                     "touched_bytes_per_launch": reach["touched_bytes_per_launch"],
+                     "units": {"n": n, "m": m, "m_visit_fw": st.m_visit_fw,
+                               "m_visit_bw": st.m_visit_bw, "pull_steps": st.pull_steps,
+                               "pull_edges_scanned": st.pull_edges},
+                     "kernels": [roof("k_trim", trim8d, float(pm[0]), st.bytes_trim), reach,
+                                 roof("k_colour", st.bytes_colour, float(pm[2]),
+                                      st.bytes_colour)]},
         "phases_ms": {k: round(float(v), 4) for k, v in
                       zip(("trim", "reach", "colour", "tail", "total"), pm)},
         "gpu_launches": 4 * K,

@@ -70,6 +70,7 @@ class Stats(C.Structure):
         ("bytes_colour", C.c_int64), ("bytes_canon", C.c_int64), ("trim_steps", C.c_int64), ("fw_steps", C.c_int64),
         ("bw_steps", C.c_int64), ("pull_steps", C.c_int64), ("colour_steps", C.c_int64),
         ("mark_steps", C.c_int64), ("grid_blocks", C.c_int32), ("err_where", C.c_int32),
+        ("m_visit_fw", C.c_int64), ("m_visit_bw", C.c_int64), ("pull_edges", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

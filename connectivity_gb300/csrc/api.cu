@@ -212,6 +212,9 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
     st->bytes_colour = kb(gb::kKColour) + 4 * (int64_t)h.kst[gb::kKColour][2];
     // final pass: one label read per vertex
     st->bytes_canon = 4 * n;
+    st->m_visit_fw = (int64_t)h.mvis[0];
+    st->m_visit_bw = (int64_t)h.mvis[1];
+    st->pull_edges = (int64_t)h.pull_edges;
     st->trim_steps = (int64_t)h.stat[gb::kStTrimSteps];
     st->fw_steps = (int64_t)h.stat[gb::kStFwSteps];
     st->bw_steps = (int64_t)h.stat[gb::kStBwSteps];

@@ -97,6 +97,10 @@ struct Ctl {
   } trace[128];
   int32_t ntrace;
   int32_t pad2;
+  // statistics runs: push-direction edges of the forward / backward reached
+  // vertices, and adjacency entries scanned by pull steps
+  unsigned long long mvis[2];
+  unsigned long long pull_edges;
   // Diagnostic: device time at which each block finished the thread tier of
   // the first pull step of the run.
   unsigned long long blk_t[256];

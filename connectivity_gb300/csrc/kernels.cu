@@ -230,8 +230,11 @@ __device__ __forceinline__ void steps_close(Ctl* c, const Steps& st) {
 // Per-thread counters of algorithmic traffic, flushed once per kernel.
 struct Tally {
   unsigned long long vtx = 0, edges = 0, list = 0;
+  unsigned long long pull_edges = 0;  // the part of `edges` scanned by pull steps
 };
 __device__ void tally_flush(const Tally& t, Ctl* c, int kernel) {
+  const unsigned long long pe = warp_sum64(t.pull_edges);
+  if (lane_id() == 0 && pe) atomicAdd(&c->pull_edges, pe);
   const unsigned long long a = warp_sum64(t.vtx), b = warp_sum64(t.edges), d = warp_sum64(t.list);
   if (lane_id() == 0) {
     if (a) atomicAdd(&c->kst[kernel][0], a);
@@ -1362,6 +1365,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   ok.edges = nullptr;
   ok.minv = nullptr;
   ok.where = 203;
+  const unsigned long long edges0 = ty.edges;
   Stage sf = stage_make(sm.stage(warp, 0));
   Stage sk = stage_make(sm.stage(warp, 1));
   int32_t* todo = sm.todo(warp);
@@ -1504,6 +1508,7 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   }
   stage_flush(sf, of, c);
   stage_flush(sk, ok, c);
+  ty.pull_edges += ty.edges - edges0;
   return true;
 }
 
@@ -1874,14 +1879,29 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_colour(Args A) {
 __global__ void k_count_unassigned(Args A) {
   Work& w = A.w;
   const int32_t n = A.g.n;
+  const GraphView& g = A.g;
+  const bool scc = A.kind == kSCC;
   int un = 0;
+  // push-direction degrees of the reached vertices: SCC forward = out,
+  // backward = in; WCC forward = out + in
+  unsigned long long mf = 0ull, mb = 0ull;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (long long)gridDim.x * blockDim.x) {
     const int32_t l = w.label[v];
     if (l < 0 || l >= n) ++un;
+    const long long dout = g.out.off[v + 1] - g.out.off[v];
+    const long long din = g.in.off != nullptr ? g.in.off[v + 1] - g.in.off[v] : 0;
+    if ((w.fvis[v >> 5] >> (v & 31)) & 1u) mf += (unsigned long long)(scc ? dout : dout + din);
+    if (scc && ((w.bvis[v >> 5] >> (v & 31)) & 1u)) mb += (unsigned long long)din;
   }
   for (int o = 16; o; o >>= 1) un += __shfl_xor_sync(kFull, un, o);
-  if (lane_id() == 0 && un) atomicAdd(&w.ctl->unassigned, un);
+  mf = warp_sum64(mf);
+  mb = warp_sum64(mb);
+  if (lane_id() == 0) {
+    if (un) atomicAdd(&w.ctl->unassigned, un);
+    if (mf) atomicAdd(&w.ctl->mvis[0], mf);
+    if (mb) atomicAdd(&w.ctl->mvis[1], mb);
+  }
 }
 
 __global__ void k_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase) {

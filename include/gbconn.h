@@ -105,6 +105,9 @@ typedef struct gb_stats {
   int64_t trim_steps, fw_steps, bw_steps, pull_steps, colour_steps, mark_steps;
   int32_t grid_blocks;
   int32_t err_where;      /* device location code of a failure, 0 if none */
+  /* push-direction edges of the vertices reached forward / backward (the
+   * m_visited of a traversal) and adjacency entries scanned by pull steps */
+  int64_t m_visit_fw, m_visit_bw, pull_edges;
 } gb_stats;
 
 /* ---- contexts --------------------------------------------------------- */
