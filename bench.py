@@ -158,6 +158,32 @@ def dist():
     return ws, rank, local
 
 
+def dist_barrier():
+    """Barrier over the ranks of an initialised process group (no-op alone)."""
+    import torch.distributed as tdist
+    if tdist.is_available() and tdist.is_initialized() and tdist.get_world_size() > 1:
+        tdist.barrier()
+
+
+def dist_max(x: float) -> float:
+    """Maximum of x over the ranks (the slowest rank's time); x alone."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return x
+    dev = (torch.device("cuda", torch.cuda.current_device()) if tdist.get_backend() == "nccl"
+           else torch.device("cpu"))
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gteps(edges_per_rank: int, ranks: int, seconds_max: float, steps: int) -> float:
+    """Whole-job GTEPS: every rank runs its own replica, so the job
+    processes ranks x edges per step in the slowest rank's time."""
+    return ranks * edges_per_rank / (seconds_max / steps) / 1e9
+
+
 def cpu_baseline_run(n, m, oo, oa, io, ia, reps):
     import oracle
     cg = oracle.CpuGraph.from_csr(n, oo, oa, io, ia)
@@ -362,18 +388,8 @@ def run_gbconn(args):
         import torch.distributed as tdist
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if ws > 1:
-            import torch.distributed as tdist
-            tdist.barrier()
-
-    def allmax(x):
-        if ws == 1:
-            return x
-        import torch.distributed as tdist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        return float(t.item())
+    barrier = dist_barrier
+    allmax = dist_max
 
     ctx = gb.Context(local)
     # a stream of our own: the library runs on it and the CUDA events are
@@ -420,7 +436,7 @@ def run_gbconn(args):
     phases = ctx.phase_times(min(K, 64))
     pm = phases.mean(axis=0)
     step_ms = T / K * 1e3
-    value = ws * m / (T / K) / 1e9
+    value = job_gteps(m, ws, T, K)
 
     # one more run with statistics (algorithmic bytes of each kernel)
     lab_dev, st = ctx.scc(g, labels=labels.data_ptr(), stats=True)
@@ -473,7 +489,7 @@ def run_gbconn(args):
                    "l2": "inputs larger than L2 (2.1 GB CSR, 129 MB L2); no flush",
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
                    "trim_level": 1, "labels": "canonical minimum member id, device memory"},
-        "e2e": {"value": round(ws * m / (TE / KE) / 1e9, 3), "unit": "GTEPS",
+        "e2e": {"value": round(job_gteps(m, ws, TE, KE), 3), "unit": "GTEPS",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(TE / KE * 1e3, 3), "steps": KE,
                 "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers)",
