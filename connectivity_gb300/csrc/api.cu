@@ -59,7 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 14 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8);
+  const size_t total = 14 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8) + 256;
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -89,7 +89,11 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.done = (uint32_t*)take(bm);
   w.blk_i = (int32_t*)take(align256(2 * G * 4));
   w.blk_l = (long long*)take(align256(G * 8));
+  w.iter_next = (int32_t*)take(256);
   w.ctl = c->d_ctl;
+  // stamps start below every step number; numbering starts at 0
+  CK(cudaMemsetAsync(w.stamp, 0xff, arr, c->stream), "workspace init");
+  CK(cudaMemsetAsync(w.iter_next, 0, sizeof(int32_t), c->stream), "workspace init");
   c->cap_n = n;
   return GB_OK;
 }
@@ -166,21 +170,46 @@ using gb::graph_alloc;
 using gb::graph_free;
 using gb::graph_hints;
 
+// Phase times (ms) of the run in ring slot i: trim, reachability and colour
+// from the device times the run kernel wrote at its phase boundaries, the
+// tail (statistics pass) and the total from the run's events.  The ring copy
+// must be current (the caller synchronised the stream).
+gb_status run_phase_ms(gb_ctx* c, int i, double* ms) {
+  const unsigned long long* t = c->h_tphase + 4 * i;
+  for (int j = 0; j < 3; ++j) ms[j] = t[j + 1] > t[j] ? (double)(t[j + 1] - t[j]) / 1e6 : 0.0;
+  cudaEvent_t* ev = c->ev[i];
+  float tail = 0.f, tot = 0.f;
+  CK(cudaEventElapsedTime(&tail, ev[1], ev[4]), "phase times");
+  CK(cudaEventElapsedTime(&tot, ev[0], ev[4]), "phase times");
+  ms[3] = tail;
+  ms[4] = tot;
+  return GB_OK;
+}
+
+gb_status copy_phase_ring(gb_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_tphase, c->d_tphase, sizeof(unsigned long long) * 4 * gb_ctx::kRing,
+                     cudaMemcpyDeviceToHost, c->stream),
+     "phase times");
+  CK(cudaStreamSynchronize(c->stream), "phase times");
+  return GB_OK;
+}
+
 gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
   CK(cudaStreamSynchronize(c->stream), "run");
   (void)g;
   const gb::Ctl& h = *c->h_ctl;
   if (st) {
+    gb_status ps = copy_phase_ring(c);
+    if (ps != GB_OK) return ps;
     std::memset(st, 0, sizeof(*st));
-    float ms[4] = {0, 0, 0, 0}, tot = 0;
-    cudaEvent_t* ev = c->ev[(c->runs - 1) % gb_ctx::kRing];
-    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
-    cudaEventElapsedTime(&tot, ev[0], ev[4]);
-    st->ms_trim = ms[0];
-    st->ms_reach = ms[1];
-    st->ms_colour = ms[2];
-    st->ms_canon = ms[3];
-    st->ms_total = tot;
+    double ms[5];
+    if (run_phase_ms(c, (c->runs - 1) % gb_ctx::kRing, ms) == GB_OK) {
+      st->ms_trim = ms[0];
+      st->ms_reach = ms[1];
+      st->ms_colour = ms[2];
+      st->ms_canon = ms[3];
+      st->ms_total = ms[4];
+    }
     st->pivot = h.pivot;
     st->colour_rounds = h.ncolour_rounds;
     st->n_trim = h.ntrim;
@@ -286,12 +315,12 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
     CK(cudaMemsetAsync(bv->pkey, 0, (size_t)bv->count * 8, sm), "memset");
     CK(cudaMemsetAsync(bv->gmin, 0x7f, (size_t)bv->count * 4, sm), "memset");
   }
+  // (the trim phase clears the reached / done bitmaps; the stamps need no
+  // clearing, see the colour phase)
   CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
-  CK(cudaMemsetAsync(w.fvis, 0, (size_t)w.nwords * 4, sm), "memset");
-  CK(cudaMemsetAsync(w.bvis, 0, (size_t)w.nwords * 4, sm), "memset");
-  CK(cudaMemsetAsync(w.done, 0, (size_t)w.nwords * 4, sm), "memset");
-  CK(cudaMemsetAsync(w.stamp, 0xff, (size_t)g->n * 4, sm), "memset");
   cudaEvent_t* ev = c->ev[c->runs % gb_ctx::kRing];
+  w.tphase = c->d_tphase + 4 * (c->runs % gb_ctx::kRing);
+  CK(cudaMemsetAsync(w.tphase, 0, 4 * sizeof(unsigned long long), sm), "memset");
   c->runs++;
   CK(gb::launch_run(gv, kind, p, w, grid, sm, ev), "kernel launch");
   CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
@@ -370,6 +399,11 @@ gb_status gb_ctx_create(int device, gb_ctx** out) {
     if ((r = cudaMalloc(&c->d_ctl, sizeof(gb::Ctl))) != cudaSuccess) { s = cuda_fail(r, "ctl"); break; }
     if ((r = cudaMallocHost(&c->h_ctl, sizeof(gb::Ctl))) != cudaSuccess) { s = cuda_fail(r, "ctl"); break; }
     if ((r = cudaMalloc(&c->d_sticky, 2 * sizeof(int))) != cudaSuccess) { s = cuda_fail(r, "sticky"); break; }
+    const size_t pr = sizeof(unsigned long long) * 4 * gb_ctx::kRing;
+    if ((r = cudaMalloc(&c->d_tphase, pr)) != cudaSuccess) { s = cuda_fail(r, "phase ring"); break; }
+    if ((r = cudaMallocHost(&c->h_tphase, pr)) != cudaSuccess) { s = cuda_fail(r, "phase ring"); break; }
+    cudaMemset(c->d_tphase, 0, pr);
+    std::memset(c->h_tphase, 0, pr);
     if ((r = cudaMallocHost(&c->h_sticky, 2 * sizeof(int))) != cudaSuccess) { s = cuda_fail(r, "sticky"); break; }
     cudaMemset(c->d_sticky, 0, 2 * sizeof(int));
     std::memset(c->h_ctl, 0, sizeof(gb::Ctl));
@@ -396,6 +430,8 @@ gb_status gb_ctx_destroy(gb_ctx* c) {
   cudaFree(c->ws);
   cudaFree(c->d_ctl);
   cudaFree(c->d_sticky);
+  cudaFree(c->d_tphase);
+  if (c->h_tphase) cudaFreeHost(c->h_tphase);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
   if (c->h_sticky) cudaFreeHost(c->h_sticky);
   for (auto& set : c->ev)
@@ -433,16 +469,11 @@ gb_status gb_ctx_sync(gb_ctx* c) {
 gb_status gb_ctx_phase_times(gb_ctx* c, int32_t count, double* ms) {
   if (!c || !ms || count < 0 || count > gb_ctx::kRing || count > c->runs) return GB_ERR_INVALID;
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  CK(cudaStreamSynchronize(c->stream), "phase times");
+  gb_status s = copy_phase_ring(c);
+  if (s != GB_OK) return s;
   for (int32_t i = 0; i < count; ++i) {
-    cudaEvent_t* ev = c->ev[(c->runs - count + i) % gb_ctx::kRing];
-    float x = 0;
-    for (int j = 0; j < 4; ++j) {
-      CK(cudaEventElapsedTime(&x, ev[j], ev[j + 1]), "phase times");
-      ms[i * 5 + j] = x;
-    }
-    CK(cudaEventElapsedTime(&x, ev[0], ev[4]), "phase times");
-    ms[i * 5 + 4] = x;
+    s = run_phase_ms(c, (int)((c->runs - count + i) % gb_ctx::kRing), ms + 5 * i);
+    if (s != GB_OK) return s;
   }
   return GB_OK;
 }

@@ -19,7 +19,10 @@ struct gb_ctx {
   int* d_sticky = nullptr;      // first error of any run since the last sync
   int* h_sticky = nullptr;      // pinned
   static constexpr int kRing = 64;
-  cudaEvent_t ev[kRing][5] = {};  // phase events of the last kRing runs
+  cudaEvent_t ev[kRing][5] = {};  // events of the last kRing runs: [0] start, [1] after the
+                                  // run kernel, [4] end (after the statistics pass)
+  unsigned long long* d_tphase = nullptr;  // kRing x 4 device phase-boundary times
+  unsigned long long* h_tphase = nullptr;  // pinned copy
   long long runs = 0;             // runs issued on this context
 };
 

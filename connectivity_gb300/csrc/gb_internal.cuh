@@ -144,6 +144,9 @@ struct Work {
   int32_t* h0;            // heavy-vertex lists
   int32_t* h1;
   int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
+  unsigned long long* tphase;  // this run's 4 phase-boundary device times, or null
+  int32_t* iter_next;     // next colour-step number (persists across runs; the
+                          // stamps hold only smaller numbers)
   long long* blk_l;
   Ctl* ctl;
 };

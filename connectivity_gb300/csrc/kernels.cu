@@ -232,15 +232,25 @@ struct Tally {
   unsigned long long vtx = 0, edges = 0, list = 0;
   unsigned long long pull_edges = 0;  // the part of `edges` scanned by pull steps
 };
-__device__ void tally_flush(const Tally& t, Ctl* c, int kernel) {
-  const unsigned long long pe = warp_sum64(t.pull_edges);
-  if (lane_id() == 0 && pe) atomicAdd(&c->pull_edges, pe);
-  const unsigned long long a = warp_sum64(t.vtx), b = warp_sum64(t.edges), d = warp_sum64(t.list);
-  if (lane_id() == 0) {
-    if (a) atomicAdd(&c->kst[kernel][0], a);
-    if (b) atomicAdd(&c->kst[kernel][1], b);
-    if (d) atomicAdd(&c->kst[kernel][2], d);
+// Only statistics runs flush (the counters are summed per block first: one
+// atomic per block and counter, not per warp, which would queue thousands of
+// atomics on four words).  All threads of the block call it.
+__device__ void tally_flush(const Tally& t, Ctl* c, int kernel, bool stats,
+                            unsigned long long* red /* 4 x kWarps shared */) {
+  if (!stats) return;
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned long long v[4] = {warp_sum64(t.vtx), warp_sum64(t.edges), warp_sum64(t.list),
+                                   warp_sum64(t.pull_edges)};
+  __syncthreads();
+  if (lane_id() == 0)
+    for (int k = 0; k < 4; ++k) red[k * kWarps + warp] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    unsigned long long x = 0ull;
+    for (int i = 0; i < nw; ++i) x += red[threadIdx.x * kWarps + i];
+    if (x) atomicAdd(threadIdx.x < 3 ? &c->kst[kernel][threadIdx.x] : &c->pull_edges, x);
   }
+  __syncthreads();
 }
 // One trace record (block 0, thread 0).
 __device__ __forceinline__ void trace_rec(Ctl* c, int32_t count, int32_t mode) {
@@ -450,6 +460,7 @@ struct Smem {
   BlockList bl;
   int warp_tmp[kWarps + 1];
   long long red_l[kWarps];
+  unsigned long long red_u[4 * kWarps];  // statistics tallies, per warp
   int red_i[kWarps];
   int32_t* stage_base;  // dynamic shared memory: kWarps x 2 x kWB, then kWarps x kTodo
   __device__ __forceinline__ int32_t* stage(int warp, int k) {
@@ -907,9 +918,7 @@ __device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsign
   return k2 > k || (k2 == k && v2 >= 0 && (v < 0 || v2 < v));
 }
 
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
-  __shared__ Smem sm;
-  sm.stage_base = g_dyn_smem;
+__device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   Work& w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -1019,7 +1028,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
         if (gone) ++removed;
       }
       const unsigned bits = __ballot_sync(kFull, keep);
-      if (wd < whi && lane == 0) w.vbits[wd] = bits;
+      if (wd < whi && lane < 4) {
+        // the run's reached / done bitmaps start empty
+        uint32_t* dst = lane == 0 ? w.vbits : lane == 1 ? w.fvis : lane == 2 ? w.bvis : w.done;
+        dst[wd] = lane == 0 ? bits : 0u;
+      }
       wvalid += __popc(bits);
       if (level2) stage_push(rs, gone, (int32_t)vv, 0ull, ro, c);
       // batch: per-graph pivot, the packed key (score, lowest id) is maxed
@@ -1217,7 +1230,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_trim(Args A) {
       list_append(v >= 0, v, g.batch.roots, &c->nroots, g.batch.count, c, 6);
     }
   }
-  tally_flush(ty, c, kKTrim);
+  tally_flush(ty, c, kKTrim, A.p.count_unassigned != 0, sm.red_u);
   steps_close(c, st);
 }
 
@@ -1620,9 +1633,7 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
 // adjacency (cc_bfs, cc_bfs.cpp:217-291).
 // ------------------------------------------------------------------------
 template <int NC>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
-  __shared__ Smem sm;
-  sm.stage_base = g_dyn_smem;
+__device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   Work& w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -1716,7 +1727,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_reach(Args A) {
   const int32_t nv = __ldcg(&c->nvalid);
   for (long long i = (long long)b * T + t; i < nv; i += (long long)G * T) w.listA[i] = __ldcg(w.listB + i);
   trace_rec(c, nv, 15);
-  tally_flush(ty, c, kKReach);
+  tally_flush(ty, c, kKReach, A.p.count_unassigned != 0, sm.red_u);
   steps_close(c, st);
 }
 
@@ -1750,7 +1761,15 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   const Adj back = adj1(g.in);
   int32_t* L = w.listA;
   int32_t* L2 = w.listB;
-  int32_t iter = 0;
+  // Propagation steps are numbered on from the previous run's last number
+  // (stamp values only ever hold numbers already used), so the stamps need
+  // no clearing per run; when the numbers run high the stamps are renewed.
+  int32_t iter = __ldcg(w.iter_next);
+  if (iter > (1 << 30)) {
+    for (long long v = gt; v < w.n; v += gstride) w.stamp[v] = -1;
+    if (!step_sync(c, st, 39)) return;
+    iter = 0;
+  }
   int rounds = 0;
   long long labelled = 0;
   int32_t* bufs[2] = {w.x0, w.x1};
@@ -1861,17 +1880,41 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   if (b == 0 && t == 0) {
     c->ncolour_rounds = rounds;
     c->ncolour = (int32_t)labelled;
+    *w.iter_next = iter;
   }
   trace_rec(c, 0, 15);
-  tally_flush(ty, c, kKColour);
+  tally_flush(ty, c, kKColour, A.p.count_unassigned != 0, sm.red_u);
   steps_close(c, st);
 }
 
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_colour(Args A) {
+// Device time at a phase boundary (block 0, thread 0), into the run's slot
+// of the context's phase-time ring.
+__device__ __forceinline__ void phase_mark(const Args& A, int i) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && A.w.tphase != nullptr) A.w.tphase[i] = gtimer();
+}
+
+// ------------------------------------------------------------------------
+// k_run: one run (trim, reachability, colour rounds) in one cooperative
+// launch; a grid barrier separates the phases, so each phase sees the
+// previous one's lists, counters and pivot.  NC: adjacency lists walked by
+// the reachability phase (1, or 2 for WCC of a directed graph).
+// ------------------------------------------------------------------------
+template <int NC>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_run(Args A) {
   __shared__ Smem sm;
   sm.stage_base = g_dyn_smem;
+  Ctl* c = A.w.ctl;
+  phase_mark(A, 0);
+  trim_phase(A, sm);
+  if (!grid_barrier(c, 900)) return;
+  phase_mark(A, 1);
+  reach_phase<NC>(A, sm);
+  if (!grid_barrier(c, 901)) return;
+  phase_mark(A, 2);
   if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
   else colour_rounds<2>(A, sm);
+  if (!grid_barrier(c, 902)) return;
+  phase_mark(A, 3);
 }
 
 // Counts labels outside [0, n) (0 after a complete run); enqueued when the
@@ -1925,8 +1968,7 @@ int max_coop_grid(int device) {
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   int best = 1 << 30;
-  const void* ks[] = {(const void*)k_trim, (const void*)k_reach<1>, (const void*)k_reach<2>,
-                      (const void*)k_colour};
+  const void* ks[] = {(const void*)k_run<1>, (const void*)k_run<2>};
   for (const void* k : ks) {
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynSmem) !=
         cudaSuccess)
@@ -1958,18 +2000,12 @@ cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p, con
   a.kind = kind;
   cudaError_t e;
   if (ev) cudaEventRecord(ev[0], stream);
-  e = coop(k_trim, grid, a, stream);
-  if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[1], stream);
   // SCC and symmetric graphs walk one CSR per direction; WCC of a directed
   // graph walks the union of both
-  e = (kind == kSCC || g.in.off == nullptr) ? coop(k_reach<1>, grid, a, stream)
-                                            : coop(k_reach<2>, grid, a, stream);
+  e = (kind == kSCC || g.in.off == nullptr) ? coop(k_run<1>, grid, a, stream)
+                                            : coop(k_run<2>, grid, a, stream);
   if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[2], stream);
-  e = coop(k_colour, grid, a, stream);
-  if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[3], stream);
+  if (ev) cudaEventRecord(ev[1], stream);
   if (p.count_unassigned) {
     k_count_unassigned<<<grid, kBlock, 0, stream>>>(a);
     e = cudaGetLastError();
