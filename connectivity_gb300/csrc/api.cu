@@ -623,9 +623,53 @@ gb_status gb_graph_from_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* out_
   return GB_OK;
 }
 
+// The device address of pinned host memory (the same address under unified
+// addressing), or null when p is not pinned host memory.
+static const void* pinned_view(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Fills g (whose buffers hold at least n / m) from the reference's CSR layout.
+// Pinned host arrays are read by the ingest kernels directly (one crossing
+// of the host link, checked on the way); other memory is copied, widened
+// and then checked on the device.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
                             const uint32_t* odl, const int32_t* in_array, const uint32_t* idl) {
+  {
+    const void* vo = pinned_view(odl);
+    const void* va = m > 0 ? pinned_view(out_array) : odl;
+    const void* vi = g->symmetric ? odl : pinned_view(idl);
+    const void* vb = g->symmetric || m == 0 ? odl : pinned_view(in_array);
+    if (vo && va && vi && vb) {
+      int* d_bad = nullptr;
+      CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
+      gb_status s = GB_OK;
+      cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+      if (e == cudaSuccess)
+        e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
+                             d_bad, c->stream);
+      if (e == cudaSuccess && !g->symmetric)
+        e = gb::ingest_csr32(n, m, (const uint32_t*)vi, (const int32_t*)vb, g->in_off, g->in_adj,
+                             d_bad, c->stream);
+      int bad = 0;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      cudaFreeAsync(d_bad, c->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "ingest");
+      if (bad) {
+        gb_set_error("CSR check: %s", "offsets not monotone from 0 to m, or an id outside [0, n)");
+        s = GB_ERR_INVALID;
+      }
+      return s;
+    }
+  }
   uint32_t* tmp = nullptr;
   CK(cudaMallocAsync(&tmp, (size_t)(n + 1) * 4, c->stream), "offset staging");
   gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);

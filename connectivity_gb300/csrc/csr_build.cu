@@ -151,6 +151,56 @@ __global__ void k_check_csr(int32_t n, int64_t m, const int64_t* off, const int3
   }
 }
 
+// Ingest of the reference's 32-bit CSR from host memory the device reads
+// directly (pinned): offsets are widened to int64 and checked (off[0] == 0,
+// off[n] == m, non-decreasing), ids are checked against [0, n), in the same
+// pass that moves the bytes, so the host link is crossed once and nothing
+// is read again on the device.
+__global__ void k_ingest_off(const uint32_t* __restrict__ h, int64_t* __restrict__ d, int32_t n,
+                             int64_t m, int* bad) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~(int64_t)31; base <= n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + lane;
+    const uint32_t x = i <= n ? h[i] : 0u;
+    uint32_t nx = __shfl_down_sync(0xffffffffu, x, 1);
+    if (lane == 31 && i + 1 <= n) nx = h[i + 1];
+    if (i <= n) {
+      d[i] = (int64_t)x;
+      if ((i == 0 && x != 0u) || (i == n && (int64_t)x != m) || (i < n && nx < x)) atomicOr(bad, 1);
+    }
+  }
+}
+__global__ void k_ingest_adj(const int32_t* __restrict__ h, int32_t* __restrict__ d, int64_t m,
+                             int32_t n, int* bad) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = true;
+  if (((reinterpret_cast<uintptr_t>(h) | reinterpret_cast<uintptr_t>(d)) & 15u) == 0u) {
+    const int64_t m4 = m / 4;
+    const int4* h4 = reinterpret_cast<const int4*>(h);
+    int4* d4 = reinterpret_cast<int4*>(d);
+    for (int64_t i = t0; i < m4; i += stride) {
+      const int4 v = h4[i];
+      d4[i] = v;
+      ok = ok && (uint32_t)v.x < (uint32_t)n && (uint32_t)v.y < (uint32_t)n &&
+           (uint32_t)v.z < (uint32_t)n && (uint32_t)v.w < (uint32_t)n;
+    }
+    for (int64_t e = m4 * 4 + t0; e < m; e += stride) {
+      const int32_t v = h[e];
+      d[e] = v;
+      ok = ok && (uint32_t)v < (uint32_t)n;
+    }
+  } else {
+    for (int64_t e = t0; e < m; e += stride) {
+      const int32_t v = h[e];
+      d[e] = v;
+      ok = ok && (uint32_t)v < (uint32_t)n;
+    }
+  }
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
 // Pivot keys: out*in (kind 0) or degree (kind 1).
 __device__ __forceinline__ unsigned long long pivot_key(const int64_t* out_off, const int64_t* in_off,
                                                         int kind, int64_t v) {
@@ -296,6 +346,15 @@ cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* a
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
+}
+
+cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
+                         int64_t* off, int32_t* adj, int* d_bad, cudaStream_t s) {
+  k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_off, off, n, m, d_bad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || m == 0) return e;
+  k_ingest_adj<<<grid_for(m / 4 + 1), 256, 0, s>>>(h_adj, adj, m, n, d_bad);
+  return cudaGetLastError();
 }
 
 cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,

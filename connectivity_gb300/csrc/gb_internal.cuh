@@ -209,6 +209,10 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
 // unless an earlier one is already there.
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
+// Reference-layout CSR (32-bit offsets) from device-readable host memory into
+// an int64-offset device CSR, checked on the way (*d_bad |= 1 on a bad CSR).
+cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
+                         int64_t* off, int32_t* adj, int* d_bad, cudaStream_t s);
 // Batch labels: global ids -> ids local to each graph.
 cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
                             cudaStream_t s);

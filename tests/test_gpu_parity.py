@@ -138,6 +138,60 @@ def test_reference_shaped_dropins():
     assert np.array_equal(lab, _wcc_want(n, s, d))
 
 
+def test_reference_shaped_dropins_pinned():
+    """Pinned host buffers take the direct ingest (read over the host link
+    by the device, checked on the way); the labels must not change, and a
+    bad CSR must still be refused."""
+    torch = pytest.importorskip("torch")
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    for n, s, d in (graphs.rmat(14, 16, 21), graphs.erdos(1001, 7003, 5)):
+        cg = oracle.CpuGraph(n, s, d)
+        odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
+        oa, ia = pin(cg.out_adj), pin(cg.in_adj)
+        # odd offsets into the arrays exercise the unaligned copy path too
+        out = pin(np.empty(n, np.int32))
+        piv, avg = cg.pivot_scc()
+        lab = gb.run_scc_ref(n, oa, ia, odl, idl, piv, avg, 10000, out)
+        assert np.array_equal(lab, _scc_want(n, s, d))
+        mg = oracle.CpuGraph(n, s, d, mirror=True)
+        mo, ma = pin(mg.out_off.astype(np.uint32)), pin(mg.out_adj)
+        piv, avg = mg.pivot_cc()
+        lab = gb.run_cc_ref(n, ma, mo, piv, avg, pin(np.empty(n, np.int32)))
+        assert np.array_equal(lab, _wcc_want(n, s, d))
+    # an id out of range, and a non-monotone offset array, in pinned memory
+    n, s, d = graphs.rmat(10, 8, 3)
+    cg = oracle.CpuGraph(n, s, d)
+    odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
+    oa, ia = pin(cg.out_adj), pin(cg.in_adj)
+    oa[len(oa) // 2] = n + 5
+    with pytest.raises(gb.GBError) as e:
+        gb.run_scc_ref(n, oa, ia, odl, idl)
+    assert e.value.status == gb.GB_ERR_INVALID
+    oa[len(oa) // 2] = 0
+    idl[n // 2], idl[n // 2 + 1] = idl[n // 2 + 1] + 1, idl[n // 2]
+    with pytest.raises(gb.GBError) as e:
+        gb.run_scc_ref(n, oa, ia, odl, idl)
+    assert e.value.status == gb.GB_ERR_INVALID
+
+
+def test_pinned_unaligned_adjacency(ctx):
+    """An adjacency array that starts off a 16-byte boundary takes the
+    scalar ingest."""
+    torch = pytest.importorskip("torch")
+    n, s, d = graphs.rmat(12, 16, 4)
+    cg = oracle.CpuGraph(n, s, d)
+    big = torch.empty(len(cg.out_adj) + 1, dtype=torch.int32).pin_memory().numpy()
+    oa = big[1:]
+    oa[:] = cg.out_adj
+    big2 = torch.empty(len(cg.in_adj) + 3, dtype=torch.int32).pin_memory().numpy()
+    ia = big2[3:]
+    ia[:] = cg.in_adj
+    odl = torch.from_numpy(cg.out_off.astype(np.uint32)).pin_memory().numpy()
+    idl = torch.from_numpy(cg.in_off.astype(np.uint32)).pin_memory().numpy()
+    lab = gb.run_scc_ref(n, oa, ia, odl, idl)
+    assert np.array_equal(lab, _scc_want(n, s, d))
+
+
 def test_device_labels_and_async(ctx):
     torch = pytest.importorskip("torch")
     n, s, d = graphs.rmat(14, 16, 11)
