@@ -109,6 +109,9 @@ _sig("gb_graph_rmat", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_doub
 _sig("gb_graph_rmat_n", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
                                     C.c_double, C.POINTER(_P)])
 _sig("gb_graph_info", C.c_int32, [_P, _I32P, _I64P, _I32P])
+_sig("gb_graph_from_file2", C.c_int32, [_P, C.c_char_p, C.c_int32, C.POINTER(_P)])
+_sig("gb_write_binary", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
+_sig("gb_write_text", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
 _sig("gb_batch_from_edges", C.c_int32, [_P, C.c_int32, _P, C.c_int64, _P, _P, C.POINTER(_P)])
 _sig("gb_batch_rmat", C.c_int32, [_P, C.c_int32, _P, _P, _P, C.c_double, C.c_double, C.c_double,
                                   C.POINTER(_P)])
@@ -194,6 +197,22 @@ def opts(**kw) -> Opts:
 # ---------------------------------------------------------------------------
 # host utilities
 # ---------------------------------------------------------------------------
+def write_binary(path: str, n: int, src, dst) -> None:
+    """Edge list in the binary graph-file format (gb_write_binary)."""
+    s = np.ascontiguousarray(src, np.int32)
+    d = np.ascontiguousarray(dst, np.int32)
+    _check(_lib.gb_write_binary(str(path).encode(), int(n), s.size, _ptr(s), _ptr(d)),
+           "gb_write_binary")
+
+
+def write_text(path: str, n: int, src, dst) -> None:
+    """Edge list in the reference's text format (gb_write_text)."""
+    s = np.ascontiguousarray(src, np.int32)
+    d = np.ascontiguousarray(dst, np.int32)
+    _check(_lib.gb_write_text(str(path).encode(), int(n), s.size, _ptr(s), _ptr(d)),
+           "gb_write_text")
+
+
 def read_edge(path: str) -> tuple[int, np.ndarray, np.ndarray]:
     """read_edge (scc_main.cpp:94-125): returns (n, src, dst)."""
     n, m = C.c_int32(), C.c_int64()
@@ -408,6 +427,15 @@ class Graph:
                    "gb_graph_from_edges")
         else:
             raise TypeError("src/dst must be numpy arrays")
+        return cls(h)
+
+    @classmethod
+    def from_file(cls, ctx: Context, path: str, chunk: int = 0) -> "Graph":
+        """A graph file (the reference's text format or the binary format),
+        parsed on the device."""
+        h = C.c_void_p()
+        _check(_lib.gb_graph_from_file2(ctx._h, str(path).encode(), chunk, C.byref(h)),
+               "gb_graph_from_file")
         return cls(h)
 
     @classmethod

@@ -163,6 +163,51 @@ extern "C" gb_status gb_output_labels(const char* path, int32_t n, const int32_t
   return ok ? GB_OK : GB_ERR_IO;
 }
 
+// Edge list in the reference's text format ("n m", then "src dst" lines),
+// the input of read_edge (scc_main.cpp:94-125).
+static char* put_u32(char* p, uint32_t v) {
+  char tmp[12];
+  int k = 0;
+  do {
+    tmp[k++] = (char)('0' + v % 10);
+    v /= 10;
+  } while (v);
+  while (k) *p++ = tmp[--k];
+  return p;
+}
+
+extern "C" gb_status gb_write_text(const char* path, int32_t n, int64_t m, const int32_t* src,
+                                   const int32_t* dst) {
+  if (!path || n < 0 || m < 0 || (m > 0 && (!src || !dst))) return GB_ERR_INVALID;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    gb_set_error("gb_write_text: cannot open %s", path);
+    return GB_ERR_IO;
+  }
+  std::vector<char> out(1 << 22);
+  int len = std::snprintf(out.data(), out.size(), "%d %lld\n", n, (long long)m);
+  char* p = out.data() + len;
+  bool ok = true;
+  for (int64_t i = 0; i < m && ok; ++i) {
+    if (src[i] < 0 || dst[i] < 0) {
+      ok = false;
+      break;
+    }
+    p = put_u32(p, (uint32_t)src[i]);
+    *p++ = ' ';
+    p = put_u32(p, (uint32_t)dst[i]);
+    *p++ = '\n';
+    if ((size_t)(p - out.data()) > out.size() - 32) {
+      ok = std::fwrite(out.data(), 1, (size_t)(p - out.data()), f) == (size_t)(p - out.data());
+      p = out.data();
+    }
+  }
+  if (ok) ok = std::fwrite(out.data(), 1, (size_t)(p - out.data()), f) == (size_t)(p - out.data());
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) gb_set_error("gb_write_text: write failed for %s", path);
+  return ok ? GB_OK : GB_ERR_IO;
+}
+
 // ---------------------------------------------------------------------------
 // Verify statistics (scc_verify.cpp:47-77, cc_verify.cpp:47-74): a label
 // histogram; components, components with more than one vertex, the largest,

@@ -5,10 +5,11 @@
 //
 // Same command line, same stdout lines ("Multistep SCC time: %9.6lf" over the
 // run, scc_main.cpp:368-378, then the scc_verify line), same label file (one
-// label per line, output_scc :193-202).  The graph is read on the host, its
-// CSR is built on the GPU (outside the timed region, as create_csr is in the
-// reference), and the timed region is the device run with the labels copied
-// back to host memory.  Labels are the canonical minimum member ids.
+// label per line, output_scc :193-202).  The graph file (the reference's
+// text format, or the binary format of gb_write_binary) is parsed and its
+// CSR built on the GPU, outside the timed region as read_edge and create_csr
+// are in the reference; the timed region is the device run with the labels
+// copied back to host memory.  Labels are the canonical minimum member ids.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -29,17 +30,16 @@ static int fail(const char* what, gb_status s) {
 int main(int argc, char** argv) {
   setbuf(stdout, NULL);
   if (argc < 2) print_usage(argv);
+  gb_ctx* ctx = nullptr;
+  gb_status s = gb_ctx_create(0, &ctx);
+  if (s != GB_OK) return fail("gb_ctx_create", s);
+  // read_edge + create_csr: the file is parsed and the CSR built on the device
+  gb_graph* g = nullptr;
+  if ((s = gb_graph_from_file(ctx, argv[1], &g)) != GB_OK) return fail("read_edge", s);
   int32_t n = 0;
   int64_t m = 0;
-  int32_t *srcs = nullptr, *dsts = nullptr;
-  gb_status s = gb_read_edge(argv[1], &n, &m, &srcs, &dsts);
-  if (s != GB_OK) return fail("read_edge", s);
-  gb_ctx* ctx = nullptr;
-  if ((s = gb_ctx_create(0, &ctx)) != GB_OK) return fail("gb_ctx_create", s);
-  gb_graph* g = nullptr;
-  if ((s = gb_graph_from_edges(ctx, n, m, srcs, dsts, &g)) != GB_OK) return fail("create_csr", s);
-  gb_free_host(srcs);
-  gb_free_host(dsts);
+  int32_t sym = 0;
+  if ((s = gb_graph_info(g, &n, &m, &sym)) != GB_OK) return fail("create_csr", s);
   std::vector<int32_t> maps((size_t)n + 1);
   gb_opts o;
   gb_opts_default(&o);

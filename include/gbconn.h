@@ -159,6 +159,23 @@ gb_status gb_graph_from_csr(gb_ctx* ctx, int32_t n, int64_t m, const int64_t* ou
 gb_status gb_graph_from_csr32(gb_ctx* ctx, int32_t n, uint32_t m, const int32_t* out_array,
                               const uint32_t* out_degree_list, const int32_t* in_array,
                               const uint32_t* in_degree_list, gb_graph** g);
+/* From a graph file, parsed on the device (read_edge, scc_main.cpp:94-125,
+ * replaced).  Text: the reference's format, "n m" then m lines "src dst"
+ * (any blanks between tokens; tokens after the first 2m ignored).  Binary:
+ * "GBEDGES1", int64 n, int64 m, m int32 sources, m int32 targets (little
+ * endian; see gb_write_binary).  GB_ERR_IO: unreadable file, bad header or
+ * too few edges; GB_ERR_INVALID: a token that is not an id in [0, n). */
+gb_status gb_graph_from_file(gb_ctx* ctx, const char* path, gb_graph** g);
+/* As gb_graph_from_file with the text tokenizer's byte chunk per thread
+ * (0: default 256); small chunks exist to test tokens across chunks. */
+gb_status gb_graph_from_file2(gb_ctx* ctx, const char* path, int32_t chunk, gb_graph** g);
+/* Writes an edge list in the reference's text format ("n m" then "src dst"
+ * lines), the input of read_edge. */
+gb_status gb_write_text(const char* path, int32_t n, int64_t m, const int32_t* src,
+                        const int32_t* dst);
+/* Writes an edge list in the binary graph-file format. */
+gb_status gb_write_binary(const char* path, int32_t n, int64_t m, const int32_t* src,
+                          const int32_t* dst);
 /* Seeded directed R-MAT graph built on the device: edge_factor << scale
  * edges drawn with probabilities (a, b, c, 1-a-b-c), self-loops and
  * duplicates removed.  Same edges as gb_rmat_edges_host. */

@@ -136,3 +136,20 @@ def test_cli_usage_without_arguments():
         r = subprocess.run([exe], capture_output=True, text=True)
         assert r.returncode == 0
         assert r.stdout == f"Usage: {exe} [graph] [optional: output file]\n"
+
+
+def test_file_writers_round_trip(tmp_path):
+    """gb_write_text writes what the host reader reads back; gb_write_binary
+    writes the documented layout."""
+    n, s, d = 1000, np.arange(0, 999, dtype=np.int32), np.arange(1, 1000, dtype=np.int32)
+    gb.write_text(tmp_path / "g.txt", n, s, d)
+    hn, hs, hd = gb.read_edge(str(tmp_path / "g.txt"))
+    assert hn == n and np.array_equal(hs, s) and np.array_equal(hd, d)
+    with open(tmp_path / "g.txt") as f:
+        assert f.readline() == "1000 999\n" and f.readline() == "0 1\n"
+    gb.write_binary(tmp_path / "g.bin", n, s, d)
+    raw = open(tmp_path / "g.bin", "rb").read()
+    assert raw[:8] == b"GBEDGES1"
+    assert np.frombuffer(raw[8:24], np.int64).tolist() == [n, 999]
+    assert np.array_equal(np.frombuffer(raw[24:24 + 4 * 999], np.int32), s)
+    assert np.array_equal(np.frombuffer(raw[24 + 4 * 999:], np.int32), d)
