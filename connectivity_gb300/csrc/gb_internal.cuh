@@ -32,12 +32,15 @@ struct Csr {
 // Counters filled during one step and read by every block after the
 // barrier that ends it.  Three slots rotate: step s reads slot s%3, appends
 // into slot (s+1)%3 and clears slot (s+2)%3.
+// The step counters take atomics from every warp of the grid, and the
+// barrier word is polled by every block: each hot word sits in its own
+// 128-byte line, so that no L2 slice serves two of them.
 struct Slot {
-  int32_t count;              // vertices appended to the step's output list
-  int32_t huge;               // heavy vertices deferred to the next step
-  int32_t cand;               // candidates kept by a pull step
+  alignas(128) int32_t count;     // vertices appended to the step's output list
+  alignas(128) int32_t cand;      // candidates kept by a pull step
+  alignas(128) int32_t huge;      // heavy vertices deferred to the next step
   int32_t pad;
-  unsigned long long edges;   // push-degree sum of the appended vertices
+  unsigned long long edges;       // push-degree sum of the appended vertices
 };
 
 // Statistic slots (64-bit counters, summed over the whole run).
@@ -55,8 +58,8 @@ enum Stat : int {
 struct Ctl {
   // grid barrier word: arrivals so far (low 32 bits, never reset within a
   // run), bit 63 = an error was raised
-  unsigned long long bar;
-  int err;
+  alignas(128) unsigned long long bar;
+  alignas(128) int err;
   int err_where;
   int step;               // step counter, continued by each kernel of a run
   int pad0;
@@ -69,12 +72,12 @@ struct Ctl {
   int32_t ncolour_rounds;
   int32_t unassigned;
   int32_t ncolour;        // vertices labelled by the colour rounds
-  int32_t minv[2];        // smallest vertex reached forward / backward
   int32_t nroots;         // batch: pivots in BatchView::roots
-  int32_t lcount[2][2];   // pull steps: warp- and block-tier list lengths
-  long long pnext[2];     // pull steps: next unclaimed candidate of the thread tier
-                          // (two sets, used by alternate pull steps)
-  int32_t pad1;
+  alignas(128) int32_t minv[2];       // smallest vertex reached forward / backward
+  alignas(128) int32_t lcount[2][2];  // pull steps: warp- and block-tier list lengths
+  alignas(128) long long pnext[2];    // pull steps: next unclaimed candidate of the thread
+                                      // tier (two sets, used by alternate pull steps)
+  alignas(128) int32_t pad1;
   unsigned long long m_cand;   // push-degree sum of the valid list after trim
   unsigned long long stat[kStNum];
   // Algorithmic traffic per kernel (trim, reach, colour, canon): vertex
