@@ -315,9 +315,12 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
     CK(cudaMemsetAsync(bv->pkey, 0, (size_t)bv->count * 8, sm), "memset");
     CK(cudaMemsetAsync(bv->gmin, 0x7f, (size_t)bv->count * 4, sm), "memset");
   }
-  // (the trim phase clears the reached / done bitmaps; the stamps need no
-  // clearing, see the colour phase)
+  // the reached and done bitmaps are adjacent in the workspace: one memset
+  // clears all three (the stamps need no clearing, see the colour phase)
   CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
+  CK(cudaMemsetAsync(w.fvis, 0,
+                     (size_t)((char*)(w.done + w.nwords) - (char*)w.fvis), sm),
+     "memset");
   cudaEvent_t* ev = c->ev[c->runs % gb_ctx::kRing];
   w.tphase = c->d_tphase + 4 * (c->runs % gb_ctx::kRing);
   CK(cudaMemsetAsync(w.tphase, 0, 4 * sizeof(unsigned long long), sm), "memset");

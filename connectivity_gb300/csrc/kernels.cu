@@ -1028,11 +1028,7 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
         if (gone) ++removed;
       }
       const unsigned bits = __ballot_sync(kFull, keep);
-      if (wd < whi && lane < 4) {
-        // the run's reached / done bitmaps start empty
-        uint32_t* dst = lane == 0 ? w.vbits : lane == 1 ? w.fvis : lane == 2 ? w.bvis : w.done;
-        dst[wd] = lane == 0 ? bits : 0u;
-      }
+      if (wd < whi && lane == 0) w.vbits[wd] = bits;
       wvalid += __popc(bits);
       if (level2) stage_push(rs, gone, (int32_t)vv, 0ull, ro, c);
       // batch: per-graph pivot, the packed key (score, lowest id) is maxed
