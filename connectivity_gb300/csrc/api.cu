@@ -59,7 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 14 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8) + 256;
+  const size_t total = 16 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8) + 256;
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -83,6 +83,8 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.candB = (int32_t*)take(arr);
   w.h0 = (int32_t*)take(arr);
   w.h1 = (int32_t*)take(arr);
+  w.xa = (int32_t*)take(arr);
+  w.xb = (int32_t*)take(arr);
   w.vbits = (uint32_t*)take(bm);
   w.fvis = (uint32_t*)take(bm);
   w.bvis = (uint32_t*)take(bm);

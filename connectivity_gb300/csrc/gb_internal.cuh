@@ -63,7 +63,8 @@ struct Ctl {
   int err_where;
   int step;               // step counter, continued by each kernel of a run
   int pad0;
-  Slot ring[3];
+  Slot ring[3][2];        // [step % 3][search]: the forward and backward searches of
+                          // one step count separately
   int32_t pivot;          // FW-BW source (-1: none)
   int32_t nvalid;         // length of the current valid list
   int32_t nvisit_fw;      // vertices reached forward
@@ -74,9 +75,9 @@ struct Ctl {
   int32_t ncolour;        // vertices labelled by the colour rounds
   int32_t nroots;         // batch: pivots in BatchView::roots
   alignas(128) int32_t minv[2];       // smallest vertex reached forward / backward
-  alignas(128) int32_t lcount[2][2];  // pull steps: warp- and block-tier list lengths
-  alignas(128) long long pnext[2];    // pull steps: next unclaimed candidate of the thread
-                                      // tier (two sets, used by alternate pull steps)
+  // pull steps, per search and per parity of the search's pull steps:
+  alignas(128) int32_t lcount[2][2][2];  // warp- and block-tier list lengths
+  alignas(128) long long pnext[2][2];    // next unclaimed candidate of the thread tier
   alignas(128) int32_t pad1;
   unsigned long long m_cand;   // push-degree sum of the valid list after trim
   unsigned long long stat[kStNum];
@@ -146,6 +147,8 @@ struct Work {
   int32_t* candB;
   int32_t* h0;            // heavy-vertex lists
   int32_t* h1;
+  int32_t* xa;            // backward search's pull tier lists when both
+  int32_t* xb;            // searches run in the same steps
   int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
   unsigned long long* tphase;  // this run's 4 phase-boundary device times, or null
   int32_t* iter_next;     // next colour-step number (persists across runs; the

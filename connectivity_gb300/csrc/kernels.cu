@@ -178,8 +178,8 @@ struct StepIn {
   int32_t count, huge, cand;
   unsigned long long edges;
 };
-__device__ __forceinline__ StepIn step_read(Ctl* c, int step) {
-  const Slot& s = c->ring[step % 3];
+__device__ __forceinline__ StepIn step_read(Ctl* c, int step, int dir = 0) {
+  const Slot& s = c->ring[step % 3][dir];
   StepIn r;
   r.count = __ldcg(&s.count);
   r.huge = __ldcg(&s.huge);
@@ -188,15 +188,17 @@ __device__ __forceinline__ StepIn step_read(Ctl* c, int step) {
   return r;
 }
 __device__ __forceinline__ void step_begin(Ctl* c, int step) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    Slot& s = c->ring[(step + 2) % 3];
+  if (blockIdx.x == 0 && threadIdx.x < 2) {
+    Slot& s = c->ring[(step + 2) % 3][threadIdx.x];
     s.count = 0;
     s.huge = 0;
     s.cand = 0;
     s.edges = 0ull;
   }
 }
-__device__ __forceinline__ Slot* step_out(Ctl* c, int step) { return &c->ring[(step + 1) % 3]; }
+__device__ __forceinline__ Slot* step_out(Ctl* c, int step, int dir = 0) {
+  return &c->ring[(step + 1) % 3][dir];
+}
 
 constexpr unsigned long long kKernelTimeLimitNs = 120ull * 1000ull * 1000ull * 1000ull;
 
@@ -1342,23 +1344,10 @@ __device__ __forceinline__ void pull_edges(const ReachSpec& R, const int32_t* to
   }
 }
 
-template <int NC>
-__device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
-                          const int32_t* cand_cur, int32_t ncur, int32_t* cand_next, long long qhi,
-                          Slot* o, int pp) {
-  Ctl* c = w.ctl;
-  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
-  const int warp = t >> 5, lane = t & 31;
-  int32_t* lc = c->lcount[pp & 1];
-  long long* pnext = &c->pnext[pp & 1];
-  if (b == 0 && t == 0) {
-    c->lcount[(pp + 1) & 1][0] = 0;
-    c->lcount[(pp + 1) & 1][1] = 0;
-    c->pnext[(pp + 1) & 1] = 0;
-  }
-  const int kt = A.p.tune.k_pull < kPullThread ? (A.p.tune.k_pull > 0 ? A.p.tune.k_pull : 1)
-                                                : kPullThread;
-  Out of;
+// The outputs of a pull step: found vertices to q (from qhi on), kept
+// candidates to cand_next, with the counters of the search's slot.
+__device__ __forceinline__ void pull_outs(const ReachSpec& R, const Work& w, int32_t* cand_next,
+                                          long long qhi, Slot* o, Out& of, Out& ok) {
   of.arr = R.q;
   of.base = qhi;
   of.cap = w.n;
@@ -1366,7 +1355,6 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   of.edges = nullptr;
   of.minv = R.minv;
   of.where = 202;
-  Out ok;
   ok.arr = cand_next;
   ok.base = 0;
   ok.cap = w.n;
@@ -1374,13 +1362,37 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   ok.edges = nullptr;
   ok.minv = nullptr;
   ok.where = 203;
+}
+
+__device__ __forceinline__ int pull_kt(const Args& A) {
+  return A.p.tune.k_pull < kPullThread ? (A.p.tune.k_pull > 0 ? A.p.tune.k_pull : 1) : kPullThread;
+}
+
+// Thread tier of a pull step (search `dir`, its pp-th pull step): fills the
+// warp- and block-tier lists wl / bl; the caller's grid barrier then
+// completes them for pull_tail.
+template <int NC>
+__device__ void pull_thread(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
+                            const int32_t* cand_cur, int32_t ncur, int32_t* cand_next,
+                            long long qhi, Slot* o, int pp, int dir, int32_t* wl, int32_t* bl) {
+  Ctl* c = w.ctl;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  int32_t* lc = c->lcount[dir][pp & 1];
+  long long* pnext = &c->pnext[dir][pp & 1];
+  if (b == 0 && t == 0) {
+    c->lcount[dir][(pp + 1) & 1][0] = 0;
+    c->lcount[dir][(pp + 1) & 1][1] = 0;
+    c->pnext[dir][(pp + 1) & 1] = 0;
+  }
+  const int kt = pull_kt(A);
+  Out of, ok;
+  pull_outs(R, w, cand_next, qhi, o, of, ok);
   const unsigned long long edges0 = ty.edges;
   Stage sf = stage_make(sm.stage(warp, 0));
   Stage sk = stage_make(sm.stage(warp, 1));
   int32_t* todo = sm.todo(warp);
   int ntodo = 0;  // warp-uniform
-  int32_t* wl = w.x1;  // warp-tier list
-  int32_t* bl = w.h1;  // block-tier list
   const long long nw = (long long)G * (T >> 5);
   const bool hints = R.pull.c[0].hint != nullptr;
   // warps claim runs of candidates from a shared counter, so a warp whose
@@ -1447,16 +1459,30 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
     }
   }
   if (ntodo > 0) pull_edges<NC>(R, todo, ntodo, kt, sf, sk, of, ok, wl, bl, lc, w.n, c, ty);
-  if (pp == 0 && t == 0 && b < kBlkTimes) c->blk_t[b] = gtimer();
-  // the warp and block tiers need the complete lists
-  if (!grid_barrier(c, 206)) return false;
+  if (pp == 0 && dir == 0 && t == 0 && b < kBlkTimes) c->blk_t[b] = gtimer();
+  stage_flush(sf, of, c);
+  stage_flush(sk, ok, c);
+  ty.pull_edges += ty.edges - edges0;
+}
+
+// Warp and block tiers of a pull step, after the grid barrier that follows
+// every search's thread tier.
+template <int NC>
+__device__ void pull_tail(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
+                          int32_t* cand_next, long long qhi, Slot* o, int pp, int dir,
+                          const int32_t* wl, const int32_t* bl) {
+  Ctl* c = w.ctl;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31;
+  const int32_t* lc = c->lcount[dir][pp & 1];
+  const int kt = pull_kt(A);
+  Out of, ok;
+  pull_outs(R, w, cand_next, qhi, o, of, ok);
+  const unsigned long long edges0 = ty.edges;
+  Stage sf = stage_make(sm.stage(warp, 0));
+  Stage sk = stage_make(sm.stage(warp, 1));
+  const long long nw = (long long)G * (T >> 5);
   const int32_t nwl = __ldcg(&lc[0]), nbl = __ldcg(&lc[1]);
-  if (b == 0 && t == 0 && c->ntrace > 0) {
-    auto& tr = c->trace[(c->ntrace - 1) % kTrace];
-    tr.t_mid = gtimer();
-    tr.nwarp = nwl;
-    tr.nblock = nbl;
-  }
   for (long long j = (long long)b * (T >> 5) + warp; j < nwl; j += nw) {
     const int32_t v = __ldcg(wl + j);
     long long s0, d0, s1, d1;
@@ -1518,25 +1544,57 @@ __device__ bool pull_step(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
   stage_flush(sf, of, c);
   stage_flush(sk, ok, c);
   ty.pull_edges += ty.edges - edges0;
-  return true;
 }
 
+// Pivot degree (smaller of in and out) from which the two searches of an
+// SCC run in the same steps.
+constexpr long long kTogetherDegree = 64;
+
+// One search (one direction of one traversal): its spec, the lists it owns,
+// and its running state.
+struct Search {
+  ReachSpec R;
+  int dir;                 // its counter set in the step ring and pull claims
+  int32_t* cand[2];        // pull candidate lists (alternating)
+  int32_t* heavy[2];       // push heavy-vertex lists (alternating)
+  int32_t* wl;             // pull warp-tier list
+  int32_t* bl;             // pull block-tier list
+  long long qlo, qhi;      // this step's frontier: q[qlo, qhi)
+  long long remaining;     // unreached candidates (estimate after push steps)
+  double avg;              // average push degree of the candidates
+  const int32_t* cand_cur;
+  int32_t ncur;
+  int32_t huge;            // heavy vertices deferred into this step
+  int cn;                  // cand[cn] receives the next kept list
+  int hsel;
+  int pp;                  // pull steps so far
+  int ti;                  // this step's trace record, or -1
+  bool pull, prev_pull, active;
+};
+
+// Runs the searches S[0, ns) to completion, all advancing in the same steps:
+// in each step every active search pushes its frontier or runs a pull step;
+// the pull steps share one internal grid barrier between their thread tiers
+// and their warp / block tiers.  S and flags are in shared memory: thread 0
+// updates them (every block computes the same state from the same
+// counters) and the block barrier that follows publishes them.  Returns
+// false when the kernel must stop.
 template <int NC>
-__device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps& st, Tally& ty,
-                     int& pp) {
+__device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const Args& A,
+                            Work& w, Smem& sm, Steps& st, Tally& ty) {
   Ctl* c = w.ctl;
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
   const Tune& tn = A.p.tune;
-  const ReachVisit<NC> rv{R.allow, R.vis, R.push};
   // the sources are the first step's frontier
-  {
+  for (int k = 0; k < ns; ++k) {
+    const ReachSpec& R = S[k].R;
     Out ro;
     ro.arr = R.q;
     ro.base = 0;
     ro.cap = w.n;
-    ro.counter = &step_out(c, st.s)->count;
-    ro.edges = &step_out(c, st.s)->edges;
+    ro.counter = &step_out(c, st.s, S[k].dir)->count;
+    ro.edges = &step_out(c, st.s, S[k].dir)->edges;
     ro.minv = R.minv;
     ro.where = 207;
     Stage rs = stage_make(sm.stage(warp, 0));
@@ -1553,72 +1611,127 @@ __device__ int reach(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Steps
     }
     stage_flush(rs, ro, c);
   }
-  if (!step_sync(c, st, 20)) return -1;
-  long long qlo = 0, qhi = 0;
-  bool pull = false, prev_pull = false;
-  // unreached candidates: exact after a pull step (the kept list), counted
-  // down by the frontier after a push step
-  long long remaining = R.ncand;
-  const double avg = R.ncand > 0 ? (double)R.m_cand / (double)R.ncand : 0.0;
-  const int32_t* cand_cur = R.cand;
-  int32_t ncur = R.ncand;
-  int32_t* cand_next = w.candA;
-  int hsel = 0;
-  int32_t* hl[2] = {w.h0, w.h1};
+  if (t == 0) {
+    for (int k = 0; k < ns; ++k) {
+      Search& q = S[k];
+      q.qlo = q.qhi = 0;
+      q.remaining = q.R.ncand;
+      q.avg = q.R.ncand > 0 ? (double)q.R.m_cand / (double)q.R.ncand : 0.0;
+      q.cand_cur = q.R.cand;
+      q.ncur = q.R.ncand;
+      q.cn = 0;
+      q.hsel = 0;
+      q.pp = 0;
+      q.pull = q.prev_pull = false;
+      q.active = true;
+    }
+  }
+  if (!step_sync(c, st, 20)) return false;
   const int s_start = st.s;
   for (;;) {
-    if (st.s - s_start >= tn.max_steps) { set_err(c, kErrIterLimit, 21); return -1; }
-    const StepIn in = step_read(c, st.s);
-    qlo = qhi;
-    qhi = qlo + in.count;
-    // a pull step does not read the push degrees of what it finds; its
-    // frontier edge count is estimated from the average degree
-    const unsigned long long medges =
-        prev_pull ? (unsigned long long)((double)in.count * avg) : in.edges;
-    if (prev_pull) {
-      cand_cur = cand_next;
-      ncur = in.cand;
-      cand_next = (cand_next == w.candA) ? w.candB : w.candA;
-      remaining = in.cand;
-    } else {
-      remaining = remaining > in.count ? remaining - in.count : 0;
+    if (st.s - s_start >= tn.max_steps) { set_err(c, kErrIterLimit, 21); return false; }
+    if (t == 0) {
+      int nactive = 0, any_pull = 0;
+      for (int k = 0; k < ns; ++k) {
+        Search& q = S[k];
+        q.ti = -1;
+        if (!q.active) continue;
+        const StepIn in = step_read(c, st.s, q.dir);
+        q.qlo = q.qhi;
+        q.qhi = q.qlo + in.count;
+        q.huge = in.huge;
+        // a pull step does not read the push degrees of what it finds; its
+        // frontier edge count is estimated from the average degree
+        const unsigned long long medges =
+            q.prev_pull ? (unsigned long long)((double)in.count * q.avg) : in.edges;
+        if (q.prev_pull) {
+          q.cand_cur = q.cand[q.cn];
+          q.ncur = in.cand;
+          q.cn ^= 1;
+          q.remaining = in.cand;
+        } else {
+          q.remaining = q.remaining > in.count ? q.remaining - in.count : 0;
+        }
+        // push -> pull when the frontier's edges outweigh the unexplored
+        // edges (estimated from the unreached candidates); pull -> push when
+        // the frontier is small against the candidates
+        if (!q.pull) {
+          const double mu = (double)q.remaining * q.avg;
+          if ((double)medges * (double)tn.alpha > mu) q.pull = true;
+        } else if ((double)in.count * (double)tn.beta < (double)q.R.ncand) {
+          q.pull = false;
+        }
+        if (b == 0) {
+          q.ti = c->ntrace % kTrace;
+          c->trace[q.ti].t = gtimer();
+          c->trace[q.ti].t_mid = 0;
+          c->trace[q.ti].nwarp = 0;
+          c->trace[q.ti].nblock = 0;
+          c->trace[q.ti].count = in.count;
+          c->trace[q.ti].mode =
+              (q.pull ? 1 : 0) | (in.huge > 0 ? 2 : 0) | (q.R.stat_slot == kStBwSteps ? 4 : 0);
+          c->ntrace++;
+        }
+        if (in.count == 0 && (q.pull || in.huge == 0)) {
+          q.active = false;
+          continue;
+        }
+        ++nactive;
+        any_pull |= q.pull ? 1 : 0;
+      }
+      flags[0] = nactive;
+      flags[1] = any_pull;
     }
-    // push -> pull when the frontier's edges outweigh the unexplored edges
-    // (estimated from the unreached candidates); pull -> push when the
-    // frontier is small against the candidates
-    if (!pull) {
-      const double mu = (double)remaining * avg;
-      if ((double)medges * (double)tn.alpha > mu) pull = true;
-    } else if ((double)in.count * (double)tn.beta < (double)R.ncand) {
-      pull = false;
+    __syncthreads();
+    if (flags[0] == 0) break;
+    const bool any_pull = flags[1] != 0;
+    for (int k = 0; k < ns; ++k) {
+      const Search& q = S[k];
+      if (!q.active) continue;
+      Slot* o = step_out(c, st.s, q.dir);
+      if (!q.pull) {
+        const ReachVisit<NC> rv{q.R.allow, q.R.vis, q.R.push};
+        const Sink sk = sink_make(q.R.q, q.qhi, w.n, o, true, q.R.minv, q.heavy[q.hsel ^ 1], w.n,
+                                  201);
+        expand<NC>(q.R.q + q.qlo, (int32_t)(q.qhi - q.qlo), q.heavy[q.hsel], q.huge, q.R.push, rv,
+                   sk, tn, sm, c, ty);
+      } else {
+        pull_thread<NC>(q.R, A, w, sm, ty, q.cand_cur, q.ncur, q.cand[q.cn], q.qhi, o, q.pp,
+                        q.dir, q.wl, q.bl);
+      }
     }
-    if (b == 0 && t == 0) {
-      const int ti = c->ntrace % kTrace;
-      c->trace[ti].t = gtimer();
-      c->trace[ti].t_mid = 0;
-      c->trace[ti].nwarp = 0;
-      c->trace[ti].nblock = 0;
-      c->trace[ti].count = in.count;
-      c->trace[ti].mode = (pull ? 1 : 0) | (in.huge > 0 ? 2 : 0) | (R.stat_slot == kStBwSteps ? 4 : 0);
-      c->ntrace++;
+    if (any_pull) {
+      // the warp and block tiers need the complete lists
+      if (!grid_barrier(c, 206)) return false;
+      for (int k = 0; k < ns; ++k) {
+        const Search& q = S[k];
+        if (!q.active || !q.pull) continue;
+        if (b == 0 && t == 0 && q.ti >= 0) {
+          c->trace[q.ti].t_mid = gtimer();
+          c->trace[q.ti].nwarp = __ldcg(&c->lcount[q.dir][q.pp & 1][0]);
+          c->trace[q.ti].nblock = __ldcg(&c->lcount[q.dir][q.pp & 1][1]);
+        }
+        pull_tail<NC>(q.R, A, w, sm, ty, q.cand[q.cn], q.qhi, step_out(c, st.s, q.dir), q.pp,
+                      q.dir, q.wl, q.bl);
+      }
     }
-    if (in.count == 0 && (pull || in.huge == 0)) break;
-    Slot* o = step_out(c, st.s);
-    if (!pull) {
-      const Sink sk = sink_make(R.q, qhi, w.n, o, true, R.minv, hl[hsel ^ 1], w.n, 201);
-      expand<NC>(R.q + qlo, (int32_t)(qhi - qlo), hl[hsel], in.huge, R.push, rv, sk, tn, sm, c, ty);
-      prev_pull = false;
-    } else {
-      if (!pull_step<NC>(R, A, w, sm, ty, cand_cur, ncur, cand_next, qhi, o, pp)) return -1;
-      ++pp;
-      prev_pull = true;
-      stat_inc(c, kStPullSteps);
+    __syncthreads();
+    if (t == 0) {
+      for (int k = 0; k < ns; ++k) {
+        Search& q = S[k];
+        if (!q.active) continue;
+        if (q.pull) {
+          ++q.pp;
+          stat_inc(c, kStPullSteps);
+        }
+        q.prev_pull = q.pull;
+        stat_inc(c, q.R.stat_slot);
+        q.hsel ^= 1;
+      }
     }
-    stat_inc(c, R.stat_slot);
-    if (!step_sync(c, st, 24)) return -1;
-    hsel ^= 1;
+    if (!step_sync(c, st, 24)) return false;
   }
-  return (int)qhi;
+  return true;
 }
 
 // ------------------------------------------------------------------------
@@ -1659,34 +1772,109 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   F.q = w.q;
   F.minv = batch ? nullptr : &c->minv[0];
   F.stat_slot = kStFwSteps;
-  int pp = 0;  // pull steps so far (selects the long-list counters)
-  const int nf = reach<NC>(F, A, w, sm, st, ty, pp);
-  if (nf < 0) return;
-  if (b == 0 && t == 0) c->nvisit_fw = nf;
-  if (scc) {
-    // backward inside the forward set; its candidates are the forward set
-    ReachSpec B;
-    B.push = adj1(g.in);
-    B.pull = adj1(g.out);
-    B.allow = w.fvis;
-    B.vis = w.bvis;
-    B.cand = w.q;
-    B.ncand = nf;
-    B.m_cand = F.m_cand;
-    B.roots = roots;
-    B.nroots = nroots;
-    B.q = w.x0;
-    B.minv = batch ? nullptr : &c->minv[1];
-    B.stat_slot = kStBwSteps;
-    const int nb = reach<1>(B, A, w, sm, st, ty, pp);
-    if (nb < 0) return;
-    if (b == 0 && t == 0) c->nscc_fwbw = nb;
-    hit = w.bvis;
-    hit_min = &c->minv[1];
-  } else {
-    if (b == 0 && t == 0) c->nscc_fwbw = nf;
-    hit = w.fvis;
-    hit_min = &c->minv[0];
+  // the search states live in shared memory (one copy per block, written
+  // by thread 0), not in every thread's local memory
+  __shared__ Search srch[2];
+  __shared__ int sflags[2];
+  Search& SF = srch[0];
+  Search& SB = srch[1];
+  if (t == 0) {
+    SF.R = F;
+    SF.dir = 0;
+    SF.cand[0] = w.candA;
+    SF.cand[1] = w.candB;
+    SF.heavy[0] = w.h0;
+    SF.heavy[1] = w.h1;
+    SF.wl = w.x1;
+    SF.bl = w.h1;
+    // the backward search's lists are all its own (live-degree counters,
+    // colours and the second valid list are free until the later phases)
+    SB.dir = 1;
+    SB.cand[0] = w.live_in;
+    SB.cand[1] = w.live_out;
+    SB.heavy[0] = w.colour;
+    SB.heavy[1] = w.listB;
+    SB.wl = w.xa;
+    SB.bl = w.xb;
+  }
+  ReachSpec B;
+  B.push = adj1(g.in);
+  B.pull = adj1(g.out);
+  B.m_cand = F.m_cand;
+  B.roots = roots;
+  B.nroots = nroots;
+  B.q = w.x0;
+  B.stat_slot = kStBwSteps;
+  // SCC of one graph from a hub pivot: both searches run in the same steps,
+  // the backward one over the whole valid set, and the component is what
+  // both reach.  Otherwise (a low-degree pivot, where the backward set can
+  // be far larger than the forward one; batches) the backward search runs
+  // after the forward one, inside the forward set, as the reference does.
+  bool together = false;
+  if constexpr (NC == 1) {
+    if (scc && !batch) {
+      const long long dout = g.out.off[pivot + 1] - g.out.off[pivot];
+      const long long din = g.in.off[pivot + 1] - g.in.off[pivot];
+      together = (dout < din ? dout : din) >= kTogetherDegree;
+    }
+    if (together) {
+      B.allow = w.vbits;
+      B.vis = w.bvis;
+      B.cand = w.listA;
+      B.ncand = nvalid;
+      B.minv = nullptr;
+      if (t == 0) SB.R = B;
+      __syncthreads();
+      if (!reach_multi<NC>(srch, 2, sflags, A, w, sm, st, ty)) return;
+      if (b == 0 && t == 0) c->nvisit_fw = (int32_t)SF.qhi;
+      // the component is what both searches reached: its smallest member
+      // and its size, while the backward bitmap becomes the intersection
+      int32_t mn = 0x7fffffff;
+      int cnt = 0;
+      for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
+        const uint32_t bw = __ldcg(w.bvis + wd);
+        const uint32_t x = __ldcg(w.fvis + wd) & bw;
+        if (x != bw) w.bvis[wd] = x;
+        if (x) {
+          const int32_t v0 = (int32_t)(wd * 32 + __ffs(x) - 1);
+          mn = v0 < mn ? v0 : mn;
+          cnt += __popc(x);
+        }
+      }
+      mn = warp_min(mn);
+      for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+      if (lane_id() == 0) {
+        if (mn != 0x7fffffff) atomicMin(&c->minv[1], mn);
+        if (cnt) atomicAdd(&c->nscc_fwbw, cnt);
+      }
+      if (!step_sync(c, st, 28)) return;
+      hit = w.bvis;
+      hit_min = &c->minv[1];
+    }
+  }
+  if (!together) {
+    __syncthreads();
+    if (!reach_multi<NC>(&SF, 1, sflags, A, w, sm, st, ty)) return;
+    const int32_t nf = (int32_t)SF.qhi;
+    if (b == 0 && t == 0) c->nvisit_fw = nf;
+    if (scc) {
+      // backward inside the forward set; its candidates are the forward set
+      B.allow = w.fvis;
+      B.vis = w.bvis;
+      B.cand = w.q;
+      B.ncand = nf;
+      B.minv = batch ? nullptr : &c->minv[1];
+      if (t == 0) SB.R = B;
+      __syncthreads();
+      if (!reach_multi<1>(&SB, 1, sflags, A, w, sm, st, ty)) return;
+      if (b == 0 && t == 0) c->nscc_fwbw = (int32_t)SB.qhi;
+      hit = w.bvis;
+      hit_min = &c->minv[1];
+    } else {
+      if (b == 0 && t == 0) c->nscc_fwbw = nf;
+      hit = w.fvis;
+      hit_min = &c->minv[0];
+    }
   }
   // batch: the smallest member of each graph's component labels it
   if (batch) {

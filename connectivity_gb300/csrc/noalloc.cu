@@ -41,7 +41,7 @@ constexpr size_t kWords = (size_t)(kNoAllocMaxVertices + 32) / 32 + 2;
 constexpr size_t kBm = al256(kWords * 4);
 constexpr size_t kCtl = al256(sizeof(gb::Ctl));
 constexpr size_t kScratchBytes =
-    kCtl + 14 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8) + 256;
+    kCtl + 16 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8) + 256;
 
 // The scratch.  Host code must not pass this name to a kernel: on the host
 // it is a stand-in symbol, not a device address; its device address comes
@@ -129,6 +129,8 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.candB = (int32_t*)take(kArr);
   w.h0 = (int32_t*)take(kArr);
   w.h1 = (int32_t*)take(kArr);
+  w.xa = (int32_t*)take(kArr);
+  w.xb = (int32_t*)take(kArr);
   w.vbits = (uint32_t*)take(kBm);
   w.fvis = (uint32_t*)take(kBm);
   w.bvis = (uint32_t*)take(kBm);
