@@ -356,14 +356,15 @@ __device__ __forceinline__ Adj adj_undirected(const GraphView& g) {
 // moves them to the global list in one atomic + coalesced copy per kWB
 // entries, which keeps the step counters (a single L2 word) cool.
 // ------------------------------------------------------------------------
-constexpr int kWB = 512;
+constexpr int kWB = 256;
 // Per-warp backlog of pull candidates the hint did not settle (entries).
 constexpr int kTodo = 384;
 // Dynamic shared memory of the cooperative kernels: two staging buffers and
 // one pull backlog per warp.
-constexpr int kDynSmem = kWarps * (2 * kWB + kTodo) * 4;
-// a warp's two staging buffers also hold the ids of 32 bitmap words
-static_assert(2 * kWB >= 32 * 32, "staging buffers too small for 32 words");
+constexpr int kWarpSmem = 2 * kWB + kTodo;
+constexpr int kDynSmem = kWarps * kWarpSmem * 4;
+// a warp's shared memory also holds the ids of 16 bitmap words
+static_assert(kWB * 2 + kTodo >= 16 * 32, "warp shared memory too small for 16 words");
 
 // A global output list.
 struct Out {
@@ -464,12 +465,14 @@ struct Smem {
   long long red_l[kWarps];
   unsigned long long red_u[4 * kWarps];  // statistics tallies, per warp
   int red_i[kWarps];
-  int32_t* stage_base;  // dynamic shared memory: kWarps x 2 x kWB, then kWarps x kTodo
+  // dynamic shared memory: per warp, contiguous, two staging buffers of kWB
+  // entries then a pull backlog of kTodo entries (kWarpSmem entries in all)
+  int32_t* stage_base;
   __device__ __forceinline__ int32_t* stage(int warp, int k) {
-    return stage_base + (warp * 2 + k) * kWB;
+    return stage_base + warp * kWarpSmem + k * kWB;
   }
   __device__ __forceinline__ int32_t* todo(int warp) {
-    return stage_base + kWarps * 2 * kWB + warp * kTodo;
+    return stage_base + warp * kWarpSmem + 2 * kWB;
   }
 };
 extern __shared__ __align__(16) int32_t g_dyn_smem[];
@@ -1188,16 +1191,27 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
       // each lane puts its word's ids at their ranks in the warp's staging
       // buffer (visiting its bits from bit `lane` on, so that the lanes of
       // dense words hit different banks), then the warp copies the buffer out
-      int32_t* buf = sm.stage(warp, 0);  // 2 * kWB >= 1024 entries
-      unsigned y = (x >> lane) | (lane ? x << (32 - lane) : 0u);
-      while (y) {
-        const int p = __ffs(y) - 1;
-        y &= y - 1;
-        const int bit = (p + lane) & 31;
-        buf[ex + __popc(x & ((1u << bit) - 1u))] = (int32_t)(wd * 32 + bit);
+      // (the warp's shared memory holds kWarpSmem ids: denser groups go in
+      // two halves of 16 words)
+      int32_t* buf = sm.stage(warp, 0);
+      const bool split = tot > kWarpSmem;
+      const int half = split ? __shfl_sync(kFull, ex, 16) : tot;  // ids of the first pass
+      for (int hh = 0; hh < (split ? 2 : 1); ++hh) {
+        const int r0 = hh ? half : 0;
+        const int cnt = hh ? tot - half : half;
+        if (!split || (lane >> 4) == hh) {
+          unsigned y = (x >> lane) | (lane ? x << (32 - lane) : 0u);
+          while (y) {
+            const int p = __ffs(y) - 1;
+            y &= y - 1;
+            const int bit = (p + lane) & 31;
+            buf[ex - r0 + __popc(x & ((1u << bit) - 1u))] = (int32_t)(wd * 32 + bit);
+          }
+        }
+        __syncwarp();
+        for (int k = lane; k < cnt; k += 32) w.listA[o + r0 + k] = buf[k];
+        __syncwarp();
       }
-      __syncwarp();
-      for (int k = lane; k < tot; k += 32) w.listA[o + k] = buf[k];
       ty.list += __popc(x);
       __syncthreads();
     }
