@@ -480,7 +480,17 @@ def run_gbconn(args):
                 "touched_bytes_per_launch": int(touched),
                 "touched_gbs": round(touched / (ms / 1e3) / 1e9, 1)}
 
-    reach = roof("k_reach", reach8d, float(pm[1]), st.bytes_reach)
+    # the run is one cooperative kernel (k_run) whose phases are timed on the
+    # device; the roofline is the kernel's, with each phase beside it
+    run_ms = float(pm[0] + pm[1] + pm[2])
+    run8d = trim8d + reach8d + st.bytes_colour
+    run = roof("k_run", run8d, run_ms, st.bytes_trim + st.bytes_reach + st.bytes_colour)
+    phases = [dict(roof("trim", trim8d, float(pm[0]), st.bytes_trim), kernel="k_run: trim phase"),
+              dict(roof("reach", reach8d, float(pm[1]), st.bytes_reach),
+                   kernel="k_run: reachability phase"),
+              dict(roof("colour", st.bytes_colour, float(pm[2]), st.bytes_colour),
+                   kernel="k_run: colour phase (bytes touched)")]
+    traffic = profile_traffic("k_run") if args.scale == SCALE else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": round(step_ms, 4), "higher_is_better": True,
@@ -494,27 +504,26 @@ def run_gbconn(args):
                 "ms_per_step": round(TE / KE * 1e3, 3), "steps": KE,
                 "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers)",
                 "labels_match_device_run": e2e_ok},
-        "roofline": {"bound": "hbm", "kernel": "k_reach (FW-BW reachability + commit)",
-                     "achieved": reach["achieved"], "peak": peak, "unit": "GB/s",
-                     "frac": reach["frac"], "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "traffic": profile_traffic() if args.scale == SCALE else None,
+        "roofline": {"bound": "hbm",
+                     "kernel": "k_run<1> (one cooperative launch per run: trim, reachability, "
+                               "colour phases)",
+                     "achieved": run["achieved"], "peak": peak, "unit": "GB/s",
+                     "frac": run["frac"], "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
+                     "traffic": traffic,
                      "traffic_source": "profiles/traffic.json (ncu, one capture at scale 24)",
-                     "dram_gbs_at_traffic": (round(profile_traffic() / (float(pm[1]) / 1e3) / 1e9, 1)
-                                             if profile_traffic() and args.scale == SCALE
-                                             else None),
-                     "algorithmic_bytes_per_launch": reach["algorithmic_bytes_per_launch"],
-                     "launch_ms": reach["launch_ms"],
-                     "touched_bytes_per_launch": reach["touched_bytes_per_launch"],
+                     "dram_gbs_at_traffic": (round(traffic / (run_ms / 1e3) / 1e9, 1)
+                                             if traffic else None),
+                     "algorithmic_bytes_per_launch": run["algorithmic_bytes_per_launch"],
+                     "launch_ms": run["launch_ms"],
+                     "touched_bytes_per_launch": run["touched_bytes_per_launch"],
                      "units": {"n": n, "m": m, "m_visit_fw": st.m_visit_fw,
                                "m_visit_bw": st.m_visit_bw, "pull_steps": st.pull_steps,
                                "pull_edges_scanned": st.pull_edges},
-                     "kernels": [roof("k_trim", trim8d, float(pm[0]), st.bytes_trim), reach,
-                                 roof("k_colour", st.bytes_colour, float(pm[2]),
-                                      st.bytes_colour)]},
+                     "phases": phases},
         "phases_ms": {k: round(float(v), 4) for k, v in
                       zip(("trim", "reach", "colour", "tail", "total"), pm)},
-        "gpu_launches": 4 * K,
-        "gpu_launches_note": "k_trim, k_reach, k_colour and the status latch per step",
+        "gpu_launches": 2 * K,
+        "gpu_launches_note": "k_run (one cooperative launch) and the status latch per step",
         "clocks": ck,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -14,7 +14,7 @@
 //   - at most kNoAllocMaxVertices vertices; larger graphs are rejected with
 //     GB_ERR_CAPACITY before any work is queued;
 //   - the array is held by every GPU that loads the library, until exit
-//     (about 15 MB);
+//     (about 17 MB);
 //   - all calls share the array and it keeps the last call's contents; every
 //     call clears what must start at zero.  Calls whose work overlaps on the
 //     GPU (two streams, or two host threads) race on it: serialise them.

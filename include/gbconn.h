@@ -225,7 +225,7 @@ gb_status gb_wcc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, cons
  * framework's memory pool, plug-ins whose host process has reserved or capped
  * device memory, loops that cannot take an allocation's latency or failure):
  * the run's scratch is a fixed static device array inside the library (about
- * 15 MB, held by every GPU that loads the library until exit).  The CSR
+ * 17 MB, held by every GPU that loads the library until exit).  The CSR
  * (out_off/in_off n+1 entries, out_adj/in_adj m entries) and labels (n
  * entries, canonical minimum member ids) are device memory owned by the
  * caller; the work goes on `stream` (NULL: the legacy default stream) and
