@@ -84,7 +84,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel="k_reach"):
+def profile_traffic(kernel="k_run"):
     """DRAM bytes per launch of a kernel from the committed ncu summary
     (profiles/traffic.json, R-MAT scale 24), or None."""
     try:

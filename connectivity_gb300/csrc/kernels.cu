@@ -1,25 +1,27 @@
 // Multistep SCC / WCC on one GB300: trim, direction-optimising FW-BW
-// reachability from a pivot, max-colour rounds to a fixed point, and
-// relabelling to each component's minimum vertex id.
+// reachability from a pivot, min-colour rounds to a fixed point; every label
+// is its component's minimum vertex id when it is assigned.
 //
-// Each phase is one cooperative persistent kernel (all blocks resident) that
-// runs its whole level loop on the device: a "step" is a grid-strided pass
-// over a frontier or candidate list ended by a bounded grid barrier, and the
+// A run is one cooperative persistent kernel (k_run, all blocks resident)
+// whose three phases are separated by grid barriers.  Each phase runs its
+// whole level loop on the device: a "step" is a grid-strided pass over a
+// frontier or candidate list ended by a bounded grid barrier, and the
 // counters that steer the next step (frontier size, frontier edge count,
-// deferred heavy vertices) rotate through three slots of the control block so
-// that no block reads a counter another block is still writing.  The host
+// deferred heavy vertices) rotate through three slots of the control block
+// so that no block reads a counter another block is still writing.  The host
 // never waits between levels.
 //
 // Reference phases (HPCGraphAnalysis/Connectivity, multistep/):
-//   k_trim    scc_trim (scc_trim.cpp:89-139), scc_trim_complete (:141-297),
-//             cc_trim (cc_trim.cpp:47-97), pivot rule of create_csr
-//             (scc_main.cpp:169-182, cc_main.cpp:148-160)
-//   k_reach   scc_fwbw_fw / scc_fwbw_bw / update_valid (scc_fwbw.cpp:47-466),
-//             cc_bfs_search / update_valid (cc_bfs.cpp:47-271)
-//   k_colour  scc_color (scc_color.cpp:47-373) run until no vertex is left,
-//             which replaces the serial Tarjan step (scc_serial.cpp:160-258);
-//             cc_color_propagate (cc_color.cpp:47-175)
-//   k_canon   maps every label to its component's minimum id
+//   trim phase    scc_trim (scc_trim.cpp:89-139), scc_trim_complete
+//                 (:141-297), cc_trim (cc_trim.cpp:47-97), pivot rule of
+//                 create_csr (scc_main.cpp:169-182, cc_main.cpp:148-160)
+//   reach phase   scc_fwbw_fw / scc_fwbw_bw / update_valid
+//                 (scc_fwbw.cpp:47-466), cc_bfs_search / update_valid
+//                 (cc_bfs.cpp:47-271)
+//   colour phase  scc_color (scc_color.cpp:47-373) run until no vertex is
+//                 left, which replaces the serial Tarjan step
+//                 (scc_serial.cpp:160-258); cc_color_propagate
+//                 (cc_color.cpp:47-175)
 #include "gb_internal.cuh"
 
 namespace gb {
@@ -911,7 +913,7 @@ __device__ bool compact_ordered(const int32_t* in, int32_t nin, int32_t* out, co
 }
 
 // ------------------------------------------------------------------------
-// k_trim: labels, valid bitmap, valid list (ordered), pivot, m_cand.
+// Trim phase: labels, valid bitmap, valid list (ordered), pivot, m_cand.
 // SCC: a vertex with no out- or no in-edge is its own component
 // (scc_trim, scc_trim.cpp:101-126); level 2 iterates to the fixed point with
 // live degree counters.  WCC: a vertex with no edge at all (cc_trim.cpp:59-
@@ -1749,7 +1751,7 @@ __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const
 }
 
 // ------------------------------------------------------------------------
-// k_reach: SCC -> forward and backward reachability from the pivot; the SCC
+// Reach phase: SCC -> forward and backward reachability from the pivot; the SCC
 // (reached both ways) leaves the valid list labelled with its smallest id
 // (or the pivot, with canonical labels off), as update_valid does with the
 // pivot (scc_fwbw, scc_fwbw.cpp:412-513).  WCC -> one search over the union
@@ -1930,7 +1932,7 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
 }
 
 // ------------------------------------------------------------------------
-// k_colour: rounds of colour propagation until no vertex is left.
+// Colour phase: rounds of colour propagation until no vertex is left.
 // SCC: each round propagates colours along out-edges to the fixed point;
 // every vertex whose colour is its own id is a root; a backward search over
 // same-colour vertices labels the root's SCC with the colour; the rest stay

@@ -85,8 +85,9 @@ typedef struct gb_opts {
 
 void gb_opts_default(gb_opts* o);
 
-/* Per-run results.  Times are device times between CUDA events on the
- * context stream, in milliseconds. */
+/* Per-run results.  Times are in milliseconds: trim, reach and colour from
+ * the device clock at the run kernel's phase boundaries; canon (the
+ * statistics pass) and total from CUDA events on the context stream. */
 typedef struct gb_stats {
   double ms_trim, ms_reach, ms_colour, ms_canon, ms_total;
   int32_t pivot;          /* FW-BW source, -1 if none */
@@ -121,15 +122,19 @@ void* gb_ctx_stream(gb_ctx* ctx);
  * raised by any run since the last wait. */
 gb_status gb_ctx_sync(gb_ctx* ctx);
 /* Device times of the last `count` runs (count <= 64), oldest first, five
- * values per run in milliseconds: trim, reach, colour, canon, total.  Waits
- * for the context's stream.  Lets a caller time every kernel of a run of
- * asynchronous calls. */
+ * values per run in milliseconds: trim, reach, colour (device clock at the
+ * run kernel's phase boundaries), the statistics pass, and the run's total
+ * (CUDA events).  Waits for the context's stream.  Lets a caller time every
+ * phase of a run of asynchronous calls. */
 gb_status gb_ctx_phase_times(gb_ctx* ctx, int32_t count, double* ms);
-/* Diagnostic: the step trace of the reachability phase of the context's
- * last completed run, oldest first: device time (ns) at the start of each
- * step's decision, vertices appended by the previous step, and mode bits
- * (1: pull step, 2: heavy vertices pending, 4: backward search).  Writes up
- * to cap entries and returns how many were written (0 on error). */
+/* Diagnostic: the step trace of the context's last completed run (its last
+ * 128 records), oldest first: device time (ns) at the start of each step,
+ * the step's input count, and a mode.  Reachability steps: bit 0 pull step,
+ * bit 1 heavy vertices pending, bit 2 backward search.  Colour steps: 8
+ * colours reset, 9 propagation, 10 roots, 11 same-colour marking, 12
+ * compaction; 15 end of a phase.  Trim: 16 start, 17 degree pass done, 18
+ * list counted, 19 list written.  Writes up to cap entries and returns how
+ * many were written (0 on error). */
 int32_t gb_ctx_reach_trace(gb_ctx* ctx, int64_t* t_ns, int32_t* count, int32_t* mode, int32_t cap);
 /* As gb_ctx_reach_trace, plus three values per step in extra (3 x cap):
  * for pull steps, ns from the step's start to the end of its thread tier,
