@@ -282,6 +282,9 @@ def batched_section(gb, ctx, stream, steps, sample=400):
     t_alone = e0.elapsed_time(e1) / 1e3
     same = all(np.array_equal(outs[i][:gs[i].n].cpu().numpy(),
                               batch_lab[b.vbase[i]:b.vbase[i + 1]]) for i in range(S))
+    # the autotuner on this batch (device-timed coordinate search)
+    from connectivity_gb300 import tune as gbtune
+    tuned = gbtune.tune_batch(ctx, b, 0, reps=2)
     out = {
         "workload": (f"{b.count:,} R-MAT graphs, vertex counts log-normal (median 2,000, sigma "
                      f"1.5, clipped 64..500,000), edge factor uniform 4..32 ({b.n:,} vertices, "
@@ -293,6 +296,9 @@ def batched_section(gb, ctx, stream, steps, sample=400):
         "per_graph_sample": f"first {S} graphs of the batch, resident, gb_scc_async back to back",
         "speedup_vs_per_graph": round((b.count / t_scc) / (S / t_alone), 1),
         "labels_equal_per_graph_runs": bool(same), "build_s": round(build_s, 2),
+        "autotuned": {"graphs_per_s": round(b.count / (tuned["ms"] / 1e3), 1),
+                      "defaults_graphs_per_s": round(b.count / (tuned["default_ms"] / 1e3), 1),
+                      "opts": tuned["opts"]},
     }
     for g in gs:
         g.close()
@@ -438,6 +444,14 @@ def run_gbconn(args):
     step_ms = T / K * 1e3
     value = job_gteps(m, ws, T, K)
 
+    # the autotuner on this graph (its timed runs are outside the timed region)
+    o_t, ms_t, ms_d = ctx.tune(g, 0, 3)
+    from connectivity_gb300 import tune as gbtune
+    autotuned = {"value": round(job_gteps(m, 1, ms_t / 1e3, 1), 3),
+                 "defaults_value": round(job_gteps(m, 1, ms_d / 1e3, 1), 3),
+                 "opts": gbtune.opts_to_dict(o_t),
+                 "note": "device time of one run, best of 3, after the coordinate search"}
+
     # one more run with statistics (algorithmic bytes of each kernel)
     lab_dev, st = ctx.scc(g, labels=labels.data_ptr(), stats=True)
     gpu_labels = labels.cpu().numpy()
@@ -520,6 +534,7 @@ def run_gbconn(args):
                                "m_visit_bw": st.m_visit_bw, "pull_steps": st.pull_steps,
                                "pull_edges_scanned": st.pull_edges},
                      "phases": phases},
+        "autotuned": autotuned,
         "phases_ms": {k: round(float(v), 4) for k, v in
                       zip(("trim", "reach", "colour", "tail", "total"), pm)},
         "gpu_launches": 2 * K,

@@ -122,6 +122,8 @@ for _n in ("gb_batch_scc", "gb_batch_wcc"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
 _sig("gb_batch_scc_async", C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
 _sig("gb_batch_destroy", C.c_int32, [_P])
+_sig("gb_tune", C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.POINTER(Opts), _P])
+_sig("gb_tune_batch", C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.POINTER(Opts), _P])
 
 
 class ServerStats(C.Structure):
@@ -398,6 +400,14 @@ class Context:
     def batch_scc_async(self, b: "Batch", labels_dev: int, o: Opts | None = None) -> None:
         _check(_lib.gb_batch_scc_async(self._h, b._h, C.c_void_p(labels_dev), C.byref(o or opts())),
                "gb_batch_scc_async")
+
+    def tune(self, target, kind: int = 0, reps: int = 3) -> tuple["Opts", float, float]:
+        """Autotuned options for a Graph or a Batch (gb_tune / gb_tune_batch),
+        the best device time and the defaults' time, in ms."""
+        o, ms = Opts(), (C.c_double * 2)()
+        fn = _lib.gb_tune_batch if isinstance(target, Batch) else _lib.gb_tune
+        _check(fn(self._h, target._h, int(kind), int(reps), C.byref(o), ms), "gb_tune")
+        return o, ms[0], ms[1]
 
     def pivot(self, g: "Graph", kind: int = 0) -> tuple[int, float]:
         p, a = C.c_int32(), C.c_double()

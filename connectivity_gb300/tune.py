@@ -1,0 +1,67 @@
+"""Size-class tuning tables for the run's tunables.
+
+The device autotuner (``gb_tune`` / ``gb_tune_batch``) times runs of one
+graph or batch and returns the best options for it.  This module runs it on
+one seeded R-MAT graph per size class and keeps the winners in a JSON table;
+``opts_for`` then picks the options of the class nearest a graph's size (by
+log2 of the vertex count).  Labels never depend on the options.
+"""
+from __future__ import annotations
+
+import json
+import math
+
+from . import Batch, Context, Graph, Opts, opts
+
+# (vertices, edge factor) of the classes tuned by default
+CLASSES = [(1 << 10, 8), (1 << 14, 16), (1 << 18, 16), (1 << 22, 16), (1 << 24, 16)]
+
+TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks")
+
+
+def opts_to_dict(o: Opts) -> dict:
+    return {k: getattr(o, k) for k in TUNED}
+
+
+def dict_to_opts(d: dict) -> Opts:
+    return opts(**{k: d[k] for k in TUNED if k in d})
+
+
+def tune_classes(ctx: Context, kind: int = 0, classes=CLASSES, reps: int = 3,
+                 seed: int = 1) -> dict:
+    """{"kind": kind, "classes": [{"n", "edge_factor", "ms", "default_ms", "opts"}]}"""
+    out = []
+    for n, ef in classes:
+        g = Graph.rmat_n(ctx, n, ef, seed)
+        o, ms, dms = ctx.tune(g, kind, reps)
+        out.append({"n": int(n), "edge_factor": int(ef), "ms": ms, "default_ms": dms,
+                    "opts": opts_to_dict(o)})
+        g.close()
+    return {"kind": int(kind), "classes": out}
+
+
+def tune_batch(ctx: Context, b: Batch, kind: int = 0, reps: int = 3) -> dict:
+    o, ms, dms = ctx.tune(b, kind, reps)
+    return {"count": b.count, "n": b.n, "m": b.m, "ms": ms, "default_ms": dms,
+            "opts": opts_to_dict(o)}
+
+
+def save(table: dict, path: str) -> None:
+    with open(path, "w") as f:
+        json.dump(table, f, indent=1)
+
+
+def load(path: str) -> dict:
+    with open(path) as f:
+        return json.load(f)
+
+
+def opts_for(table: dict, n: int) -> Opts:
+    """Options of the class whose vertex count is nearest n on a log scale
+    (the defaults when the table is empty)."""
+    classes = table.get("classes", [])
+    if not classes:
+        return opts()
+    ln = math.log2(max(n, 1))
+    best = min(classes, key=lambda c: abs(math.log2(max(c["n"], 1)) - ln))
+    return dict_to_opts(best["opts"])

@@ -275,6 +275,21 @@ gb_status gb_batch_scc_async(gb_ctx* ctx, const gb_batch* b, int32_t* labels_dev
                              const gb_opts* opts);
 gb_status gb_batch_destroy(gb_batch* b);
 
+/* ---- autotuner ---------------------------------------------------------- */
+/* No counterpart in the reference (its switch constants are fixed,
+ * scc_main.cpp:64-65).  Picks the run's tunables for one graph or batch by
+ * timing runs on the device: the push-tier degree cutoffs (t_block, t_grid),
+ * the pull step's per-thread edge budget (k_pull), the direction-switch
+ * factors (alpha, beta) and the number of resident blocks (grid_blocks).
+ * Coordinate descent from gb_opts_default over a fixed candidate set, two
+ * passes; each time is the minimum of `reps` device-timed runs after one
+ * warm-up.  kind 0 = SCC, 1 = WCC.  ms (2 values, or NULL): the best time
+ * and the defaults' time.  Labels do not depend on the tunables. */
+gb_status gb_tune(gb_ctx* ctx, const gb_graph* g, int32_t kind, int32_t reps, gb_opts* best,
+                  double* ms);
+gb_status gb_tune_batch(gb_ctx* ctx, const gb_batch* b, int32_t kind, int32_t reps,
+                        gb_opts* best, double* ms);
+
 /* ---- serving: a request stream with continuous batching --------------- */
 /* No counterpart in the reference, whose equivalent is one run_scc / run_cc
  * call per request (multistep/scc_main.cpp:210, cc_main.cpp:184).  A server

@@ -153,3 +153,19 @@ def test_file_writers_round_trip(tmp_path):
     assert np.frombuffer(raw[8:24], np.int64).tolist() == [n, 999]
     assert np.array_equal(np.frombuffer(raw[24:24 + 4 * 999], np.int32), s)
     assert np.array_equal(np.frombuffer(raw[24 + 4 * 999:], np.int32), d)
+
+
+def test_tune_table_lookup():
+    """Size-class tables: options of the class nearest on a log scale."""
+    from connectivity_gb300 import tune
+    assert tune.opts_for({}, 100).t_block == gb.opts().t_block
+    table = {"kind": 0, "classes": [
+        {"n": 1 << 10, "opts": {"t_block": 128, "t_grid": 8192, "k_pull": 2, "alpha": 5.0,
+                                "beta": 10.0, "grid_blocks": 0}},
+        {"n": 1 << 20, "opts": {"t_block": 2048, "t_grid": 131072, "k_pull": 4, "alpha": 50.0,
+                                "beta": 100.0, "grid_blocks": 76}}]}
+    assert tune.opts_for(table, 600).t_block == 128
+    assert tune.opts_for(table, 1 << 19).t_block == 2048
+    o = tune.opts_for(table, 1 << 22)
+    assert (o.t_grid, o.k_pull, o.grid_blocks) == (131072, 4, 76)
+    assert tune.dict_to_opts(tune.opts_to_dict(o)).beta == 100.0
