@@ -193,7 +193,14 @@ def cpu_baseline_run(n, m, oo, oa, io, ia, reps):
         t0 = time.perf_counter()
         oracle.scc(cg, canonical=False)
         best = min(best, time.perf_counter() - t0)
-    return lab, best, oracle.num_threads()
+    # one thread, one run (the per-core figure beside the all-core one)
+    cores = oracle.num_threads()
+    oracle.set_threads(1)
+    t0 = time.perf_counter()
+    oracle.scc(cg, canonical=False)
+    one = time.perf_counter() - t0
+    oracle.set_threads(cores)
+    return lab, best, cores, one
 
 
 def run_reference(args):
@@ -306,7 +313,7 @@ def batched_section(gb, ctx, stream, steps, sample=400):
     return out
 
 
-def served_section(gb, device, rate, seconds, pool_size):
+def served_section(gb, device, rate, seconds, pool_size, tuned_opts=None):
     """gb_server under a Poisson stream; the same arrivals served by one
     launch per request (FIFO over measured per-request service times)."""
     import numpy as np
@@ -348,6 +355,8 @@ def served_section(gb, device, rate, seconds, pool_size):
     outs = [np.empty(pool[i][0], np.int32) for i in idx]
     sctx = gb.Context(device)
     sv = gb.Server(sctx, budget_bytes=0, max_graphs=8192)
+    if tuned_opts is not None:
+        sv.set_opts(tuned_opts)
     for j in range(cnt):
         n, s, d = pool[idx[j]]
         sv.submit(int(kinds[j]), n, s, d, arrival_ns=int(arr[j]), out=outs[j])
@@ -542,11 +551,13 @@ def run_gbconn(args):
         "clocks": ck,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        want, tcpu, cores = cpu_baseline_run(n, m, oo, oa, io, ia, args.cpu_reps)
+        want, tcpu, cores, tone = cpu_baseline_run(n, m, oo, oa, io, ia, args.cpu_reps)
         line["cpu_baseline"] = {
             "value": round(m / tcpu / 1e9, 4), "unit": "GTEPS", "cores": cores, "kind": "port",
             "sample": f"full workload, best of {args.cpu_reps} runs after 1 warm-up "
-                      "(oracle/multistep.c, OpenMP restatement of run_scc)"}
+                      "(oracle/multistep.c, OpenMP restatement of run_scc)",
+            "one_thread_value": round(m / tone / 1e9, 4),
+            "host": {"nproc": os.cpu_count(), "machine": os.uname().machine}}
         line["parity"] = {"labels_equal_oracle": bool(np.array_equal(gpu_labels, want)),
                           "verify_line": gb.scc_verify(gpu_labels).strip()}
     g.close()
@@ -555,8 +566,11 @@ def run_gbconn(args):
         line["batched"] = batched_section(gb, ctx, stream, 5)
     ctx.close()
     if "served" in sections:
+        # (the options the autotuner finds for the 20,000-graph batch do not
+        # suit the server's merged runs of about 60 graphs: defaults)
         line["served"] = served_section(gb, local, args.serve_rate, args.serve_seconds,
                                         args.serve_pool)
+        line["served"]["opts"] = "defaults"
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -135,6 +135,7 @@ class ServerStats(C.Structure):
 
 _sig("gb_server_create", C.c_int32, [_P, C.c_int64, C.c_int32, C.POINTER(_P)])
 _sig("gb_server_start", C.c_int32, [_P])
+_sig("gb_server_set_opts", C.c_int32, [_P, C.POINTER(Opts)])
 _sig("gb_server_submit", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int64, _P, _P, _P, C.c_int64,
                                      _I64P])
 _sig("gb_server_wait", C.c_int32, [_P, C.c_int64, _I64P])
@@ -571,6 +572,10 @@ class Server:
                "gb_server_create")
         self._h = h
         self._keep: dict[int, tuple] = {}
+
+    def set_opts(self, o: "Opts") -> None:
+        """Options of the merged runs (before start)."""
+        _check(_lib.gb_server_set_opts(self._h, C.byref(o)), "gb_server_set_opts")
 
     def start(self) -> None:
         _check(_lib.gb_server_start(self._h), "gb_server_start")

@@ -118,6 +118,7 @@ int64_t request_bytes(int32_t n, int64_t m) {
 
 struct gb_server {
   gb_ctx* ctx = nullptr;
+  gb_opts opts{};   // options of the merged runs
   cudaStream_t copy = nullptr;
   int64_t budget = 0;
   int32_t max_graphs = 0;
@@ -241,7 +242,7 @@ gb_status part_launch(gb_server* sv, Part& p, int kind) {
                                   &p.batch);
   if (st != GB_OK) return st;
   if (cudaMallocAsync(&p.d_labels, (size_t)(p.n > 0 ? p.n : 1) * 4, s) != cudaSuccess) return GB_ERR_OOM;
-  st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels, nullptr, nullptr,
+  st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels, &sv->opts, nullptr,
                      false);
   if (st != GB_OK) return st;
   if (p.n > 0 &&
@@ -360,6 +361,7 @@ gb_status gb_server_create(gb_ctx* ctx, int64_t budget_bytes, int32_t max_graphs
   gb_server* sv = new (std::nothrow) gb_server();
   if (!sv) return GB_ERR_OOM;
   sv->ctx = ctx;
+  gb_opts_default(&sv->opts);
   sv->budget = budget_bytes;
   sv->max_graphs = max_graphs;
   // freed graph memory stays in the pool for the next requests
@@ -377,6 +379,14 @@ gb_status gb_server_create(gb_ctx* ctx, int64_t budget_bytes, int32_t max_graphs
     cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
   }
   *out = sv;
+  return GB_OK;
+}
+
+gb_status gb_server_set_opts(gb_server* sv, const gb_opts* o) {
+  if (!sv || !o) return GB_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (sv->started) return GB_ERR_INVALID;
+  sv->opts = *o;
   return GB_OK;
 }
 

@@ -314,6 +314,9 @@ typedef struct gb_server_stats {
 /* budget_bytes <= 0: half the device's free memory at creation. */
 gb_status gb_server_create(gb_ctx* ctx, int64_t budget_bytes, int32_t max_graphs,
                            gb_server** server);
+/* Options of the merged runs (default gb_opts_default); before the start
+ * only.  gb_tune_batch on a sample of the expected requests finds them. */
+gb_status gb_server_set_opts(gb_server* server, const gb_opts* opts);
 /* Starts the engine and the server clock (t = 0). */
 gb_status gb_server_start(gb_server* server);
 /* kind 0 = SCC, 1 = WCC.  src / dst / labels_out are host arrays that stay
