@@ -59,7 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 16 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8) + 256;
+  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8);
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -71,7 +71,6 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   };
   w.label = (int32_t*)take(arr);
   w.colour = (int32_t*)take(arr);
-  w.stamp = (int32_t*)take(arr);
   w.live_in = (int32_t*)take(arr);
   w.live_out = (int32_t*)take(arr);
   w.listA = (int32_t*)take(arr);
@@ -91,11 +90,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.done = (uint32_t*)take(bm);
   w.blk_i = (int32_t*)take(align256(2 * G * 4));
   w.blk_l = (long long*)take(align256(G * 8));
-  w.iter_next = (int32_t*)take(256);
   w.ctl = c->d_ctl;
-  // stamps start below every step number; numbering starts at 0
-  CK(cudaMemsetAsync(w.stamp, 0xff, arr, c->stream), "workspace init");
-  CK(cudaMemsetAsync(w.iter_next, 0, sizeof(int32_t), c->stream), "workspace init");
   c->cap_n = n;
   return GB_OK;
 }
@@ -318,7 +313,7 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
     CK(cudaMemsetAsync(bv->gmin, 0x7f, (size_t)bv->count * 4, sm), "memset");
   }
   // the reached and done bitmaps are adjacent in the workspace: one memset
-  // clears all three (the stamps need no clearing, see the colour phase)
+  // clears all three
   CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(gb::Ctl), sm), "memset");
   CK(cudaMemsetAsync(w.fvis, 0,
                      (size_t)((char*)(w.done + w.nwords) - (char*)w.fvis), sm),

@@ -131,7 +131,6 @@ struct Work {
   int64_t m;
   int32_t* label;
   int32_t* colour;        // colours; canonicalisation reuses it
-  int32_t* stamp;
   int32_t* live_in;
   int32_t* live_out;
   uint32_t* vbits;        // valid (unassigned) vertices
@@ -151,8 +150,6 @@ struct Work {
   int32_t* xb;            // searches run in the same steps
   int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
   unsigned long long* tphase;  // this run's 4 phase-boundary device times, or null
-  int32_t* iter_next;     // next colour-step number (persists across runs; the
-                          // stamps hold only smaller numbers)
   long long* blk_l;
   Ctl* ctl;
 };

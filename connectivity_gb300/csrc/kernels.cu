@@ -523,6 +523,75 @@ __device__ __forceinline__ void visit_edges(const V& vis, const int32_t (&sv)[kE
 }
 
 constexpr int kSmallFront = 8;
+constexpr int kLocalRounds = 16;       // local rounds per step
+constexpr long long kLocalDegree = 4096;  // heavier vertices go to the next step
+
+// Local rounds (visitors with kLocal): the vertices this warp appended in
+// its stage are expanded by the warp itself, up to kLocalRounds rounds, so a
+// propagation runs several hops per grid step.  Every acceptance hands its
+// vertex to exactly one warp (the colour visitor: each successful lowering;
+// the mark visitor: each claim), and that warp either expands it here, with
+// the vertex's value read now, or appends it for the next step, so nothing
+// is lost.  A vertex heavier than kLocalDegree goes to the next step.
+template <int NC, class V>
+__device__ __forceinline__ void local_rounds(const Adj& a, const V& vis, Stage& st,
+                                             const Sink& sk, Smem& sm, Ctl* c, Tally& ty) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t* loc = sm.stage(warp, 1);  // free in push steps: kWB entries
+  for (int r = 0; r < kLocalRounds; ++r) {
+    const int cnt = st.n;  // warp-uniform, at most kWB
+    if (cnt == 0) break;
+    __syncwarp();
+    for (int i = lane; i < cnt; i += 32) loc[i] = st.buf[i];
+    __syncwarp();
+    st.n = 0;
+    for (int b0 = 0; b0 < cnt; b0 += 32) {
+      const int i = b0 + lane;
+      const int32_t v = i < cnt ? loc[i] : -1;
+      long long s0 = 0, d0 = 0, s1 = 0, d1 = 0;
+      if (v >= 0) {
+        rec_load<NC>(a, v, s0, d0, s1, d1);
+        ty.vtx += NC;
+        ty.list++;
+      }
+      const long long d = d0 + d1;
+      const bool heavy = v >= 0 && d > kLocalDegree;
+      list_append(heavy, v, sk.out.arr + sk.out.base, sk.out.counter, sk.out.cap - sk.out.base, c,
+                  304);
+      const long long mine = (v >= 0 && !heavy) ? d : 0;
+      const int32_t sv = mine ? vis.source(v) : 0;
+      long long tot;
+      const long long ex = warp_excl64(mine, tot);
+      for (long long eb = 0; eb < tot; eb += 32 * kEU) {
+        int32_t svq[kEU], w[kEU];
+        int k[kEU];
+        bool act[kEU];
+#pragma unroll
+        for (int q = 0; q < kEU; ++q) {
+          const long long e = eb + q * 32 + lane;
+          act[q] = e < tot;
+          int j = 0;
+#pragma unroll
+          for (int stp = 16; stp; stp >>= 1) {
+            const int cnd = j + stp;
+            const long long exc = shfl64(ex, cnd);
+            if (exc <= e) j = cnd;
+          }
+          const long long ej = shfl64(ex, j);
+          svq[q] = __shfl_sync(kFull, sv, j);
+          const long long s0j = shfl64(s0, j), d0j = shfl64(d0, j), s1j = shfl64(s1, j);
+          w[q] = 0;
+          k[q] = 0;
+          if (act[q]) {
+            w[q] = adj_at<NC>(a, s0j, d0j, s1j, e - ej, k[q]);
+            ty.edges++;
+          }
+        }
+        visit_edges(vis, svq, w, k, act, st, sk, c);
+      }
+    }
+  }
+}
 
 // ------------------------------------------------------------------------
 // Frontier expansion (push).  Three tiers by degree:
@@ -599,6 +668,7 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
     }
   }
   if (small) {
+    if constexpr (V::kLocal) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
     stage_flush(st, sk.out, c);
     return;
   }
@@ -691,6 +761,7 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
       visit_edges(vis, svq, w, k, act, st, sk, c);
     }
   }
+  if constexpr (V::kLocal) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
   stage_flush(st, sk.out, c);
   __syncthreads();
 }
@@ -702,6 +773,7 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
 template <int NC>
 struct ReachVisit {
   static constexpr bool kWeighted = true;
+  static constexpr bool kLocal = false;
   const uint32_t* allow;
   uint32_t* vis;
   Adj push;
@@ -727,14 +799,15 @@ struct ReachVisit {
 // Colour push: colour[w] = min(colour[w], colour[v]) over valid w.  The
 // reference pushes the maximum (scc_color.cpp:89-113, cc_color.cpp:103-127);
 // pushing the minimum is the same algorithm mirrored, and its roots are the
-// smallest ids of their SCCs, so the labels come out canonical.  A vertex
-// whose colour fell is queued once per step (iteration stamp).
+// smallest ids of their SCCs, so the labels come out canonical.  Every
+// lowering that succeeds hands w on (to the lowering warp's local rounds or
+// to the next step), so a vertex lowered twice in a step is pushed twice,
+// each time with its colour at that moment.
 struct ColourVisit {
   static constexpr bool kWeighted = false;
+  static constexpr bool kLocal = true;
   const uint32_t* valid;
   int32_t* colour;
-  int32_t* stamp;
-  int32_t iter;
   __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
   __device__ __forceinline__ void edges(const int32_t (&cv)[kEU], const int32_t (&w)[kEU],
                                         const int (&)[kEU], const bool (&act)[kEU],
@@ -750,12 +823,7 @@ struct ColourVisit {
 #pragma unroll
     for (int q = 0; q < kEU; ++q) m[q] = p[q] ? atomicMin(colour + w[q], cv[q]) : cv[q];
 #pragma unroll
-    for (int q = 0; q < kEU; ++q) p[q] = p[q] && m[q] > cv[q];
-    int32_t x[kEU];
-#pragma unroll
-    for (int q = 0; q < kEU; ++q) x[q] = p[q] ? atomicExch(stamp + w[q], iter) : iter;
-#pragma unroll
-    for (int q = 0; q < kEU; ++q) out[q] = p[q] && x[q] != iter;
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && m[q] > cv[q];
   }
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
 };
@@ -765,6 +833,7 @@ struct ColourVisit {
 // root's SCC and is labelled with the colour.
 struct MarkVisit {
   static constexpr bool kWeighted = false;
+  static constexpr bool kLocal = true;
   const uint32_t* valid;
   uint32_t* done;
   const int32_t* colour;
@@ -796,6 +865,7 @@ struct MarkVisit {
 // with itself (scc_trim_complete, scc_trim.cpp:205-263).
 struct TrimVisit {
   static constexpr bool kWeighted = false;
+  static constexpr bool kLocal = false;
   uint32_t* valid;
   int32_t* live_in;
   int32_t* live_out;
@@ -1961,15 +2031,6 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   const Adj back = adj1(g.in);
   int32_t* L = w.listA;
   int32_t* L2 = w.listB;
-  // Propagation steps are numbered on from the previous run's last number
-  // (stamp values only ever hold numbers already used), so the stamps need
-  // no clearing per run; when the numbers run high the stamps are renewed.
-  int32_t iter = __ldcg(w.iter_next);
-  if (iter > (1 << 30)) {
-    for (long long v = gt; v < w.n; v += gstride) w.stamp[v] = -1;
-    if (!step_sync(c, st, 39)) return;
-    iter = 0;
-  }
   int rounds = 0;
   long long labelled = 0;
   int32_t* bufs[2] = {w.x0, w.x1};
@@ -1992,7 +2053,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
       for (;;) {
         if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 32); return; }
         trace_rec(c, nfront, 9);
-        const ColourVisit cv{w.vbits, w.colour, w.stamp, iter++};
+        const ColourVisit cv{w.vbits, w.colour};
         const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, nullptr,
                                   hl[hs ^ 1], w.n, 301);
         expand<NC>(front, nfront, hl[hs], nheavy, prop, cv, sk, tn, sm, c, ty);
@@ -2080,7 +2141,6 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   if (b == 0 && t == 0) {
     c->ncolour_rounds = rounds;
     c->ncolour = (int32_t)labelled;
-    *w.iter_next = iter;
   }
   trace_rec(c, 0, 15);
   tally_flush(ty, c, kKColour, A.p.count_unassigned != 0, sm.red_u);

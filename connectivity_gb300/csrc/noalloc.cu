@@ -41,7 +41,7 @@ constexpr size_t kWords = (size_t)(kNoAllocMaxVertices + 32) / 32 + 2;
 constexpr size_t kBm = al256(kWords * 4);
 constexpr size_t kCtl = al256(sizeof(gb::Ctl));
 constexpr size_t kScratchBytes =
-    kCtl + 16 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8) + 256;
+    kCtl + 15 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8);
 
 // The scratch.  Host code must not pass this name to a kernel: on the host
 // it is a stand-in symbol, not a device address; its device address comes
@@ -117,7 +117,6 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.label = labels;  // the caller's output array
   take(kArr);        // (the workspace label slot stays unused here)
   w.colour = (int32_t*)take(kArr);
-  w.stamp = (int32_t*)take(kArr);
   w.live_in = (int32_t*)take(kArr);
   w.live_out = (int32_t*)take(kArr);
   w.listA = (int32_t*)take(kArr);
@@ -137,7 +136,6 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.done = (uint32_t*)take(kBm);
   w.blk_i = (int32_t*)take(al256(2 * kNoAllocMaxGrid * 4));
   w.blk_l = (long long*)take(al256(kNoAllocMaxGrid * 8));
-  w.iter_next = (int32_t*)take(256);
   w.ctl = ctl;
   w.n = n;
   w.nwords = (n + 31) / 32;
@@ -148,9 +146,7 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(gb::Ctl), s)) != cudaSuccess ||
       (e = cudaMemsetAsync(w.fvis, 0, (size_t)w.nwords * 4, s)) != cudaSuccess ||
       (e = cudaMemsetAsync(w.bvis, 0, (size_t)w.nwords * 4, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(w.done, 0, (size_t)w.nwords * 4, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(w.stamp, 0xff, (size_t)n * 4, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(w.iter_next, 0, sizeof(int32_t), s)) != cudaSuccess) {
+      (e = cudaMemsetAsync(w.done, 0, (size_t)w.nwords * 4, s)) != cudaSuccess) {
     gb_set_error("gb_scc_noalloc: %s", cudaGetErrorString(e));
     return GB_ERR_CUDA;
   }
