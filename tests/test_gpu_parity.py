@@ -93,7 +93,18 @@ def test_grid_scc(ctx, side, variant):
     assert np.array_equal(lab, want)
 
 
-@pytest.mark.parametrize("side", [64, 256])
+@pytest.mark.parametrize("trim", [1, 2])
+def test_grid_1024_scc(ctx, trim):
+    """The high-diameter lattice with chains at 1024^2 (1.15 M vertices): the
+    colour rounds with local continuation against the oracle."""
+    n, s, d = graphs.grid(1024)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab, st = ctx.scc(g, o=gb.opts(trim_level=trim), stats=True)
+    assert st.colour_rounds > 10  # the colour phase does the work here
+    assert np.array_equal(lab, _scc_want(n, s, d))
+
+
+@pytest.mark.parametrize("side", [64, 256, 1024])
 def test_grid_wcc(ctx, side):
     n, s, d = graphs.grid(side)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -235,3 +246,42 @@ def test_rmat_s20_scc_and_wcc(ctx):
     g = gb.Graph.from_edges(ctx, n, s, d)
     assert np.array_equal(ctx.scc(g), _scc_want(n, s, d))
     assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+
+
+def _hub_graph(core=300, up=4000, down=3000, seed=12):
+    """A hub pivot (vertex 0: >= 64 in- and out-edges inside a core SCC) with a
+    large region upstream (reaches the core only) and one downstream (reached
+    only), both made of 2-cycles so that trim keeps them: the forward and
+    backward sets differ a lot and the component is their intersection."""
+    r = np.random.default_rng(seed)
+    e = []
+    c = np.arange(core)
+    e += list(zip(c, np.roll(c, -1)))                       # a cycle through the core
+    e += [(0, int(x)) for x in r.choice(np.arange(1, core), 80, replace=False)]
+    e += [(int(x), 0) for x in r.choice(np.arange(1, core), 80, replace=False)]
+    base = core
+    for i in range(up // 2):                                 # upstream 2-cycles -> core
+        a, b = base + 2 * i, base + 2 * i + 1
+        e += [(a, b), (b, a), (b, int(r.integers(0, core)))]
+    base += up
+    for i in range(down // 2):                               # core -> downstream 2-cycles
+        a, b = base + 2 * i, base + 2 * i + 1
+        e += [(a, b), (b, a), (int(r.integers(0, core)), a)]
+    n = base + down
+    perm = r.permutation(n).astype(np.int32)                 # hide the structure in the ids
+    perm[perm == 0], perm[0] = perm[0], 0                    # keep the hub's id 0
+    s = perm[np.array([x for x, _ in e], np.int64)].astype(np.int32)
+    d = perm[np.array([y for _, y in e], np.int64)].astype(np.int32)
+    return n, s, d
+
+
+def test_searches_together_from_hub_pivot(ctx):
+    n, s, d = _hub_graph()
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    piv, _ = ctx.pivot(g, 0)
+    lab, st = ctx.scc(g, stats=True)
+    assert np.array_equal(lab, _scc_want(n, s, d))
+    # the pivot is a hub, so the two searches ran together: the forward set
+    # holds the core and the downstream region, the component the core only
+    assert st.n_fwbw == 300 and st.n_visit_fw == 300 + 3000
+    assert np.array_equal(ctx.scc(g, o=gb.opts(trim_level=2)), lab)
