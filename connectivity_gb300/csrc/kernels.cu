@@ -668,7 +668,9 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
     }
   }
   if (small) {
-    if constexpr (V::kLocal) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
+    if constexpr (V::kLocal) {
+      if (vis.local()) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
+    }
     stage_flush(st, sk.out, c);
     return;
   }
@@ -761,7 +763,9 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
       visit_edges(vis, svq, w, k, act, st, sk, c);
     }
   }
-  if constexpr (V::kLocal) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
+  if constexpr (V::kLocal) {
+    if (vis.local()) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
+  }
   stage_flush(st, sk.out, c);
   __syncthreads();
 }
@@ -773,10 +777,12 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
 template <int NC>
 struct ReachVisit {
   static constexpr bool kWeighted = true;
-  static constexpr bool kLocal = false;
+  static constexpr bool kLocal = true;
   const uint32_t* allow;
   uint32_t* vis;
   Adj push;
+  bool local_ok;  // this search may expand its claims in local rounds
+  __device__ __forceinline__ bool local() const { return local_ok; }
   __device__ __forceinline__ int32_t source(int32_t) const { return 0; }
   __device__ __forceinline__ void edges(const int32_t (&)[kEU], const int32_t (&w)[kEU],
                                         const int (&)[kEU], const bool (&act)[kEU],
@@ -808,6 +814,7 @@ struct ColourVisit {
   static constexpr bool kLocal = true;
   const uint32_t* valid;
   int32_t* colour;
+  __device__ __forceinline__ bool local() const { return true; }
   __device__ __forceinline__ int32_t source(int32_t v) const { return __ldcg(colour + v); }
   __device__ __forceinline__ void edges(const int32_t (&cv)[kEU], const int32_t (&w)[kEU],
                                         const int (&)[kEU], const bool (&act)[kEU],
@@ -834,6 +841,7 @@ struct ColourVisit {
 struct MarkVisit {
   static constexpr bool kWeighted = false;
   static constexpr bool kLocal = true;
+  __device__ __forceinline__ bool local() const { return true; }
   const uint32_t* valid;
   uint32_t* done;
   const int32_t* colour;
@@ -1330,6 +1338,8 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
 // id.  Returns -1 on error.
 // ------------------------------------------------------------------------
 struct ReachSpec {
+  bool local;             // push steps may run local rounds (its visit list is not
+                          // read afterwards, and its graph is sparse)
   Adj push, pull;
   const uint32_t* allow;
   uint32_t* vis;
@@ -1635,6 +1645,9 @@ __device__ void pull_tail(const ReachSpec& R, const Args& A, Work& w, Smem& sm, 
 // Pivot degree (smaller of in and out) from which the two searches of an
 // SCC run in the same steps.
 constexpr long long kTogetherDegree = 64;
+// Average push degree of the valid vertices up to which searches run local
+// rounds in their push steps.
+constexpr double kLocalAvgDegree = 8.0;
 
 // One search (one direction of one traversal): its spec, the lists it owns,
 // and its running state.
@@ -1776,7 +1789,7 @@ __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const
       if (!q.active) continue;
       Slot* o = step_out(c, st.s, q.dir);
       if (!q.pull) {
-        const ReachVisit<NC> rv{q.R.allow, q.R.vis, q.R.push};
+        const ReachVisit<NC> rv{q.R.allow, q.R.vis, q.R.push, q.R.local};
         const Sink sk = sink_make(q.R.q, q.qhi, w.n, o, true, q.R.minv, q.heavy[q.hsel ^ 1], w.n,
                                   201);
         expand<NC>(q.R.q + q.qlo, (int32_t)(q.qhi - q.qlo), q.heavy[q.hsel], q.huge, q.R.push, rv,
@@ -1858,6 +1871,24 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   F.q = w.q;
   F.minv = batch ? nullptr : &c->minv[0];
   F.stat_slot = kStFwSteps;
+  // SCC of one graph from a hub pivot: both searches run in the same steps,
+  // the backward one over the whole valid set, and the component is what
+  // both reach.  Otherwise (a low-degree pivot, where the backward set can
+  // be far larger than the forward one; batches) the backward search runs
+  // after the forward one, inside the forward set, as the reference does.
+  bool together = false;
+  if constexpr (NC == 1) {
+    if (scc && !batch) {
+      const long long dout = g.out.off[pivot + 1] - g.out.off[pivot];
+      const long long din = g.in.off[pivot + 1] - g.in.off[pivot];
+      together = (dout < din ? dout : din) >= kTogetherDegree;
+    }
+  }
+  // Local rounds in push steps: on sparse graphs, and only for a search
+  // whose visit list is not read afterwards (the forward list of a
+  // sequential SCC is the backward search's candidate list).
+  const bool sparse = (double)F.m_cand <= kLocalAvgDegree * (double)nvalid;
+  F.local = sparse && (!scc || together);
   // the search states live in shared memory (one copy per block, written
   // by thread 0), not in every thread's local memory
   __shared__ Search srch[2];
@@ -1891,18 +1922,8 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   B.nroots = nroots;
   B.q = w.x0;
   B.stat_slot = kStBwSteps;
-  // SCC of one graph from a hub pivot: both searches run in the same steps,
-  // the backward one over the whole valid set, and the component is what
-  // both reach.  Otherwise (a low-degree pivot, where the backward set can
-  // be far larger than the forward one; batches) the backward search runs
-  // after the forward one, inside the forward set, as the reference does.
-  bool together = false;
+  B.local = sparse;
   if constexpr (NC == 1) {
-    if (scc && !batch) {
-      const long long dout = g.out.off[pivot + 1] - g.out.off[pivot];
-      const long long din = g.in.off[pivot + 1] - g.in.off[pivot];
-      together = (dout < din ? dout : din) >= kTogetherDegree;
-    }
     if (together) {
       B.allow = w.vbits;
       B.vis = w.bvis;
@@ -1912,26 +1933,27 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
       if (t == 0) SB.R = B;
       __syncthreads();
       if (!reach_multi<NC>(srch, 2, sflags, A, w, sm, st, ty)) return;
-      if (b == 0 && t == 0) c->nvisit_fw = (int32_t)SF.qhi;
-      // the component is what both searches reached: its smallest member
-      // and its size, while the backward bitmap becomes the intersection
+      // the component is what both searches reached: its smallest member,
+      // while the backward bitmap becomes the intersection (the forward
+      // count comes from the bitmap: local rounds leave no visit list)
       int32_t mn = 0x7fffffff;
-      int cnt = 0;
+      int nfw = 0;
       for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
         const uint32_t bw = __ldcg(w.bvis + wd);
-        const uint32_t x = __ldcg(w.fvis + wd) & bw;
+        const uint32_t fw = __ldcg(w.fvis + wd);
+        const uint32_t x = fw & bw;
         if (x != bw) w.bvis[wd] = x;
+        nfw += __popc(fw);
         if (x) {
           const int32_t v0 = (int32_t)(wd * 32 + __ffs(x) - 1);
           mn = v0 < mn ? v0 : mn;
-          cnt += __popc(x);
         }
       }
       mn = warp_min(mn);
-      for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+      for (int o = 16; o; o >>= 1) nfw += __shfl_xor_sync(kFull, nfw, o);
       if (lane_id() == 0) {
         if (mn != 0x7fffffff) atomicMin(&c->minv[1], mn);
-        if (cnt) atomicAdd(&c->nscc_fwbw, cnt);
+        if (nfw) atomicAdd(&c->nvisit_fw, nfw);
       }
       if (!step_sync(c, st, 28)) return;
       hit = w.bvis;
@@ -1941,9 +1963,9 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   if (!together) {
     __syncthreads();
     if (!reach_multi<NC>(&SF, 1, sflags, A, w, sm, st, ty)) return;
-    const int32_t nf = (int32_t)SF.qhi;
-    if (b == 0 && t == 0) c->nvisit_fw = nf;
+    const int32_t nf = (int32_t)SF.qhi;  // the whole forward set: no local rounds
     if (scc) {
+      if (b == 0 && t == 0) c->nvisit_fw = nf;
       // backward inside the forward set; its candidates are the forward set
       B.allow = w.fvis;
       B.vis = w.bvis;
@@ -1953,11 +1975,9 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
       if (t == 0) SB.R = B;
       __syncthreads();
       if (!reach_multi<1>(&SB, 1, sflags, A, w, sm, st, ty)) return;
-      if (b == 0 && t == 0) c->nscc_fwbw = (int32_t)SB.qhi;
       hit = w.bvis;
       hit_min = &c->minv[1];
     } else {
-      if (b == 0 && t == 0) c->nscc_fwbw = nf;
       hit = w.fvis;
       hit_min = &c->minv[0];
     }
@@ -1983,9 +2003,19 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   const int32_t lab = A.p.canonical ? (batch ? -1 : __ldcg(hit_min)) : pivot;
   // take the component out of the valid set (update_valid,
   // scc_fwbw.cpp:425-433) and label it while the valid list is compacted
+  // (the component's size is counted here from its bitmap)
+  int nhit = 0;
   for (long long wd = (long long)b * T + t; wd < w.nwords; wd += (long long)G * T) {
     const uint32_t h = __ldcg(hit + wd);
-    if (h) w.vbits[wd] = __ldcg(w.vbits + wd) & ~h;
+    if (h) {
+      w.vbits[wd] = __ldcg(w.vbits + wd) & ~h;
+      nhit += __popc(h);
+    }
+  }
+  for (int o = 16; o; o >>= 1) nhit += __shfl_xor_sync(kFull, nhit, o);
+  if (lane_id() == 0 && nhit) {
+    atomicAdd(&c->nscc_fwbw, nhit);
+    if (!scc) atomicAdd(&c->nvisit_fw, nhit);
   }
   const bool canon = A.p.canonical != 0;
   auto put = [&](int32_t v) {
