@@ -99,7 +99,8 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
   gb_opts d;
   gb_opts_default(&d);
   if (!o) o = &d;
-  p.trim_level = o->trim_level >= 2 ? 2 : 1;
+  p.trim_level = o->trim_level >= 2 ? 2 : (o->trim_level <= 0 ? 0 : 1);
+  p.trim_pairs = o->trim_pairs ? 1 : 0;
   p.canonical = o->canonical ? 1 : 0;
   p.pivot_hint = o->pivot;
   p.tune.t_block = o->t_block > 32 ? o->t_block : 32;
@@ -365,6 +366,7 @@ void gb_opts_default(gb_opts* o) {
   o->beta = 25.0f;
   o->max_steps = 1 << 30;
   o->grid_blocks = 0;
+  o->trim_pairs = 0;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {

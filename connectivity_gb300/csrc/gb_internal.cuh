@@ -180,7 +180,8 @@ struct GraphView {
 enum RunKind : int { kSCC = 0, kWCC = 1 };
 
 struct RunParams {
-  int32_t trim_level;     // 1: one pass, 2: fixed point
+  int32_t trim_level;     // 0: none, 1: one pass, 2: fixed point
+  int32_t trim_pairs;     // 1: size-2 components leave with the trim
   int32_t canonical;      // 1: relabel with the minimum member id
   int32_t pivot_hint;     // >= 0: use as FW-BW source if still valid
   int32_t count_unassigned;  // 1: a final pass counts labels outside [0, n)

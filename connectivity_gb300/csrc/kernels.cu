@@ -969,7 +969,8 @@ __device__ bool compact_ordered(const int32_t* in, int32_t nin, int32_t* out, co
   block_excl(pre, boff, sm.warp_tmp);
   if (b == G - 1 && t == 0) *total = boff + tot;
   int run = boff + woff;
-  for (long long base = wlo; base < whi; base += kCG) {
+  // (a warp whose range keeps nothing has nothing to write)
+  for (long long base = wlo; cnt > 0 && base < whi; base += kCG) {
     int32_t v[kCU];
 #pragma unroll
     for (int j = 0; j < kCU; ++j) {
@@ -1003,6 +1004,44 @@ __device__ __forceinline__ bool better(unsigned long long k2, int32_t v2, unsign
   return k2 > k || (k2 == k && v2 >= 0 && (v < 0 || v2 < v));
 }
 
+// Ordered valid list: a warp's group of words with at least this many valid
+// ids is written word by word by the whole warp; sparser groups go through
+// the warp's staging buffer (which holds kWarpSmem >= this ids).
+constexpr int kTrimDenseIds = 256;
+static_assert(kTrimDenseIds <= kWarpSmem, "sparse groups fit the staging buffer");
+
+// Size-2 components (an extension of the trim): u and p form a component
+// when each is the other's only valid in-neighbour, or each the other's only
+// valid out-neighbour (self-loops ignored).  Then nothing outside the pair
+// reaches it (or is reached from it), and u and p reach each other.  Edges
+// to vertices outside the valid set, and to vertices that other pairs
+// remove during the same pass, come from or lead to whole components of
+// their own, so they change no verdict.  Only vertices of degree at most
+// kPairDeg in the tested direction are examined.
+constexpr long long kPairDeg = 16;
+__device__ __forceinline__ int32_t sole_valid_nbr(const Csr& cs, const uint32_t* valid, int32_t u) {
+  const long long s = __ldg(cs.off + u), e = __ldg(cs.off + u + 1);
+  if (e - s > kPairDeg) return -1;
+  int32_t p = -1;
+  for (long long i = s; i < e; ++i) {
+    const int32_t x = __ldg(cs.adj + i);
+    if (x == u || !bit_get(valid, x)) continue;
+    if (p < 0) p = x;
+    else if (x != p) return -1;
+  }
+  return p;
+}
+// The partner of u in a size-2 component when it has the larger id (the
+// smaller member removes the pair), else -1.
+__device__ __forceinline__ int32_t pair_partner(const GraphView& g, const uint32_t* valid,
+                                                int32_t u) {
+  int32_t p = sole_valid_nbr(g.in, valid, u);
+  if (p > u && sole_valid_nbr(g.in, valid, p) == u) return p;
+  p = sole_valid_nbr(g.out, valid, u);
+  if (p > u && sole_valid_nbr(g.out, valid, p) == u) return p;
+  return -1;
+}
+
 __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -1010,7 +1049,9 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
   const bool scc = A.kind == kSCC;
+  const bool level0 = scc && A.p.trim_level <= 0;
   const bool level2 = scc && A.p.trim_level >= 2;
+  const bool pairs = scc && A.p.trim_pairs != 0;
   Tally ty;
   if (ld_vol(&c->err)) return;
   Steps st = steps_open(c);
@@ -1043,7 +1084,8 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   // issue all their offset loads before using any.  Each warp counts the
   // valid vertices it saw.
   constexpr int kTrimU = 4;
-  const long long bchunk = ((long long)w.nwords + G - 1) / G;
+  // (a multiple of 4 words, so the list pass can read 16-byte groups)
+  const long long bchunk = (((long long)w.nwords + G - 1) / G + 3) & ~3ll;
   const long long wlo = bchunk * b < w.nwords ? bchunk * b : w.nwords;
   const long long whi = wlo + bchunk < w.nwords ? wlo + bchunk : w.nwords;
   int wvalid = 0;  // warp-uniform
@@ -1088,7 +1130,7 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
         const long long din = i1[j] - i0[j];
         ty.vtx += g.in.off != nullptr ? 2 : 1;
         if (scc) {
-          keep = dout > 0 && din > 0;
+          keep = level0 || (dout > 0 && din > 0);
           if (keep) {
             const unsigned long long prod = (unsigned long long)dout * (unsigned long long)din;
             if (prod > best_key) { best_key = prod; best_v = v; }
@@ -1153,7 +1195,7 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
     __syncthreads();
     btot = sm.warp_tmp[kWarps];
   };
-  if (!level2) block_total();
+  if (!level2 && !pairs) block_total();
   // block reduction of the pivot candidates
   {
     unsigned long long k = best_key;
@@ -1204,8 +1246,7 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
     if (lane == 0) c->pivot = bk > 0ull ? bv : -1;
   }
 
-  // Level 2: propagate removals to the fixed point, then count the warp's
-  // share of the block's range again.
+  // Level 2: propagate removals to the fixed point.
   if (level2) {
     const Adj both = adj2(g.out, g.in);
     int32_t* bufs[2] = {w.x0, w.x1};
@@ -1221,6 +1262,27 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
       if (!step_sync(c, st, 3)) return;
       cur ^= 1;
     }
+  }
+  // Size-2 components: warp k of the block takes the block's words k, k+32,
+  // ...; each lane tests the vertex of its bit.
+  if (pairs) {
+    for (long long wd = wlo + warp; wd < whi; wd += (T >> 5)) {
+      const uint32_t x = __ldcg(w.vbits + wd);  // one load: the same word in every lane
+      if (x == 0u) continue;
+      if ((x >> lane) & 1u) {
+        const int32_t u = (int32_t)(wd * 32 + lane);
+        const int32_t p = pair_partner(g, w.vbits, u);
+        if (p >= 0 && bit_release(w.vbits, u)) {
+          bit_release(w.vbits, p);
+          w.label[u] = u;
+          w.label[p] = u;
+        }
+      }
+    }
+    if (!step_sync(c, st, 7)) return;
+  }
+  // count the warp's share of the block's range again
+  if (level2 || pairs) {
     wvalid = 0;
     for (long long wd0 = wlo + warp * 32; wd0 < whi; wd0 += (long long)T) {
       const long long wd = wd0 + lane;
@@ -1233,25 +1295,49 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   }
   trace_rec(c, 0, 18);
 
-  // Ordered valid list: per iteration warp k of the block takes the k-th
-  // group of 32 words; the warps' counts are scanned in shared memory and
-  // each warp writes the ids of its words with coalesced stores.
+  // Ordered valid list: per iteration each thread takes kListW consecutive
+  // words (warp k of the block the k-th group of 32 x kListW); the warps'
+  // counts are scanned in shared memory and each warp writes the ids of its
+  // words.  The words are loaded before the block's offset is known.
   {
+    constexpr int kListW = 4;
+    const long long span = (long long)T * kListW;
+    unsigned x[kListW];
+    auto load_words = [&](long long base) {
+      const long long wq = base + (long long)t * kListW;
+      if (wq + kListW <= whi && (reinterpret_cast<uintptr_t>(w.vbits + wq) & 15u) == 0u) {
+        const uint4 q4 = __ldcg(reinterpret_cast<const uint4*>(w.vbits + wq));
+        x[0] = q4.x;
+        x[1] = q4.y;
+        x[2] = q4.z;
+        x[3] = q4.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < kListW; ++j) x[j] = wq + j < whi ? __ldcg(w.vbits + wq + j) : 0u;
+      }
+    };
+    if (wlo < whi) load_words(wlo);
     int pre = 0;
     for (int j = t; j < b; j += T) pre += __ldcg(w.blk_i + j);
     int boff;
     block_excl(pre, boff, sm.warp_tmp);
     if (b == G - 1 && t == 0) {
       c->nvalid = boff + btot;
-      if (level2) c->ntrim = g.n - (boff + btot);
+      if (level2 || pairs) c->ntrim = g.n - (boff + btot);
     }
     long long run = boff;
-    for (long long base = wlo; base < whi; base += (long long)T) {
-      const long long wd0 = base + warp * 32;
-      const long long wd = wd0 + lane;
-      const unsigned x = wd < whi ? __ldcg(w.vbits + wd) : 0u;
+    for (long long base = wlo; base < whi; base += span) {
+      if (base != wlo) load_words(base);
+      const long long wq = base + (long long)t * kListW;
+      int cs[kListW];
+      int sum = 0;
+#pragma unroll
+      for (int j = 0; j < kListW; ++j) {
+        cs[j] = sum;
+        sum += __popc(x[j]);
+      }
       int tot;
-      const int ex = warp_excl(__popc(x), tot);
+      const int ex = warp_excl(sum, tot);
       if (lane == 0) sm.warp_tmp[warp] = tot;
       __syncthreads();
       if (warp == 0) {
@@ -1268,31 +1354,45 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
       __syncthreads();
       const long long o = run + sm.warp_tmp[warp];
       run += sm.warp_tmp[kWarps];
-      // each lane puts its word's ids at their ranks in the warp's staging
-      // buffer (visiting its bits from bit `lane` on, so that the lanes of
-      // dense words hit different banks), then the warp copies the buffer out
-      // (the warp's shared memory holds kWarpSmem ids: denser groups go in
-      // two halves of 16 words)
-      int32_t* buf = sm.stage(warp, 0);
-      const bool split = tot > kWarpSmem;
-      const int half = split ? __shfl_sync(kFull, ex, 16) : tot;  // ids of the first pass
-      for (int hh = 0; hh < (split ? 2 : 1); ++hh) {
-        const int r0 = hh ? half : 0;
-        const int cnt = hh ? tot - half : half;
-        if (!split || (lane >> 4) == hh) {
-          unsigned y = (x >> lane) | (lane ? x << (32 - lane) : 0u);
+      if (tot >= kTrimDenseIds) {
+        // dense group: the warp writes its words one at a time, a lane per
+        // bit, so every store is a contiguous run of ids
+        const long long v0 = (base + (long long)warp * 32 * kListW) * 32;
+#pragma unroll
+        for (int j = 0; j < kListW; ++j) {
+          unsigned nz = __ballot_sync(kFull, x[j] != 0u);
+          while (nz) {
+            const int k = __ffs(nz) - 1;
+            nz &= nz - 1;
+            const unsigned xk = __shfl_sync(kFull, x[j], k);
+            const int ek = __shfl_sync(kFull, ex + cs[j], k);
+            if ((xk >> lane) & 1u)
+              w.listA[o + ek + __popc(xk & ((1u << lane) - 1u))] =
+                  (int32_t)(v0 + (long long)(k * kListW + j) * 32 + lane);
+          }
+        }
+      } else {
+        // sparse group: each lane puts its words' ids at their ranks in the
+        // warp's staging buffer (visiting each word's bits from bit `lane`
+        // on, so that the lanes of dense words hit different banks), then
+        // the warp copies the buffer out
+        int32_t* buf = sm.stage(warp, 0);
+#pragma unroll
+        for (int j = 0; j < kListW; ++j) {
+          const unsigned xj = x[j];
+          unsigned y = (xj >> lane) | (lane ? xj << (32 - lane) : 0u);
           while (y) {
             const int p = __ffs(y) - 1;
             y &= y - 1;
             const int bit = (p + lane) & 31;
-            buf[ex - r0 + __popc(x & ((1u << bit) - 1u))] = (int32_t)(wd * 32 + bit);
+            buf[ex + cs[j] + __popc(xj & ((1u << bit) - 1u))] = (int32_t)((wq + j) * 32 + bit);
           }
         }
         __syncwarp();
-        for (int k = lane; k < cnt; k += 32) w.listA[o + r0 + k] = buf[k];
+        for (int k = lane; k < tot; k += 32) w.listA[o + k] = buf[k];
         __syncwarp();
       }
-      ty.list += __popc(x);
+      ty.list += sum;
       __syncthreads();
     }
   }

@@ -60,10 +60,12 @@ typedef struct gb_graph gb_graph; /* device-resident out- and in-CSR */
 
 /* Run options.  gb_opts_default fills the defaults noted per field. */
 typedef struct gb_opts {
-  int32_t trim_level;  /* 1: one pass (reference default, TRIM_LEVEL 1 at
-                          multistep/scc_main.cpp:61, scc_trim.cpp:89-139);
-                          2: iterate to the fixed point (scc_trim_complete,
-                          scc_trim.cpp:141-297).  Default 1. SCC only. */
+  int32_t trim_level;  /* 0: no trim (TRIM_LEVEL 0, multistep/scc_main.cpp:
+                          241-246); 1: one pass (reference default,
+                          TRIM_LEVEL 1 at scc_main.cpp:61, scc_trim.cpp:
+                          89-139); 2: iterate to the fixed point
+                          (scc_trim_complete, scc_trim.cpp:141-297).
+                          Default 1. SCC only. */
   int32_t canonical;   /* 1: minimum-member labels (default); 0: labels as
                           the phases produce them */
   int32_t pivot;       /* -1 (default): the reference rule, lowest id of
@@ -81,6 +83,11 @@ typedef struct gb_opts {
                           (25, the reference's BETA scc_main.cpp:65) */
   int32_t max_steps;   /* cap on device steps per phase (1 << 30) */
   int32_t grid_blocks; /* 0: all resident blocks; else a smaller grid */
+  int32_t trim_pairs;  /* 1: after the trim, remove size-2 SCCs (two vertices
+                          that are each other's only in-neighbour, or only
+                          out-neighbour, among the valid vertices), labelled
+                          with the smaller id.  No reference counterpart;
+                          default 0.  SCC only. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);

@@ -133,6 +133,19 @@ int32_t orc_pivot_cc(const orc_graph* g, double* avg_degree) {
 /* ------------------------------------------------------------------ */
 /* Trim.                                                               */
 
+/* No trim (TRIM_LEVEL 0, scc_main.cpp:229-246): every vertex stays valid,
+ * the valid list is 0..n-1 and every label starts at -1. */
+static int64_t trim_none(const orc_graph* g, uint8_t* valid, int32_t* labels,
+                         int32_t* list, int64_t* nlist) {
+  for (int32_t v = 0; v < g->n; ++v) {
+    valid[v] = 1;
+    labels[v] = -1;
+    list[v] = v;
+  }
+  *nlist = g->n;
+  return 0;
+}
+
 /* One pass: in- or out-degree 0 in the original graph -> own component
  * (scc_trim, scc_trim.cpp:89-139).  Survivors go to list. */
 static int64_t trim_once(const orc_graph* g, uint8_t* valid, int32_t* labels,
@@ -454,8 +467,9 @@ static int64_t tarjan_valid(const orc_graph* g, const uint8_t* valid,
 }
 
 /* ------------------------------------------------------------------ */
-/* run_scc (scc_main.cpp:210-317).  trim_level 1 = scc_trim (the
- * reference default, TRIM_LEVEL 1 at :61), 2 = scc_trim_complete. */
+/* run_scc (scc_main.cpp:210-317).  trim_level 0 = no trim, 1 = scc_trim
+ * (the reference default, TRIM_LEVEL 1 at :61), 2 = scc_trim_complete
+ * (the switch at :241-259). */
 int orc_scc(const orc_graph* g, int32_t* labels, int32_t pivot, double avg_degree,
             int32_t vert_cutoff, int32_t trim_level, orc_times* tm) {
   int32_t n = g->n;
@@ -470,8 +484,9 @@ int orc_scc(const orc_graph* g, int32_t* labels, int32_t pivot, double avg_degre
   int64_t nlist = 0;
   if (!valid || !list) return 2;
 
-  tm->num_trim = trim_level >= 2 ? trim_fixed_point(g, valid, labels, list, &nlist)
-                                 : trim_once(g, valid, labels, list, &nlist);
+  tm->num_trim = trim_level <= 0 ? trim_none(g, valid, labels, list, &nlist)
+                 : trim_level >= 2 ? trim_fixed_point(g, valid, labels, list, &nlist)
+                                   : trim_once(g, valid, labels, list, &nlist);
   t1 = now_s(); tm->trim = t1 - t0; t0 = t1;
 
   if (pivot >= 0 && pivot < n && valid[pivot]) {

@@ -16,7 +16,10 @@ CASES = graphs.edge_cases()
 
 VARIANTS = {
     "default": {},
+    "trim0": {"trim_level": 0},
     "trim2": {"trim_level": 2},
+    "pairs": {"trim_pairs": 1},
+    "pairs2": {"trim_level": 2, "trim_pairs": 1},
     # tiny tiers push every vertex through the block and grid-slice paths
     "tiers": {"t_block": 33, "t_grid": 64},
     "pull_early": {"alpha": 1e9, "beta": 1e-3, "k_pull": 1},
@@ -66,7 +69,8 @@ def test_reference_golden_vector(ctx):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "trim2", "tiers", "pull_early", "small_grid"])
+@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "tiers", "pull_early",
+                                     "small_grid"])
 def test_rmat_scc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -84,7 +88,7 @@ def test_rmat_wcc(ctx, scale, ef, variant):
 
 
 @pytest.mark.parametrize("side", [16, 64, 128])
-@pytest.mark.parametrize("variant", ["default", "trim2"])
+@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "pairs2"])
 def test_grid_scc(ctx, side, variant):
     n, s, d = graphs.grid(side)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -285,3 +289,66 @@ def test_searches_together_from_hub_pivot(ctx):
     # holds the core and the downstream region, the component the core only
     assert st.n_fwbw == 300 and st.n_visit_fw == 300 + 3000
     assert np.array_equal(ctx.scc(g, o=gb.opts(trim_level=2)), lab)
+
+
+def _planted_pairs(npairs, nrest, seed):
+    """npairs two-cycles (2i, 2i+1) on top of a random graph over the other
+    nrest vertices: the first half take edges only from their partner (in
+    pattern) and point into the rest, the second half point only to their
+    partner (out pattern) and are pointed to from the rest."""
+    rng = np.random.default_rng(seed)
+    n = 2 * npairs + nrest
+    base = 2 * npairs
+    s, d = [], []
+    for i in range(npairs):
+        u, v = 2 * i, 2 * i + 1
+        s += [u, v]
+        d += [v, u]
+        other = base + rng.integers(0, nrest, 3)
+        if i < npairs // 2:
+            s += [u, v, u]
+            d += other.tolist()
+        else:
+            s += other.tolist()
+            d += [u, v, v]
+    m = 4 * nrest
+    s += (base + rng.integers(0, nrest, m)).tolist()
+    d += (base + rng.integers(0, nrest, m)).tolist()
+    s = np.array(s, np.int32)
+    d = np.array(d, np.int32)
+    keep = s != d
+    e = np.unique(np.stack([s[keep], d[keep]], 1), axis=0)
+    return n, e[:, 0].copy(), e[:, 1].copy()
+
+
+@pytest.mark.parametrize("trim", [1, 2])
+def test_trim_pairs_planted(ctx, trim):
+    """Every planted two-cycle leaves with the trim (the size-2 pass adds at
+    least 2 per pair to the trim count, and no more than the graph's size-2
+    SCCs), and the labels still equal the oracle's."""
+    n, s, d = _planted_pairs(500, 3000, 11)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    want = _scc_want(n, s, d)
+    lab0, st0 = ctx.scc(g, o=gb.opts(trim_level=trim), stats=True)
+    lab1, st1 = ctx.scc(g, o=gb.opts(trim_level=trim, trim_pairs=1), stats=True)
+    assert np.array_equal(lab0, want) and np.array_equal(lab1, want)
+    sizes = np.bincount(want, minlength=n)
+    found = st1.n_trim - st0.n_trim
+    assert 2 * 500 <= found <= 2 * int((sizes == 2).sum())
+    assert found % 2 == 0
+
+
+def test_trim_pairs_only_pairs(ctx):
+    """A graph of nothing but two-cycles: the size-2 pass removes every
+    vertex, the pivot among them, and nothing is left for FW-BW or colour."""
+    npairs = 1000
+    u = np.arange(0, 2 * npairs, 2, dtype=np.int32)
+    s = np.concatenate([u, u + 1])
+    d = np.concatenate([u + 1, u])
+    n = 2 * npairs
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab, st = ctx.scc(g, o=gb.opts(trim_pairs=1), stats=True)
+    assert np.array_equal(lab, np.repeat(u, 2))
+    assert st.n_trim == n and st.n_fwbw == 0 and st.colour_rounds == 0
+    lab0, st0 = ctx.scc(g, o=gb.opts(trim_level=0), stats=True)
+    assert np.array_equal(lab0, lab) and st0.n_trim == 0

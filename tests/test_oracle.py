@@ -59,7 +59,9 @@ def test_oracle_variants_agree(case):
     name, (n, s, d) = case
     g = oracle.CpuGraph(n, s, d)
     base = oracle.scc(g)
-    # fixed-point trim, no serial step, and an independent Tarjan
+    # no trim, fixed-point trim, no serial step, and an independent Tarjan
+    lab0, t0 = oracle.scc(g, trim_level=0, times=True)
+    assert np.array_equal(lab0, base) and t0.num_trim == 0
     assert np.array_equal(oracle.scc(g, trim_level=2), base)
     assert np.array_equal(oracle.scc(g, vert_cutoff=0), base)
     assert np.array_equal(oracle.tarjan(g), base)
