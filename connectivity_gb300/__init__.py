@@ -56,6 +56,7 @@ class Opts(C.Structure):
         ("vert_cutoff", C.c_int32), ("t_block", C.c_int32), ("t_grid", C.c_int32),
         ("k_pull", C.c_int32), ("alpha", C.c_float), ("beta", C.c_float),
         ("max_steps", C.c_int32), ("grid_blocks", C.c_int32), ("trim_pairs", C.c_int32),
+        ("fwbw_rounds", C.c_int32),
     ]
 
 
@@ -71,6 +72,7 @@ class Stats(C.Structure):
         ("bw_steps", C.c_int64), ("pull_steps", C.c_int64), ("colour_steps", C.c_int64),
         ("mark_steps", C.c_int64), ("grid_blocks", C.c_int32), ("err_where", C.c_int32),
         ("m_visit_fw", C.c_int64), ("m_visit_bw", C.c_int64), ("pull_edges", C.c_int64),
+        ("fwbw_rounds", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

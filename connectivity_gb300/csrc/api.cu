@@ -59,7 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(G * 8);
+  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(2 * G * 8);
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -89,7 +89,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.bvis = (uint32_t*)take(bm);
   w.done = (uint32_t*)take(bm);
   w.blk_i = (int32_t*)take(align256(2 * G * 4));
-  w.blk_l = (long long*)take(align256(G * 8));
+  w.blk_l = (long long*)take(align256(2 * G * 8));
   w.ctl = c->d_ctl;
   c->cap_n = n;
   return GB_OK;
@@ -101,6 +101,7 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
   if (!o) o = &d;
   p.trim_level = o->trim_level >= 2 ? 2 : (o->trim_level <= 0 ? 0 : 1);
   p.trim_pairs = o->trim_pairs ? 1 : 0;
+  p.fwbw_rounds = o->fwbw_rounds > 1 ? o->fwbw_rounds : 1;
   p.canonical = o->canonical ? 1 : 0;
   p.pivot_hint = o->pivot;
   p.tune.t_block = o->t_block > 32 ? o->t_block : 32;
@@ -242,6 +243,7 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
     st->m_visit_fw = (int64_t)h.mvis[0];
     st->m_visit_bw = (int64_t)h.mvis[1];
     st->pull_edges = (int64_t)h.pull_edges;
+    st->fwbw_rounds = (h.pivot >= 0 ? 1 : 0) + (int64_t)h.nrounds;
     st->trim_steps = (int64_t)h.stat[gb::kStTrimSteps];
     st->fw_steps = (int64_t)h.stat[gb::kStFwSteps];
     st->bw_steps = (int64_t)h.stat[gb::kStBwSteps];
@@ -367,6 +369,7 @@ void gb_opts_default(gb_opts* o) {
   o->max_steps = 1 << 30;
   o->grid_blocks = 0;
   o->trim_pairs = 0;
+  o->fwbw_rounds = 1;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {

@@ -74,6 +74,8 @@ struct Ctl {
   int32_t unassigned;
   int32_t ncolour;        // vertices labelled by the colour rounds
   int32_t nroots;         // batch: pivots in BatchView::roots
+  int32_t rpivot;         // pivot of the FW-BW round after the first (-1: none)
+  int32_t nrounds;        // FW-BW rounds after the first
   alignas(128) int32_t minv[2];       // smallest vertex reached forward / backward
   // pull steps, per search and per parity of the search's pull steps:
   alignas(128) int32_t lcount[2][2][2];  // warp- and block-tier list lengths
@@ -150,7 +152,7 @@ struct Work {
   int32_t* xb;            // searches run in the same steps
   int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
   unsigned long long* tphase;  // this run's 4 phase-boundary device times, or null
-  long long* blk_l;
+  long long* blk_l;       // per-block scratch (2 x grid size: pivot keys, then edge sums)
   Ctl* ctl;
 };
 
@@ -182,6 +184,7 @@ enum RunKind : int { kSCC = 0, kWCC = 1 };
 struct RunParams {
   int32_t trim_level;     // 0: none, 1: one pass, 2: fixed point
   int32_t trim_pairs;     // 1: size-2 components leave with the trim
+  int32_t fwbw_rounds;    // FW-BW rounds, each from a new pivot (>= 1)
   int32_t canonical;      // 1: relabel with the minimum member id
   int32_t pivot_hint;     // >= 0: use as FW-BW source if still valid
   int32_t count_unassigned;  // 1: a final pass counts labels outside [0, n)
@@ -193,6 +196,12 @@ cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p,
                        const Work& w, int grid, cudaStream_t stream,
                        cudaEvent_t* ev /* 5 events or null */);
 int max_coop_grid(int device);   // cooperative grid size for the run kernels
+// The run with FW-BW rounds after the first (kernels_rounds.cu; launch_run
+// calls it when p.fwbw_rounds > 1 for a single graph), and the blocks per SM
+// of its kernels.
+cudaError_t launch_run_rounds(const GraphView& g, RunKind kind, const RunParams& p,
+                              const Work& w, int grid, cudaStream_t stream);
+int run_rounds_blocks_per_sm();
 
 // CSR construction (csr_build.cu).  build_csr sorts device edge arrays into
 // out- and (if in_off != null) in-CSR; *ids_ok = false if an id is outside

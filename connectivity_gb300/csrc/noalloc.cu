@@ -41,7 +41,7 @@ constexpr size_t kWords = (size_t)(kNoAllocMaxVertices + 32) / 32 + 2;
 constexpr size_t kBm = al256(kWords * 4);
 constexpr size_t kCtl = al256(sizeof(gb::Ctl));
 constexpr size_t kScratchBytes =
-    kCtl + 15 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(kNoAllocMaxGrid * 8);
+    kCtl + 15 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(2 * kNoAllocMaxGrid * 8);
 
 // The scratch.  Host code must not pass this name to a kernel: on the host
 // it is a stand-in symbol, not a device address; its device address comes
@@ -135,7 +135,7 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.bvis = (uint32_t*)take(kBm);
   w.done = (uint32_t*)take(kBm);
   w.blk_i = (int32_t*)take(al256(2 * kNoAllocMaxGrid * 4));
-  w.blk_l = (long long*)take(al256(kNoAllocMaxGrid * 8));
+  w.blk_l = (long long*)take(al256(2 * kNoAllocMaxGrid * 8));
   w.ctl = ctl;
   w.n = n;
   w.nwords = (n + 31) / 32;
@@ -159,6 +159,7 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   gb_opts_default(&o);
   gb::RunParams prm{};
   prm.trim_level = o.trim_level;
+  prm.fwbw_rounds = 1;
   prm.canonical = 1;
   prm.pivot_hint = -1;
   prm.count_unassigned = 0;

@@ -88,6 +88,12 @@ typedef struct gb_opts {
                           out-neighbour, among the valid vertices), labelled
                           with the smaller id.  No reference counterpart;
                           default 0.  SCC only. */
+  int32_t fwbw_rounds; /* FW-BW rounds before the colour rounds, each from a
+                          new pivot chosen by the same rule among the
+                          vertices still valid (1: the reference's single
+                          round, scc_main.cpp:273-276, the default).  A round
+                          is skipped once fewer than 4096 vertices are left.
+                          Ignored by batches. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);
@@ -116,6 +122,7 @@ typedef struct gb_stats {
   /* push-direction edges of the vertices reached forward / backward (the
    * m_visited of a traversal) and adjacency entries scanned by pull steps */
   int64_t m_visit_fw, m_visit_bw, pull_edges;
+  int64_t fwbw_rounds;    /* FW-BW rounds run (0 when there was no pivot) */
 } gb_stats;
 
 /* ---- contexts --------------------------------------------------------- */

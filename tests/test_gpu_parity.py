@@ -20,6 +20,7 @@ VARIANTS = {
     "trim2": {"trim_level": 2},
     "pairs": {"trim_pairs": 1},
     "pairs2": {"trim_level": 2, "trim_pairs": 1},
+    "rounds": {"fwbw_rounds": 4},
     # tiny tiers push every vertex through the block and grid-slice paths
     "tiers": {"t_block": 33, "t_grid": 64},
     "pull_early": {"alpha": 1e9, "beta": 1e-3, "k_pull": 1},
@@ -69,8 +70,8 @@ def test_reference_golden_vector(ctx):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "tiers", "pull_early",
-                                     "small_grid"])
+@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "rounds", "tiers",
+                                     "pull_early", "small_grid"])
 def test_rmat_scc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -80,7 +81,7 @@ def test_rmat_scc(ctx, scale, ef, variant):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (14, 16), (16, 16), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "pull_early"])
+@pytest.mark.parametrize("variant", ["default", "pull_early", "rounds"])
 def test_rmat_wcc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -352,3 +353,44 @@ def test_trim_pairs_only_pairs(ctx):
     assert st.n_trim == n and st.n_fwbw == 0 and st.colour_rounds == 0
     lab0, st0 = ctx.scc(g, o=gb.opts(trim_level=0), stats=True)
     assert np.array_equal(lab0, lab) and st0.n_trim == 0
+
+
+def _disjoint_rmats(k, scale, ef):
+    """k R-MAT graphs with different seeds, side by side (k large SCCs)."""
+    ss, dd, n = [], [], 0
+    for i in range(k):
+        m, s, d = graphs.rmat(scale, ef, seed=10 + i)
+        ss.append(s + n)
+        dd.append(d + n)
+        n += m
+    return n, np.concatenate(ss).astype(np.int32), np.concatenate(dd).astype(np.int32)
+
+
+@pytest.mark.parametrize("kind", ["scc", "wcc"])
+def test_repivot_rounds_take_the_next_components(ctx, kind):
+    """Four disjoint R-MATs: each FW-BW round after the first starts from
+    the next pivot by the reference rule and takes another large component
+    out before the colour rounds; labels stay equal to the oracle's."""
+    n, s, d = _disjoint_rmats(4, 14, 8)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    fn = ctx.scc if kind == "scc" else ctx.wcc
+    want = _scc_want(n, s, d) if kind == "scc" else _wcc_want(n, s, d)
+    lab1, st1 = fn(g, o=gb.opts(fwbw_rounds=1), stats=True)
+    lab4, st4 = fn(g, o=gb.opts(fwbw_rounds=4), stats=True)
+    assert np.array_equal(lab1, want) and np.array_equal(lab4, want)
+    assert st1.fwbw_rounds == 1 and st4.fwbw_rounds == 4
+    sizes = np.sort(np.bincount(want))[::-1]
+    assert st1.n_fwbw in set(sizes[:4].tolist())
+    # each round labels one whole component: four of the largest
+    assert st4.n_fwbw > st1.n_fwbw
+    assert st4.n_fwbw <= sizes[:4].sum()
+
+
+def test_repivot_stops_when_little_is_left(ctx):
+    """Rounds stop once fewer than 4096 vertices are valid (the colour
+    rounds take the rest), whatever the option asks for."""
+    n, s, d = graphs.rmat(10, 16)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab, st = ctx.scc(g, o=gb.opts(fwbw_rounds=50), stats=True)
+    assert np.array_equal(lab, _scc_want(n, s, d))
+    assert st.fwbw_rounds == 1
