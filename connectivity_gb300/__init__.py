@@ -56,7 +56,7 @@ class Opts(C.Structure):
         ("vert_cutoff", C.c_int32), ("t_block", C.c_int32), ("t_grid", C.c_int32),
         ("k_pull", C.c_int32), ("alpha", C.c_float), ("beta", C.c_float),
         ("max_steps", C.c_int32), ("grid_blocks", C.c_int32), ("trim_pairs", C.c_int32),
-        ("fwbw_rounds", C.c_int32),
+        ("fwbw_rounds", C.c_int32), ("expand_mode", C.c_int32),
     ]
 
 

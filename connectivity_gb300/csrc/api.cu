@@ -110,6 +110,7 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
   p.tune.alpha = o->alpha > 0 ? o->alpha : 15.0f;
   p.tune.beta = o->beta > 0 ? o->beta : 25.0f;
   p.tune.max_steps = o->max_steps > 0 ? o->max_steps : (1 << 30);
+  p.tune.expand_mode = o->expand_mode == 1 ? 1 : 0;
 }
 
 }  // namespace
@@ -370,6 +371,7 @@ void gb_opts_default(gb_opts* o) {
   o->grid_blocks = 0;
   o->trim_pairs = 0;
   o->fwbw_rounds = 1;
+  o->expand_mode = 0;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {

@@ -124,6 +124,8 @@ struct Tune {
   float alpha;            // push -> pull when m_f > m_u / alpha
   float beta;             // pull -> push when n_f < n_cand / beta
   int32_t max_steps;      // cap on barrier steps per kernel
+  int32_t expand_mode;    // push steps of the searches: 0 degree tiers,
+                          // 1 global edge balance
 };
 
 // Device workspace of one run (all arrays sized for n vertices).
@@ -196,12 +198,12 @@ cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p,
                        const Work& w, int grid, cudaStream_t stream,
                        cudaEvent_t* ev /* 5 events or null */);
 int max_coop_grid(int device);   // cooperative grid size for the run kernels
-// The run with FW-BW rounds after the first (kernels_rounds.cu; launch_run
-// calls it when p.fwbw_rounds > 1 for a single graph), and the blocks per SM
-// of its kernels.
-cudaError_t launch_run_rounds(const GraphView& g, RunKind kind, const RunParams& p,
-                              const Work& w, int grid, cudaStream_t stream);
-int run_rounds_blocks_per_sm();
+// The run with the optional features compiled in (kernels_options.cu;
+// launch_run calls it for fwbw_rounds > 1 on a single graph or for
+// expand_mode 1), and the blocks per SM of its kernels.
+cudaError_t launch_run_options(const GraphView& g, RunKind kind, const RunParams& p,
+                               const Work& w, int grid, cudaStream_t stream);
+int run_options_blocks_per_sm();
 
 // CSR construction (csr_build.cu).  build_csr sorts device edge arrays into
 // out- and (if in_off != null) in-CSR; *ids_ok = false if an id is outside

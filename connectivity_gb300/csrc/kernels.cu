@@ -1,6 +1,7 @@
 // Default run kernels (one FW-BW round), the statistics and batch-label
 // kernels, and the host launchers.  The device code of a run is in
-// run_device.cuh; the multi-round run kernels are in kernels_rounds.cu.
+// run_device.cuh; the run kernels with the optional features compiled in
+// are in kernels_options.cu.
 #include "run_device.cuh"
 
 namespace gb {
@@ -49,7 +50,7 @@ __global__ void k_localize(int32_t* labels, int32_t n, const int32_t* gid, const
 int max_coop_grid(int device) {
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-  int best = run_rounds_blocks_per_sm();
+  int best = run_options_blocks_per_sm();
   const int per[] = {run_blocks_per_sm(k_run<1, false>), run_blocks_per_sm(k_run<2, false>)};
   for (int k : per) best = k < best ? k : best;
   if (best < 1) return 0;
@@ -76,8 +77,8 @@ cudaError_t launch_run(const GraphView& g, RunKind kind, const RunParams& p, con
   if (ev) cudaEventRecord(ev[0], stream);
   // SCC and symmetric graphs walk one CSR per direction; WCC of a directed
   // graph walks the union of both
-  if (p.fwbw_rounds > 1 && g.batch.gid == nullptr)
-    e = launch_run_rounds(g, kind, p, w, grid, stream);
+  if ((p.fwbw_rounds > 1 && g.batch.gid == nullptr) || p.tune.expand_mode != 0)
+    e = launch_run_options(g, kind, p, w, grid, stream);
   else
     e = (kind == kSCC || g.in.off == nullptr) ? coop(k_run<1, false>, grid, a, stream)
                                               : coop(k_run<2, false>, grid, a, stream);

@@ -1,11 +1,12 @@
-// Run kernels with FW-BW rounds after the first (fwbw_rounds > 1), in their
-// own translation unit: the default run kernels in kernels.cu keep their
-// code whether or not this variant exists.
+// Run kernels with the optional features compiled in (FW-BW rounds after the
+// first, the edge-balanced push), in their own translation unit: the default
+// run kernels in kernels.cu keep their code whether or not this variant
+// exists.
 #include "run_device.cuh"
 
 namespace gb {
 
-cudaError_t launch_run_rounds(const GraphView& g, RunKind kind, const RunParams& p, const Work& w,
+cudaError_t launch_run_options(const GraphView& g, RunKind kind, const RunParams& p, const Work& w,
                               int grid, cudaStream_t stream) {
   Args a{};
   a.g = g;
@@ -16,7 +17,7 @@ cudaError_t launch_run_rounds(const GraphView& g, RunKind kind, const RunParams&
                                                : coop(k_run<2, true>, grid, a, stream);
 }
 
-int run_rounds_blocks_per_sm() {
+int run_options_blocks_per_sm() {
   const int a = run_blocks_per_sm(k_run<1, true>), b = run_blocks_per_sm(k_run<2, true>);
   return a < b ? a : b;
 }

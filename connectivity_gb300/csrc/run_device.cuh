@@ -23,7 +23,8 @@
 //                 (scc_serial.cpp:160-258); cc_color_propagate
 //                 (cc_color.cpp:47-175)
 // This header holds the device code of a run; kernels.cu instantiates the
-// default run kernels and kernels_rounds.cu the multi-round ones.
+// default run kernels and kernels_options.cu the ones with the optional
+// features compiled in.
 #pragma once
 #include "gb_internal.cuh"
 
@@ -526,7 +527,7 @@ __device__ __forceinline__ void visit_edges(const V& vis, const int32_t (&sv)[kE
 }
 
 constexpr int kSmallFront = 8;
-constexpr int kLocalRounds = 16;       // local rounds per step
+constexpr int kLocalRounds = 32;       // local rounds per step
 constexpr long long kLocalDegree = 4096;  // heavier vertices go to the next step
 
 // Local rounds (visitors with kLocal): the vertices this warp appended in
@@ -601,8 +602,11 @@ __device__ __forceinline__ void local_rounds(const Adj& a, const V& vis, Stage& 
 //   d >= t_grid : deferred to the next step, where every block takes a
 //                 1/grid slice of the vertex's edges;
 //   d >= t_block: the whole block walks the edges (per-block list);
-//   otherwise   : a warp takes 32 vertices, scans their degrees and walks
-//                 the concatenated edge lists 32 edges at a time.
+//   otherwise   : a warp takes 32 vertices (fewer when the frontier is
+//                 smaller than 32 per warp of the grid: then every warp
+//                 gets a share, and with it its own chain of local rounds),
+//                 scans their degrees and walks the concatenated edge lists
+//                 32 edges at a time.
 // A frontier of at most kSmallFront vertices is sliced across all blocks in
 // the same step.  The visitor decides per edge whether the far end is
 // appended.  Ends with every warp's staging flushed.
@@ -681,11 +685,13 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
   if (t == 0) sm.bl.cnt = 0;
   __syncthreads();
   const long long nw = (long long)G * (T >> 5);
-  for (long long base = ((long long)b * (T >> 5) + warp) * 32; base < nfront; base += nw * 32) {
+  // a frontier smaller than 32 per warp is spread over all warps
+  const int vpw = (long long)nfront >= nw * 32 ? 32 : (int)(((long long)nfront + nw - 1) / nw);
+  for (long long base = ((long long)b * (T >> 5) + warp) * vpw; base < nfront; base += nw * vpw) {
     const long long i = base + lane;
     int32_t v = -1;
     long long s0 = 0, d0 = 0, s1 = 0, d1 = 0;
-    if (i < nfront) {
+    if (lane < vpw && i < nfront) {
       v = __ldcg(front + i);
       rec_load<NC>(a, v, s0, d0, s1, d1);
       ty.list++;
@@ -771,6 +777,162 @@ __device__ void expand(const int32_t* front, int32_t nfront, const int32_t* heav
   }
   stage_flush(st, sk.out, c);
   __syncthreads();
+}
+
+// ------------------------------------------------------------------------
+// Global edge-balanced push (Tune::expand_mode 1): the Kokkos variant's
+// "manhattan global" scheme (kokkos_scc/fwbw_manhattan_global.cpp:186-289),
+// restated for this kernel as an alternative to the degree tiers.  The
+// frontier's edges are numbered in frontier order and every warp of the grid
+// takes an equal contiguous share of the numbers, so no vertex is deferred
+// and no tier decides who walks it.  The numbering needs the frontier's
+// degree prefix: each block sums the 32-vertex groups of its contiguous
+// share of the frontier (group prefixes local to the block go to `pre`, the
+// block's total to btot[b]); one grid barrier publishes the totals; each
+// warp then finds the group of its first edge (a scan of the block totals,
+// then a binary search over that block's group prefixes) and walks group by
+// group to the end of its share.  Every warp of the grid reads the block
+// totals, and with a small frontier the same few groups: those reads go
+// through L1 (values written before the last grid barrier are seen, since
+// the barrier's acquire invalidates the SM's L1), so that one L2 request per
+// SM, not one per warp, serves them.  Returns false when the kernel must
+// stop.
+// ------------------------------------------------------------------------
+template <int NC, class V>
+__device__ __noinline__ bool expand_balanced(const int32_t* front, int32_t nfront, const Adj& a,
+                                             const V& vis, const Sink& sk,
+                                             long long* pre /* >= ceil(nfront / 32) */,
+                                             long long* btot /* grid size */, Smem& sm, Ctl* c,
+                                             Tally& ty) {
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const int warp = t >> 5, lane = t & 31, nwarps = T >> 5;
+  Stage st = stage_make(sm.stage(warp, 0));
+  const long long ngroups = ((long long)nfront + 31) / 32;
+  const long long gpb = (ngroups + G - 1) / G;
+  const long long g0 = gpb * b < ngroups ? gpb * b : ngroups;
+  const long long g1 = g0 + gpb < ngroups ? g0 + gpb : ngroups;
+  // (a) the block's groups, one per warp per round: sums, then a block scan
+  long long run = 0;  // the block's edges before this round (same in every thread)
+  for (long long r0 = g0; r0 < g1; r0 += nwarps) {
+    const long long gi = r0 + warp;
+    long long d = 0;
+    if (gi < g1 && gi * 32 + lane < nfront) {
+      d = (long long)adj_degree<NC>(a, __ldcg(front + gi * 32 + lane));
+      ty.vtx += NC;
+    }
+    const long long gsum = warp_sum64(d);
+    __syncthreads();
+    if (lane == 0) sm.red_l[warp] = gsum;
+    __syncthreads();
+    if (warp == 0) {
+      const long long x = lane < nwarps ? sm.red_l[lane] : 0;
+      long long tot;
+      const long long ex = warp_excl64(x, tot);
+      if (lane < nwarps) sm.red_l[lane] = ex;
+      if (lane == 0) sm.red_u[0] = (unsigned long long)tot;
+    }
+    __syncthreads();
+    if (gi < g1 && lane == 0) pre[gi] = run + sm.red_l[warp];
+    run += (long long)sm.red_u[0];
+  }
+  if (t == 0) btot[b] = run;
+  if (!grid_barrier(c, 210)) return false;
+  // (b) the block totals' prefix, per warp: lane L holds blocks
+  // [L * per, (L + 1) * per)
+  const int per = (G + 31) / 32;
+  long long lsum = 0;
+  for (int j = 0; j < per; ++j) {
+    const int bb = lane * per + j;
+    if (bb < G) lsum += btot[bb];
+  }
+  long long E;
+  const long long lpre = warp_excl64(lsum, E);
+  const long long W = (long long)G * nwarps;
+  const long long gw = (long long)b * nwarps + warp;
+  const long long e0 = E * gw / W, e1 = E * (gw + 1) / W;
+  if (e0 < e1) {
+    // the block whose edges hold e0
+    int blk = -1;
+    long long bstart = 0;
+    {
+      long long p = lpre;
+      for (int j = 0; j < per; ++j) {
+        const int bb = lane * per + j;
+        const long long tb = bb < G ? btot[bb] : 0;
+        if (tb > 0 && p <= e0 && e0 < p + tb) {
+          blk = bb;
+          bstart = p;
+        }
+        p += tb;
+      }
+    }
+    const unsigned m = __ballot_sync(kFull, blk >= 0);
+    const int src = __ffs(m) - 1;  // exactly one lane holds it (e0 < E)
+    blk = __shfl_sync(kFull, blk, src);
+    bstart = shfl64(bstart, src);
+    // the last group of that block whose local prefix is <= e0 - bstart
+    const long long x = e0 - bstart;
+    long long lo = gpb * blk, hi = gpb * blk + gpb < ngroups ? gpb * blk + gpb : ngroups;
+    while (hi - lo > 1) {
+      const long long mid = (lo + hi) >> 1;
+      if (pre[mid] <= x) lo = mid;
+      else hi = mid;
+    }
+    long long gi = lo;
+    long long P = bstart + pre[gi];  // global number of the group's first edge
+    // (c) walk the groups from there to the end of this warp's share
+    while (P < e1 && gi < ngroups) {
+      const long long i = gi * 32 + lane;
+      long long s0 = 0, d0 = 0, s1 = 0, d1 = 0;
+      int32_t v = -1;
+      if (i < nfront) {
+        v = front[i];
+        rec_load<NC>(a, v, s0, d0, s1, d1);
+        ty.list++;
+      }
+      const int32_t sv = v >= 0 ? vis.source(v) : 0;
+      long long tot;
+      const long long ex = warp_excl64(d0 + d1, tot);
+      const long long lo_e = (e0 > P ? e0 : P) - P;
+      const long long hi_e = (e1 < P + tot ? e1 : P + tot) - P;
+      for (long long eb = lo_e; eb < hi_e; eb += 32 * kEU) {
+        int32_t svq[kEU], w[kEU];
+        int k[kEU];
+        bool act[kEU];
+#pragma unroll
+        for (int q = 0; q < kEU; ++q) {
+          const long long e = eb + q * 32 + lane;
+          act[q] = e < hi_e;
+          // the owner of edge e: the last lane whose exclusive prefix is <= e
+          int j = 0;
+#pragma unroll
+          for (int stp = 16; stp; stp >>= 1) {
+            const int cnd = j + stp;
+            const long long exc = shfl64(ex, cnd);
+            if (exc <= e) j = cnd;
+          }
+          const long long ej = shfl64(ex, j);
+          svq[q] = __shfl_sync(kFull, sv, j);
+          const long long s0j = shfl64(s0, j), d0j = shfl64(d0, j), s1j = shfl64(s1, j);
+          w[q] = 0;
+          k[q] = 0;
+          if (act[q]) {
+            w[q] = adj_at<NC>(a, s0j, d0j, s1j, e - ej, k[q]);
+            ty.edges++;
+          }
+        }
+        visit_edges(vis, svq, w, k, act, st, sk, c);
+      }
+      P += tot;
+      ++gi;
+    }
+  }
+  if constexpr (V::kLocal) {
+    if (vis.local()) local_rounds<NC>(a, vis, st, sk, sm, c, ty);
+  }
+  stage_flush(st, sk.out, c);
+  __syncthreads();
+  return true;
 }
 
 // ------------------------------------------------------------------------
@@ -1781,7 +1943,9 @@ struct Search {
 // updates them (every block computes the same state from the same
 // counters) and the block barrier that follows publishes them.  Returns
 // false when the kernel must stop.
-template <int NC>
+// kOptions: the optional run features are compiled in (here the edge-
+// balanced push, Tune::expand_mode 1).
+template <int NC, bool kOptions = false>
 __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const Args& A,
                             Work& w, Smem& sm, Steps& st, Tally& ty) {
   Ctl* c = w.ctl;
@@ -1895,8 +2059,22 @@ __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const
         const ReachVisit<NC> rv{q.R.allow, q.R.vis, q.R.push, q.R.local};
         const Sink sk = sink_make(q.R.q, q.qhi, w.n, o, true, q.R.minv, q.heavy[q.hsel ^ 1], w.n,
                                   201);
-        expand<NC>(q.R.q + q.qlo, (int32_t)(q.qhi - q.qlo), q.heavy[q.hsel], q.huge, q.R.push, rv,
-                   sk, tn, sm, c, ty);
+        bool tiers = true;
+        if constexpr (kOptions) {
+          if (tn.expand_mode == 1) {
+            // (its group prefixes go to the search's pull warp-tier list and
+            // its block totals to the search's half of blk_l, both free in
+            // a push step)
+            if (!expand_balanced<NC>(q.R.q + q.qlo, (int32_t)(q.qhi - q.qlo), q.R.push, rv, sk,
+                                     reinterpret_cast<long long*>(q.wl),
+                                     w.blk_l + (long long)q.dir * G, sm, c, ty))
+              return false;
+            tiers = false;
+          }
+        }
+        if (tiers)
+          expand<NC>(q.R.q + q.qlo, (int32_t)(q.qhi - q.qlo), q.heavy[q.hsel], q.huge, q.R.push,
+                     rv, sk, tn, sm, c, ty);
       } else {
         pull_thread<NC>(q.R, A, w, sm, ty, q.cand_cur, q.ncur, q.cand[q.cn], q.qhi, o, q.pp,
                         q.dir, q.wl, q.bl);
@@ -2034,8 +2212,9 @@ __device__ bool repivot(const Args& A, Smem& sm) {
 // pivot (scc_fwbw, scc_fwbw.cpp:412-513).  WCC -> one search over the union
 // adjacency (cc_bfs, cc_bfs.cpp:217-291).
 // ------------------------------------------------------------------------
-// kRepeat: a round after the first, from the pivot chosen by repivot.
-template <int NC, bool kRepeat = false>
+// kRepeat: a round after the first, from the pivot chosen by repivot;
+// kOptions: as for reach_multi.
+template <int NC, bool kRepeat = false, bool kOptions = false>
 __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   Work& w = A.w;
   Ctl* c = w.ctl;
@@ -2128,7 +2307,7 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
       B.minv = nullptr;
       if (t == 0) SB.R = B;
       __syncthreads();
-      if (!reach_multi<NC>(srch, 2, sflags, A, w, sm, st, ty)) return;
+      if (!reach_multi<NC, kOptions>(srch, 2, sflags, A, w, sm, st, ty)) return;
       // the component is what both searches reached: its smallest member,
       // while the backward bitmap becomes the intersection (the forward
       // count comes from the bitmap: local rounds leave no visit list)
@@ -2158,7 +2337,7 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
   }
   if (!together) {
     __syncthreads();
-    if (!reach_multi<NC>(&SF, 1, sflags, A, w, sm, st, ty)) return;
+    if (!reach_multi<NC, kOptions>(&SF, 1, sflags, A, w, sm, st, ty)) return;
     const int32_t nf = (int32_t)SF.qhi;  // the whole forward set: no local rounds
     if (scc) {
       if (b == 0 && t == 0) atomicAdd(&c->nvisit_fw, nf);
@@ -2170,7 +2349,7 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
       B.minv = batch ? nullptr : &c->minv[1];
       if (t == 0) SB.R = B;
       __syncthreads();
-      if (!reach_multi<1>(&SB, 1, sflags, A, w, sm, st, ty)) return;
+      if (!reach_multi<1, kOptions>(&SB, 1, sflags, A, w, sm, st, ty)) return;
       hit = w.bvis;
       hit_min = &c->minv[1];
     } else {
@@ -2385,11 +2564,13 @@ __device__ __forceinline__ void phase_mark(const Args& A, int i) {
 // previous one's lists, counters and pivot.  NC: adjacency lists walked by
 // the reachability phase (1, or 2 for WCC of a directed graph).
 // ------------------------------------------------------------------------
-// kRounds: FW-BW rounds after the first, each from a new pivot while at
-// least kRepivotMin vertices are valid (fwbw_rounds > 1, single graphs).
-// That variant is compiled in its own translation unit, so the code of the
-// default run is the same with or without it.
-template <int NC, bool kRounds>
+// kOptions: the optional features are compiled in: FW-BW rounds after the
+// first, each from a new pivot while at least kRepivotMin vertices are valid
+// (fwbw_rounds > 1, single graphs), and the edge-balanced push
+// (expand_mode 1).  That variant is compiled in its own translation unit
+// (kernels_options.cu), so the code of the default run is the same with or
+// without it.
+template <int NC, bool kOptions>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_run(Args A) {
   __shared__ Smem sm;
   sm.stage_base = g_dyn_smem;
@@ -2398,14 +2579,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_run(Args A) {
   trim_phase(A, sm);
   if (!grid_barrier(c, 900)) return;
   phase_mark(A, 1);
-  reach_phase<NC>(A, sm);
-  if constexpr (kRounds) {
-    for (int r = 1; r < A.p.fwbw_rounds; ++r) {
+  reach_phase<NC, false, kOptions>(A, sm);
+  if constexpr (kOptions) {
+    for (int r = 1; r < A.p.fwbw_rounds && A.g.batch.gid == nullptr; ++r) {
       if (!grid_barrier(c, 32)) return;  // the last round's valid count
       if (__ldcg(&c->nvalid) < kRepivotMin) break;
       if (!repivot(A, sm)) return;
       if (__ldcg(&c->rpivot) < 0) break;
-      reach_phase<NC, true>(A, sm);
+      reach_phase<NC, true, true>(A, sm);
     }
   }
   if (!grid_barrier(c, 901)) return;

@@ -4,8 +4,11 @@
 // The tunables are the degree cutoffs of the push tiers (t_block: a block
 // walks the vertex; t_grid: every block takes a slice), the in-edges a
 // thread scans in a pull step before the candidate moves to a warp (k_pull),
-// the direction-switch factors (alpha: push -> pull, beta: pull -> push) and
-// the number of resident blocks the cooperative kernel uses.  The search is
+// the direction-switch factors (alpha: push -> pull, beta: pull -> push),
+// the number of resident blocks the cooperative kernel uses, and the push
+// scheme of the searches: the degree tiers (warp, block, grid slice) or the
+// global edge balance of the Kokkos variant's "manhattan global" FW-BW
+// (kokkos_scc/fwbw_manhattan_global.cpp:186-289).  The search is
 // coordinate descent from the defaults: each tunable in turn tries its
 // candidate values with the others held, and a value is kept when it beats
 // the best time so far by more than 2 %; two passes.  Every time is the
@@ -28,7 +31,8 @@
 namespace {
 
 struct Param {
-  int which;  // 0 t_block, 1 t_grid, 2 k_pull, 3 alpha, 4 beta, 5 grid_blocks (fraction)
+  int which;  // 0 t_block, 1 t_grid, 2 k_pull, 3 alpha, 4 beta, 5 grid_blocks (fraction),
+              // 6 expand_mode
   std::vector<double> values;
 };
 
@@ -40,6 +44,7 @@ void set_param(gb_opts& o, int which, double v, int grid) {
     case 3: o.alpha = (float)v; break;
     case 4: o.beta = (float)v; break;
     case 5: o.grid_blocks = v >= 1.0 ? 0 : std::max(1, (int)(grid * v)); break;
+    case 6: o.expand_mode = (int32_t)v; break;
   }
 }
 
@@ -50,6 +55,7 @@ double get_param(const gb_opts& o, int which, int grid) {
     case 2: return o.k_pull;
     case 3: return o.alpha;
     case 4: return o.beta;
+    case 6: return o.expand_mode;
     default: return o.grid_blocks <= 0 ? 1.0 : (double)o.grid_blocks / grid;
   }
 }
@@ -90,6 +96,7 @@ gb_status tune(gb_ctx* c, int reps, Run run, gb_opts* best, double* ms_out) {
       {3, {5, 15, 50}},
       {4, {10, 25, 100}},
       {5, {0.5, 1.0}},
+      {6, {0, 1}},
   };
   gb_opts cur;
   gb_opts_default(&cur);

@@ -16,7 +16,7 @@ from . import Batch, Context, Graph, Opts, opts
 # (vertices, edge factor) of the classes tuned by default
 CLASSES = [(1 << 10, 8), (1 << 14, 16), (1 << 18, 16), (1 << 22, 16), (1 << 24, 16)]
 
-TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks")
+TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode")
 
 
 def opts_to_dict(o: Opts) -> dict:

@@ -94,6 +94,13 @@ typedef struct gb_opts {
                           round, scc_main.cpp:273-276, the default).  A round
                           is skipped once fewer than 4096 vertices are left.
                           Ignored by batches. */
+  int32_t expand_mode; /* push steps of the searches: 0 (default) degree
+                          tiers (warp / block / grid slice, t_block and
+                          t_grid); 1 global edge balance: the frontier's
+                          edges split evenly over all warps, the scheme of
+                          the Kokkos variant's manhattan-global FW-BW
+                          (kokkos_scc/fwbw_manhattan_global.cpp:186-289).
+                          An autotuner candidate. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);

@@ -53,7 +53,8 @@ def test_batch_from_edges_edge_cases(ctx):
     b = gb.Batch.from_edges(ctx, np.array(vb), np.concatenate(ss).astype(np.int32),
                             np.concatenate(dd).astype(np.int32))
     for variant in ({}, {"trim_level": 2}, {"t_block": 33, "t_grid": 64},
-                    {"alpha": 1e9, "beta": 1e-3, "k_pull": 1}):
+                    {"alpha": 1e9, "beta": 1e-3, "k_pull": 1}, {"trim_level": 0},
+                    {"trim_pairs": 1}, {"expand_mode": 1}, {"fwbw_rounds": 3}):
         scc = b.split(ctx.batch_scc(b, o=gb.opts(**variant)))
         wcc = b.split(ctx.batch_wcc(b, o=gb.opts(**variant)))
         for i, (name, n, s, d) in enumerate(cases):

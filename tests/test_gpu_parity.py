@@ -21,6 +21,8 @@ VARIANTS = {
     "pairs": {"trim_pairs": 1},
     "pairs2": {"trim_level": 2, "trim_pairs": 1},
     "rounds": {"fwbw_rounds": 4},
+    "balanced": {"expand_mode": 1},
+    "balanced_rounds": {"expand_mode": 1, "fwbw_rounds": 3, "trim_pairs": 1},
     # tiny tiers push every vertex through the block and grid-slice paths
     "tiers": {"t_block": 33, "t_grid": 64},
     "pull_early": {"alpha": 1e9, "beta": 1e-3, "k_pull": 1},
@@ -50,7 +52,7 @@ def test_scc_edge_cases(ctx, case, variant):
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-@pytest.mark.parametrize("variant", ["default", "tiers", "pull_early", "small_grid"])
+@pytest.mark.parametrize("variant", ["default", "tiers", "pull_early", "small_grid", "balanced"])
 def test_wcc_edge_cases(ctx, case, variant):
     name, n, s, d = case
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -70,8 +72,8 @@ def test_reference_golden_vector(ctx):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "rounds", "tiers",
-                                     "pull_early", "small_grid"])
+@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "rounds", "balanced",
+                                     "balanced_rounds", "tiers", "pull_early", "small_grid"])
 def test_rmat_scc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -81,7 +83,7 @@ def test_rmat_scc(ctx, scale, ef, variant):
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (14, 16), (16, 16), (18, 8)])
-@pytest.mark.parametrize("variant", ["default", "pull_early", "rounds"])
+@pytest.mark.parametrize("variant", ["default", "pull_early", "rounds", "balanced"])
 def test_rmat_wcc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -89,7 +91,7 @@ def test_rmat_wcc(ctx, scale, ef, variant):
 
 
 @pytest.mark.parametrize("side", [16, 64, 128])
-@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "pairs2"])
+@pytest.mark.parametrize("variant", ["default", "trim0", "trim2", "pairs", "pairs2", "balanced"])
 def test_grid_scc(ctx, side, variant):
     n, s, d = graphs.grid(side)
     g = gb.Graph.from_edges(ctx, n, s, d)
@@ -394,3 +396,20 @@ def test_repivot_stops_when_little_is_left(ctx):
     lab, st = ctx.scc(g, o=gb.opts(fwbw_rounds=50), stats=True)
     assert np.array_equal(lab, _scc_want(n, s, d))
     assert st.fwbw_rounds == 1
+
+
+@pytest.mark.parametrize("kind", ["scc", "wcc"])
+def test_balanced_push_same_work(ctx, kind):
+    """The edge-balanced push walks each reached vertex's edges once, as the
+    tiers do: same labels and the same visited edge counts (push steps
+    only)."""
+    n, s, d = graphs.rmat(16, 16)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    fn = ctx.scc if kind == "scc" else ctx.wcc
+    o_t = gb.opts(alpha=1e-9)
+    o_b = gb.opts(alpha=1e-9, expand_mode=1)
+    lt, st_t = fn(g, o=o_t, stats=True)
+    lb, st_b = fn(g, o=o_b, stats=True)
+    assert np.array_equal(lt, lb)
+    assert st_b.m_visit_fw == st_t.m_visit_fw and st_b.m_visit_bw == st_t.m_visit_bw
+    assert st_b.pull_steps == 0 and st_t.pull_steps == 0
