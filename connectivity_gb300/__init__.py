@@ -94,6 +94,7 @@ def _sig(name, res, args):
 _sig("gb_status_string", C.c_char_p, [C.c_int32])
 _sig("gb_last_error", C.c_char_p, [])
 _sig("gb_opts_default", None, [C.POINTER(Opts)])
+_sig("gb_struct_sizes", None, [C.POINTER(C.c_int64)])
 _sig("gb_ctx_create", C.c_int32, [C.c_int, C.POINTER(_P)])
 _sig("gb_ctx_destroy", C.c_int32, [_P])
 _sig("gb_ctx_set_stream", C.c_int32, [_P, _P])

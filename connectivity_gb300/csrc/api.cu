@@ -356,6 +356,13 @@ int32_t g_stage_n = -1;
 
 extern "C" {
 
+void gb_struct_sizes(int64_t sizes[3]) {
+  if (!sizes) return;
+  sizes[0] = (int64_t)sizeof(gb_opts);
+  sizes[1] = (int64_t)sizeof(gb_stats);
+  sizes[2] = (int64_t)sizeof(gb_server_stats);
+}
+
 void gb_opts_default(gb_opts* o) {
   if (!o) return;
   o->trim_level = 1;

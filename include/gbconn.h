@@ -105,6 +105,11 @@ typedef struct gb_opts {
 
 void gb_opts_default(gb_opts* o);
 
+/* sizeof(gb_opts), sizeof(gb_stats) and sizeof(gb_server_stats) as this
+ * library was built, into sizes[0..2]: bindings that mirror the structs
+ * (ctypes, cgo) check their layouts against it.  No device is needed. */
+void gb_struct_sizes(int64_t sizes[3]);
+
 /* Per-run results.  Times are in milliseconds: trim, reach and colour from
  * the device clock at the run kernel's phase boundaries; canon (the
  * statistics pass) and total from CUDA events on the context stream. */

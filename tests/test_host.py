@@ -32,6 +32,23 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_struct_layouts_match_the_library():
+    """The ctypes mirrors of gb_opts, gb_stats and gb_server_stats have the
+    sizes the library was built with, and gb_opts_default fills the mirror
+    with the documented defaults without writing past it."""
+    sizes = (ctypes.c_int64 * 3)()
+    gb._lib.gb_struct_sizes(sizes)
+    assert list(sizes) == [ctypes.sizeof(gb.Opts), ctypes.sizeof(gb.Stats),
+                           ctypes.sizeof(gb.ServerStats)]
+    buf = (ctypes.c_ubyte * (ctypes.sizeof(gb.Opts) + 16))(*([0xAB] * (ctypes.sizeof(gb.Opts) + 16)))
+    o = gb.Opts.from_buffer(buf)
+    gb._lib.gb_opts_default(ctypes.byref(o))
+    assert bytes(buf[ctypes.sizeof(gb.Opts):]) == b"\xab" * 16
+    assert (o.trim_level, o.canonical, o.pivot, o.k_pull, o.trim_pairs, o.fwbw_rounds,
+            o.expand_mode) == (1, 1, -1, 4, 0, 1, 0)
+    assert o.alpha == 15.0 and o.beta == 25.0
+
+
 def test_status_strings():
     lib = ctypes.CDLL(gb.LIB_PATH)
     lib.gb_status_string.restype = ctypes.c_char_p
