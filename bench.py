@@ -68,7 +68,10 @@ def parse():
     p.add_argument("--scale", type=int, default=SCALE,
                    help="R-MAT scale of the headline graph (smaller only for profiling)")
     p.add_argument("--sections", default="headline,batched,served",
-                   help="comma list of headline, batched, served")
+                   help="comma list of headline, batched, served, grid (the 4096^2 "
+                        "lattice, not in the default list)")
+    p.add_argument("--grid-side", type=int, default=4096,
+                   help="lattice side of the grid section (smaller only for profiling)")
     p.add_argument("--serve-rate", type=float, default=20000.0)
     p.add_argument("--serve-seconds", type=float, default=1.5)
     p.add_argument("--serve-pool", type=int, default=400)
@@ -310,6 +313,42 @@ def batched_section(gb, ctx, stream, steps, sample=400):
     for g in gs:
         g.close()
     b.close()
+    return out
+
+
+def grid_section(gb, ctx, side=4096, reps=2):
+    import torch
+    """Config 3: the oriented side x side lattice with chains, where the
+    colour rounds do the work.  Device time per run (best of reps after one
+    warm-up) and the colour phase's bytes touched per second against the HBM
+    peak: that phase is bound by chains of dependent hops, not by bandwidth."""
+    n, s, d = gb.grid_edges(side)
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    peak, kind = peaks()
+    # (an NVTX range, so that a profiler can select these runs: ncu --nvtx
+    # --nvtx-include "grid/")
+    torch.cuda.nvtx.range_push("grid")
+    out = {"workload": (f"{side}x{side} oriented lattice plus chains, seed 2 ({n:,} vertices, "
+                        f"{s.size:,} edges); not part of the headline")}
+    for name, fn in (("scc", ctx.scc), ("wcc", ctx.wcc)):
+        fn(g)
+        runs = [fn(g, stats=True)[1] for _ in range(reps)]
+        st = min(runs, key=lambda x: x.ms_total)
+        e = {"ms_per_run": round(st.ms_total, 3),
+             "phases_ms": {"trim": round(st.ms_trim, 3), "reach": round(st.ms_reach, 3),
+                           "colour": round(st.ms_colour, 3)},
+             "colour_rounds": int(st.colour_rounds),
+             "steps": {"search": int(st.fw_steps + st.bw_steps), "colour": int(st.colour_steps),
+                       "mark": int(st.mark_steps)}}
+        if st.ms_colour > 0:
+            gbs = st.bytes_colour / (st.ms_colour * 1e-3) / 1e9
+            e["colour_roofline"] = {"bytes_touched": int(st.bytes_colour),
+                                    "achieved_gbs": round(gbs, 1), "peak": peak,
+                                    "peak_source": f"{kind} hbm_gbs", "frac": round(gbs / peak, 4),
+                                    "bound": "latency (chains of dependent hops)"}
+        out[name] = e
+    torch.cuda.nvtx.range_pop()
+    g.close()
     return out
 
 
@@ -575,6 +614,8 @@ def run_gbconn(args):
                           "verify_line": gb.scc_verify(gpu_labels).strip()}
     g.close()
     del labels
+    if "grid" in sections:
+        line["grid"] = grid_section(gb, ctx, side=args.grid_side)
     if "batched" in sections:
         line["batched"] = batched_section(gb, ctx, stream, 5)
     ctx.close()
