@@ -199,12 +199,15 @@ gb_status part_upload(gb_server* sv, Part& p) {
       cudaMemcpyAsync(p.d_vb, p.vbase.data(), p.vbase.size() * 8, cudaMemcpyHostToDevice, cs) !=
           cudaSuccess)
     return GB_ERR_CUDA;
+  // (the pinned buffers are sized at creation and grow by half again when
+  // a merged set outgrows them: pinning inside the request stream stalls it)
   if ((size_t)p.n > p.h_cap) {
     if (p.h_labels) cudaFreeHost(p.h_labels);
     p.h_labels = nullptr;
+    const size_t want = std::max((size_t)p.n, p.h_cap * 3 / 2);
     p.h_cap = 0;
-    if (cudaMallocHost(&p.h_labels, (size_t)(p.n > 0 ? p.n : 1) * 4) != cudaSuccess) return GB_ERR_OOM;
-    p.h_cap = (size_t)p.n;
+    if (cudaMallocHost(&p.h_labels, want * 4) != cudaSuccess) return GB_ERR_OOM;
+    p.h_cap = want;
   }
   if (p.reqs.size() > p.h_bad_cap) {
     if (p.h_bad) cudaFreeHost(p.h_bad);
@@ -213,6 +216,19 @@ gb_status part_upload(gb_server* sv, Part& p) {
     if (cudaMallocHost(&p.h_bad, p.reqs.size() * 4) != cudaSuccess) return GB_ERR_OOM;
     p.h_bad_cap = p.reqs.size();
   }
+  return GB_OK;
+}
+
+// Pinned host buffers of every part, sized before the server starts.
+constexpr size_t kInitLabels = size_t(1) << 22;  // labels per part (16 MB)
+gb_status reserve_parts(gb_server* sv) {
+  for (auto& f : sv->fl)
+    for (auto& p : f.part) {
+      if (cudaMallocHost(&p.h_labels, kInitLabels * 4) != cudaSuccess) return GB_ERR_OOM;
+      p.h_cap = kInitLabels;
+      if (cudaMallocHost(&p.h_bad, (size_t)sv->max_graphs * 4) != cudaSuccess) return GB_ERR_OOM;
+      p.h_bad_cap = (size_t)sv->max_graphs;
+    }
   return GB_OK;
 }
 
@@ -377,6 +393,10 @@ gb_status gb_server_create(gb_ctx* ctx, int64_t budget_bytes, int32_t max_graphs
   for (auto& f : sv->fl) {
     cudaEventCreateWithFlags(&f.uploaded, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
+  }
+  if (reserve_parts(sv) != GB_OK) {
+    gb_server_destroy(sv);
+    return GB_ERR_OOM;
   }
   *out = sv;
   return GB_OK;
