@@ -81,11 +81,6 @@ __device__ __forceinline__ bool bit_release(uint32_t* bm, int32_t v) {
   return (atomicAnd(bm + (v >> 5), ~b) & b) != 0u;
 }
 
-// Bulk prefetch of [p, p + bytes) into L2 (p 16-byte aligned, bytes a
-// multiple of 16, the range inside one allocation).
-__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
 __device__ __forceinline__ long long shfl64(long long x, int src) {
   int lo = __shfl_sync(kFull, (int)(x & 0xffffffffll), src);
   int hi = __shfl_sync(kFull, (int)(x >> 32), src);
@@ -1254,21 +1249,10 @@ __device__ __forceinline__ void trim_phase(Args& A, Smem& sm) {
   const long long wlo = bchunk * b < w.nwords ? bchunk * b : w.nwords;
   const long long whi = wlo + bchunk < w.nwords ? wlo + bchunk : w.nwords;
   int wvalid = 0;  // warp-uniform
-  // The L2 is asked ahead (a bulk prefetch of the warp's next words of both
-  // offset arrays) while this iteration's loads are outstanding.
+  // (a bulk L2 prefetch of the warp's next words, two iterations ahead, was
+  // measured 3 us slower per R-MAT-24 run than none)
   const bool has_in = g.in.off != nullptr;
-  constexpr long long kTrimAhead = 2;  // iterations ahead
-  // (caller-supplied CSRs need not be 16-byte aligned: no prefetch then)
-  const bool pf_ok = ((reinterpret_cast<uintptr_t>(g.out.off) |
-                       (has_in ? reinterpret_cast<uintptr_t>(g.in.off) : 0u)) & 15u) == 0u;
   for (long long wd0 = wlo + warp * kTrimU; wd0 < whi; wd0 += (T >> 5) * kTrimU) {
-    {
-      const long long pw = wd0 + kTrimAhead * (T >> 5) * kTrimU;
-      if (pf_ok && lane == 0 && pw + kTrimU <= whi && (pw + kTrimU) * 32 <= (long long)g.n + 1) {
-        prefetch_l2(g.out.off + pw * 32, kTrimU * 32 * 8);
-        if (has_in) prefetch_l2(g.in.off + pw * 32, kTrimU * 32 * 8);
-      }
-    }
     long long o0[kTrimU], o1[kTrimU], i0[kTrimU], i1[kTrimU];
 #pragma unroll
     for (int j = 0; j < kTrimU; ++j) {
