@@ -180,9 +180,13 @@ def test_tune_table_lookup():
         {"n": 1 << 10, "opts": {"t_block": 128, "t_grid": 8192, "k_pull": 2, "alpha": 5.0,
                                 "beta": 10.0, "grid_blocks": 0}},
         {"n": 1 << 20, "opts": {"t_block": 2048, "t_grid": 131072, "k_pull": 4, "alpha": 50.0,
-                                "beta": 100.0, "grid_blocks": 76}}]}
+                                "beta": 100.0, "grid_blocks": 76, "expand_mode": 1}}]}
     assert tune.opts_for(table, 600).t_block == 128
+    assert tune.opts_for(table, 600).expand_mode == 0  # (a table written before the field)
     assert tune.opts_for(table, 1 << 19).t_block == 2048
     o = tune.opts_for(table, 1 << 22)
-    assert (o.t_grid, o.k_pull, o.grid_blocks) == (131072, 4, 76)
-    assert tune.dict_to_opts(tune.opts_to_dict(o)).beta == 100.0
+    assert (o.t_grid, o.k_pull, o.grid_blocks, o.expand_mode) == (131072, 4, 76, 1)
+    back = tune.dict_to_opts(tune.opts_to_dict(o))
+    assert back.beta == 100.0 and back.expand_mode == 1
+    # options outside the tuned set keep their defaults
+    assert (back.trim_level, back.fwbw_rounds, back.trim_pairs) == (1, 1, 0)
