@@ -103,3 +103,35 @@ def test_oracle_against_live_reference(seed):
     assert np.array_equal(oracle.canonical(raw), oracle.scc(oracle.CpuGraph(n, s, d)))
     raw, line, _ = oracle.ref_run("cc", n, s, d, threads=4)
     assert np.array_equal(oracle.canonical(raw), oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_random_graphs_against_scipy(seed):
+    """Random graphs of mixed shape (sparse, dense, planted cycles and
+    two-cycles, self-loops and duplicate edges): the oracle's SCC labels at
+    every trim level, and its CC labels, equal scipy's components in
+    canonical form."""
+    sp = pytest.importorskip("scipy.sparse")
+    csg = pytest.importorskip("scipy.sparse.csgraph")
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(2, 3000))
+    m = int(rng.integers(0, 4 * n))
+    s = rng.integers(0, n, m)
+    d = rng.integers(0, n, m)
+    # a few planted cycles and two-cycles
+    for _ in range(int(rng.integers(0, 20))):
+        k = int(rng.integers(2, 40))
+        cyc = rng.choice(n, size=min(k, n), replace=False)
+        s = np.concatenate([s, cyc])
+        d = np.concatenate([d, np.roll(cyc, -1)])
+    s = s.astype(np.int32)
+    d = d.astype(np.int32)
+    a = sp.csr_matrix((np.ones(s.size, np.int8), (s, d)), shape=(n, n))
+    _, lab = csg.connected_components(a, directed=True, connection="strong")
+    want = oracle.canonical(lab.astype(np.int32))
+    g = oracle.CpuGraph(n, s, d)
+    for trim in (0, 1, 2):
+        assert np.array_equal(oracle.scc(g, trim_level=trim), want), trim
+    _, lab = csg.connected_components(a, directed=True, connection="weak")
+    assert np.array_equal(oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)),
+                          oracle.canonical(lab.astype(np.int32)))
