@@ -398,7 +398,7 @@ gb_status gb_cc_verify(int32_t n, const int32_t* labels, char* line, size_t cap,
 /* Host relabelling to the minimum member id. */
 gb_status gb_canonicalize(int32_t n, int32_t* labels);
 /* Seeded generators (host, deterministic across machines).
- * R-MAT: as gb_graph_rmat; *src/*dst malloc'd, sorted by (src, dst). */
+ * R-MAT: as gb_graph_rmat; the edge arrays (*src, *dst) are malloc'd and sorted by (src, dst). */
 gb_status gb_rmat_edges_host(int32_t scale, int32_t edge_factor, uint64_t seed, double a,
                              double b, double c, int64_t* m, int32_t** src, int32_t** dst);
 /* R-MAT on any n (the batch rule, see gb_graph_rmat_n). */
