@@ -157,6 +157,8 @@ for _n in ("gb_scc_async", "gb_wcc_async"):
 _sig("gb_run_scc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int])
 _sig("gb_run_cc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, C.c_int, C.c_double])
 _sig("gb_read_edge", C.c_int32, [C.c_char_p, _I32P, _I64P, C.POINTER(_P), C.POINTER(_P)])
+_sig("gb_read_edge_pieces", C.c_int32,
+     [C.c_char_p, C.c_int32, _I32P, _I64P, C.POINTER(_P), C.POINTER(_P)])
 _sig("gb_free_host", None, [_P])
 _sig("gb_output_labels", C.c_int32, [C.c_char_p, C.c_int32, _P])
 _sig("gb_scc_verify", C.c_int32, [C.c_int32, _P, C.c_char_p, C.c_size_t, _I64P])
@@ -219,12 +221,13 @@ def write_text(path: str, n: int, src, dst) -> None:
            "gb_write_text")
 
 
-def read_edge(path: str) -> tuple[int, np.ndarray, np.ndarray]:
-    """read_edge (scc_main.cpp:94-125): returns (n, src, dst)."""
+def read_edge(path: str, pieces: int = 0) -> tuple[int, np.ndarray, np.ndarray]:
+    """read_edge (scc_main.cpp:94-125): returns (n, src, dst).  pieces: how
+    many pieces the body is parsed in by host threads (0: automatic)."""
     n, m = C.c_int32(), C.c_int64()
     s, d = C.c_void_p(), C.c_void_p()
-    _check(_lib.gb_read_edge(path.encode(), C.byref(n), C.byref(m), C.byref(s), C.byref(d)),
-           "read_edge")
+    _check(_lib.gb_read_edge_pieces(str(path).encode(), int(pieces), C.byref(n), C.byref(m),
+                                    C.byref(s), C.byref(d)), "read_edge")
     return n.value, _take(s, m.value, np.int32), _take(d, m.value, np.int32)
 
 

@@ -14,7 +14,11 @@
 #include <string>
 #include <vector>
 
+#include <fcntl.h>
 #include <omp.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "../../include/gbconn.h"
 #include "gen_common.h"
@@ -81,28 +85,132 @@ struct Cursor {
 };
 }  // namespace
 
-extern "C" gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int32_t** srcs,
-                                  int32_t** dsts) {
+// The body is parsed in pieces by OpenMP threads.  A piece starts at a
+// blank, so it never splits a number, and every piece is read with the same
+// cursor as a whole file would be.  Pass 1 counts the numbers each piece
+// holds up to its end or its first unreadable byte; a prefix over the counts
+// places each piece's numbers in the global sequence; pass 2 stores number
+// k into edge k / 2 and notes the first edge with an id outside [0, n).
+// The outcome is the sequential reader's: the first failure in edge order
+// wins (an unreadable or missing number: GB_ERR_IO; an id out of range in an
+// edge read whole: GB_ERR_INVALID), and numbers after the first 2m are
+// ignored.
+namespace {
+struct Piece {
+  const char* lo;
+  const char* hi;
+  long long count = 0;  // numbers read before hi or the failure
+  bool failed = false;  // an unreadable byte before hi
+  long long first = 0;  // global index of the piece's first number
+};
+
+long long read_body(const char* body, const char* end, long long nn, long long mm, int pieces,
+                    int32_t* s, int32_t* d, long long* bad_edge) {
+  // returns the count of numbers readable before the first failure (capped
+  // at 2m); *bad_edge = first edge with an id out of range, or mm
+  const long long len = (long long)(end - body);
+  if (pieces <= 0) {
+    const long long want = len / (1 << 20) + 1;  // about 1 MB per piece
+    pieces = (int)std::min<long long>(want, 64LL * omp_get_max_threads());
+  }
+  if (pieces > len) pieces = (int)std::max<long long>(len, 1);
+  auto blank = [](char ch) { return ch == ' ' || ch == '\t' || ch == '\r' || ch == '\n'; };
+  std::vector<Piece> pc((size_t)pieces);
+  for (int i = 0; i < pieces; ++i) {
+    const char* lo = body + len * i / pieces;
+    if (i > 0)
+      while (lo < end && !blank(*lo)) ++lo;  // start at a blank (or the end)
+    pc[(size_t)i].lo = lo;
+  }
+  for (int i = 0; i < pieces; ++i) pc[(size_t)i].hi = i + 1 < pieces ? pc[(size_t)i + 1].lo : end;
+  for (int i = 0; i + 1 < pieces; ++i)  // a later start pushed past an earlier one
+    if (pc[(size_t)i].hi < pc[(size_t)i].lo) pc[(size_t)i].hi = pc[(size_t)i].lo;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < pieces; ++i) {
+    Piece& q = pc[(size_t)i];
+    Cursor c{q.lo, q.hi};
+    long long v;
+    while (c.skip_ws()) {
+      if (!c.read_i64(v)) {
+        q.failed = true;
+        break;
+      }
+      ++q.count;
+    }
+  }
+  long long avail = 0;  // numbers before the first failure
+  bool stop = false;
+  for (int i = 0; i < pieces; ++i) {
+    Piece& q = pc[(size_t)i];
+    if (stop) {  // after the first failure, or past 2m numbers: not stored
+      q.count = 0;
+      continue;
+    }
+    q.first = avail;
+    avail += q.count;
+    stop = q.failed || avail >= 2 * mm;
+  }
+  if (avail > 2 * mm) avail = 2 * mm;
+  long long bad = mm;
+#pragma omp parallel for schedule(dynamic, 1) reduction(min : bad)
+  for (int i = 0; i < pieces; ++i) {
+    Piece& q = pc[(size_t)i];
+    if (q.count == 0 || q.first >= avail) continue;
+    Cursor c{q.lo, q.hi};
+    long long v = 0;
+    for (long long k = q.first; k < avail && k < q.first + q.count; ++k) {
+      c.read_i64(v);  // counted in pass 1: it reads
+      const long long e = k >> 1;
+      if (v < 0 || v >= nn) bad = std::min(bad, e);
+      if (k & 1) d[e] = (int32_t)v;
+      else s[e] = (int32_t)v;
+    }
+  }
+  *bad_edge = bad;
+  return avail;
+}
+}  // namespace
+
+extern "C" gb_status gb_read_edge_pieces(const char* path, int32_t pieces, int32_t* n, int64_t* m,
+                                         int32_t** srcs, int32_t** dsts) {
   if (!path || !n || !m || !srcs || !dsts) {
     gb_set_error("gb_read_edge: null argument%s", "");
     return GB_ERR_INVALID;
   }
-  FILE* f = std::fopen(path, "rb");
-  if (!f) {
+  // the file is mapped, not copied (a multi-GB edge list is parsed in place)
+  const int fd = ::open(path, O_RDONLY);
+  if (fd < 0) {
     gb_set_error("gb_read_edge: cannot open %s", path);
     return GB_ERR_IO;
   }
-  std::fseek(f, 0, SEEK_END);
-  long long size = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  std::vector<char> buf((size_t)(size > 0 ? size : 0) + 1);
-  if (size > 0 && std::fread(buf.data(), 1, (size_t)size, f) != (size_t)size) {
-    std::fclose(f);
-    gb_set_error("gb_read_edge: short read of %s", path);
+  struct stat sb;
+  if (::fstat(fd, &sb) != 0) {
+    ::close(fd);
+    gb_set_error("gb_read_edge: cannot stat %s", path);
     return GB_ERR_IO;
   }
-  std::fclose(f);
-  Cursor c{buf.data(), buf.data() + size};
+  const size_t size = (size_t)(sb.st_size > 0 ? sb.st_size : 0);
+  const char* base = "";
+  void* map = nullptr;
+  if (size > 0) {
+    map = ::mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+    if (map == MAP_FAILED) {
+      ::close(fd);
+      gb_set_error("gb_read_edge: cannot map %s", path);
+      return GB_ERR_IO;
+    }
+    ::madvise(map, size, MADV_SEQUENTIAL);
+    base = (const char*)map;
+  }
+  ::close(fd);
+  struct Unmap {
+    void* p;
+    size_t n;
+    ~Unmap() {
+      if (p) ::munmap(p, n);
+    }
+  } unmap{map, size};
+  Cursor c{base, base + size};
   long long nn, mm;
   if (!c.read_i64(nn) || !c.read_i64(mm) || nn < 0 || nn > 0x7fffffffll || mm < 0) {
     gb_set_error("gb_read_edge: bad header in %s", path);
@@ -116,28 +224,31 @@ extern "C" gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int3
     gb_set_error("gb_read_edge: out of host memory%s", "");
     return GB_ERR_OOM;
   }
-  for (long long i = 0; i < mm; ++i) {
-    long long a, b;
-    if (!c.read_i64(a) || !c.read_i64(b)) {
-      std::free(s);
-      std::free(d);
-      gb_set_error("gb_read_edge: fewer edges than the header says in %s", path);
-      return GB_ERR_IO;
-    }
-    if (a < 0 || a >= nn || b < 0 || b >= nn) {
-      std::free(s);
-      std::free(d);
-      gb_set_error("gb_read_edge: vertex id out of range in %s", path);
-      return GB_ERR_INVALID;
-    }
-    s[i] = (int32_t)a;
-    d[i] = (int32_t)b;
+  long long bad = mm;
+  const long long avail = read_body(c.p, base + size, nn, mm, pieces, s, d, &bad);
+  const long long whole = avail / 2;  // edges read whole before the first failure
+  if (bad < whole) {
+    std::free(s);
+    std::free(d);
+    gb_set_error("gb_read_edge: vertex id out of range in %s", path);
+    return GB_ERR_INVALID;
+  }
+  if (avail < 2 * mm) {
+    std::free(s);
+    std::free(d);
+    gb_set_error("gb_read_edge: fewer edges than the header says in %s", path);
+    return GB_ERR_IO;
   }
   *n = (int32_t)nn;
   *m = mm;
   *srcs = s;
   *dsts = d;
   return GB_OK;
+}
+
+extern "C" gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int32_t** srcs,
+                                  int32_t** dsts) {
+  return gb_read_edge_pieces(path, 0, n, m, srcs, dsts);
 }
 
 extern "C" gb_status gb_output_labels(const char* path, int32_t n, const int32_t* labels) {

@@ -382,6 +382,11 @@ gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out
  * reader mirrors the edges (cc_main.cpp:102-118); here mirroring is done by
  * gb_wcc itself, so one reader serves both. */
 gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int32_t** srcs, int32_t** dsts);
+/* gb_read_edge with the body parsed in `pieces` pieces by OpenMP threads (0:
+ * about 1 MB each, the choice gb_read_edge makes).  Every piece count gives
+ * the same arrays and the same status as one piece. */
+gb_status gb_read_edge_pieces(const char* path, int32_t pieces, int32_t* n, int64_t* m,
+                              int32_t** srcs, int32_t** dsts);
 void gb_free_host(void* p);
 /* output_scc / output_cc (scc_main.cpp:193-202, cc_main.cpp:167-176): one
  * label per line. */

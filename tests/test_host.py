@@ -89,6 +89,86 @@ def test_read_edge_and_errors(tmp_path):
     assert e.value.status == 6
 
 
+def _seq_read(text):
+    """The reader's sequential semantics, restated: (status, n, src, dst)."""
+    blank = " \t\r\n"
+    pos = [0]
+
+    def num():
+        i = pos[0]
+        while i < len(text) and text[i] in blank:
+            i += 1
+        if i >= len(text):
+            pos[0] = i
+            return None
+        j = i
+        if text[j] in "+-":
+            j += 1
+        k = j
+        while k < len(text) and text[k].isdigit():
+            k += 1
+        if k == j or int(text[j:k]) > (1 << 62):
+            pos[0] = i
+            return None
+        pos[0] = k
+        return int(text[i:k])
+
+    nn, mm = num(), num()
+    if nn is None or mm is None or nn < 0 or nn > 0x7FFFFFFF or mm < 0:
+        return 6, None, None, None
+    src, dst = [], []
+    for _ in range(mm):
+        a = num()
+        b = num() if a is not None else None
+        if a is None or b is None:
+            return 6, None, None, None
+        if not (0 <= a < nn and 0 <= b < nn):
+            return 1, None, None, None
+        src.append(a)
+        dst.append(b)
+    return 0, nn, src, dst
+
+
+def test_read_edge_pieces_match_sequential(tmp_path):
+    """The body parsed in any number of pieces gives the sequential reader's
+    arrays and status, on good files and on every kind of bad one."""
+    rng = np.random.default_rng(5)
+    texts = []
+    for t in range(40):
+        n = int(rng.integers(1, 50))
+        m = int(rng.integers(0, 60))
+        toks = [str(int(x)) for x in rng.integers(0, n, 2 * m)]
+        kind = t % 8
+        if kind == 1 and toks:  # an id out of range somewhere
+            toks[int(rng.integers(0, len(toks)))] = str(n + int(rng.integers(0, 5)))
+        elif kind == 2 and toks:  # garbage somewhere
+            toks[int(rng.integers(0, len(toks)))] = rng.choice(["x", "1a", "+", "-", "--3"])
+        elif kind == 3:  # truncated
+            toks = toks[: int(rng.integers(0, len(toks) + 1))]
+        elif kind == 4 and len(toks) >= 4:  # out of range, then garbage later (or earlier)
+            i, j = sorted(rng.choice(len(toks), 2, replace=False))
+            toks[int(i)], toks[int(j)] = (str(n), "x") if t % 16 < 8 else ("x", str(n))
+        elif kind == 5:  # extra tokens after the edges
+            toks += ["7", "x", "-1"]
+        elif kind == 6 and toks:  # signs and glued numbers
+            toks[int(rng.integers(0, len(toks)))] = rng.choice(["+0", "-0", "0-0", "1+0"])
+        seps = [rng.choice([" ", "  ", "\t", "\n", "\r\n", " \n "]) for _ in toks]
+        body = "".join(sep + tok for sep, tok in zip(seps, toks))
+        texts.append(f"{n} {m}{body}\n")
+    for i, text in enumerate(texts):
+        p = tmp_path / f"g{i}.txt"
+        p.write_text(text)
+        want = _seq_read(text)
+        for pieces in (1, 2, 3, 7, 64, 1000):
+            if want[0] == 0:
+                n, s_, d_ = gb.read_edge(str(p), pieces=pieces)
+                assert n == want[1] and s_.tolist() == want[2] and d_.tolist() == want[3], (i, pieces)
+            else:
+                with pytest.raises(gb.GBError) as e:
+                    gb.read_edge(str(p), pieces=pieces)
+                assert e.value.status == want[0], (i, pieces, text)
+
+
 def test_output_labels(tmp_path):
     p = tmp_path / "out.txt"
     gb.output_labels(str(p), np.array([0, 0, 2, -1], np.int32))
