@@ -251,31 +251,7 @@ extern "C" gb_status gb_read_edge(const char* path, int32_t* n, int64_t* m, int3
   return gb_read_edge_pieces(path, 0, n, m, srcs, dsts);
 }
 
-extern "C" gb_status gb_output_labels(const char* path, int32_t n, const int32_t* labels) {
-  if (!path || (n > 0 && !labels) || n < 0) return GB_ERR_INVALID;
-  FILE* f = std::fopen(path, "wb");
-  if (!f) {
-    gb_set_error("gb_output_labels: cannot open %s", path);
-    return GB_ERR_IO;
-  }
-  std::vector<char> out;
-  out.reserve(1 << 20);
-  char tmp[16];
-  for (int32_t i = 0; i < n; ++i) {
-    int len = std::snprintf(tmp, sizeof(tmp), "%d\n", labels[i]);
-    out.insert(out.end(), tmp, tmp + len);
-    if (out.size() > (1u << 20)) {
-      if (std::fwrite(out.data(), 1, out.size(), f) != out.size()) { std::fclose(f); return GB_ERR_IO; }
-      out.clear();
-    }
-  }
-  bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
-  ok = (std::fclose(f) == 0) && ok;
-  return ok ? GB_OK : GB_ERR_IO;
-}
-
-// Edge list in the reference's text format ("n m", then "src dst" lines),
-// the input of read_edge (scc_main.cpp:94-125).
+// The decimal digits of v at p; returns the end.
 static char* put_u32(char* p, uint32_t v) {
   char tmp[12];
   int k = 0;
@@ -287,6 +263,36 @@ static char* put_u32(char* p, uint32_t v) {
   return p;
 }
 
+// One label per line ("%d\n", as output_scc writes them), formatted in
+// 1 MB blocks of lines.
+extern "C" gb_status gb_output_labels(const char* path, int32_t n, const int32_t* labels) {
+  if (!path || (n > 0 && !labels) || n < 0) return GB_ERR_INVALID;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    gb_set_error("gb_output_labels: cannot open %s", path);
+    return GB_ERR_IO;
+  }
+  constexpr size_t kBlock = 1 << 20;
+  std::vector<char> out(kBlock + 16);
+  char* p = out.data();
+  bool ok = true;
+  for (int32_t i = 0; i < n && ok; ++i) {
+    const int32_t l = labels[i];
+    if (l < 0) *p++ = '-';
+    p = put_u32(p, l < 0 ? 0u - (uint32_t)l : (uint32_t)l);
+    *p++ = '\n';
+    if ((size_t)(p - out.data()) >= kBlock) {
+      ok = std::fwrite(out.data(), 1, (size_t)(p - out.data()), f) == (size_t)(p - out.data());
+      p = out.data();
+    }
+  }
+  ok = ok && std::fwrite(out.data(), 1, (size_t)(p - out.data()), f) == (size_t)(p - out.data());
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? GB_OK : GB_ERR_IO;
+}
+
+// Edge list in the reference's text format ("n m", then "src dst" lines),
+// the input of read_edge (scc_main.cpp:94-125).
 extern "C" gb_status gb_write_text(const char* path, int32_t n, int64_t m, const int32_t* src,
                                    const int32_t* dst) {
   if (!path || n < 0 || m < 0 || (m > 0 && (!src || !dst))) return GB_ERR_INVALID;

@@ -173,6 +173,13 @@ def test_output_labels(tmp_path):
     p = tmp_path / "out.txt"
     gb.output_labels(str(p), np.array([0, 0, 2, -1], np.int32))
     assert p.read_text() == "0\n0\n2\n-1\n"
+    # more than one 1 MB block, and the int32 extremes
+    lab = np.random.default_rng(3).integers(-5, 1 << 31, 400_000).astype(np.int32)
+    lab[:3] = [np.iinfo(np.int32).min, np.iinfo(np.int32).max, 0]
+    gb.output_labels(str(p), lab)
+    assert p.read_text() == "".join(f"{x}\n" for x in lab.tolist())
+    gb.output_labels(str(p), np.zeros(0, np.int32))
+    assert p.read_text() == ""
 
 
 def test_verify_lines():
