@@ -112,6 +112,8 @@ _sig("gb_graph_rmat", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_doub
 _sig("gb_graph_rmat_n", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
                                     C.c_double, C.POINTER(_P)])
 _sig("gb_graph_info", C.c_int32, [_P, _I32P, _I64P, _I32P])
+_sig("gb_graph_set_hints", C.c_int32, [_P, _P, C.c_int32])
+_sig("gb_graph_has_hints", C.c_int32, [_P, _I32P])
 _sig("gb_graph_from_file2", C.c_int32, [_P, C.c_char_p, C.c_int32, C.POINTER(_P)])
 _sig("gb_write_binary", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
 _sig("gb_write_text", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
@@ -490,6 +492,16 @@ class Graph:
         _check(_lib.gb_graph_csr_to_host(self._h, _ptr(oo), _ptr(oa), _ptr(io), _ptr(ia)),
                "gb_graph_csr_to_host")
         return oo, oa, io, ia
+
+    def set_hints(self, ctx: Context, on: bool) -> None:
+        """Builds (on) or frees (off) the graph's pull hints."""
+        _check(_lib.gb_graph_set_hints(ctx._h, self._h, 1 if on else 0), "gb_graph_set_hints")
+
+    @property
+    def has_hints(self) -> bool:
+        v = C.c_int32()
+        _check(_lib.gb_graph_has_hints(self._h, C.byref(v)), "gb_graph_has_hints")
+        return bool(v.value)
 
     def device_csr(self) -> tuple[int, int, int, int]:
         ps = [C.c_void_p() for _ in range(4)]

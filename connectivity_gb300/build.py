@@ -5,7 +5,7 @@ compiled in parallel.  Outputs:
     connectivity_gb300/libgbconn.so
     connectivity_gb300/bin/scc, connectivity_gb300/bin/cc
     oracle/liboracle.so                (test infrastructure)
-    oracle/_ref/ref_scc, ref_cc        (only where the reference tree exists)
+    oracle/_ref/ref_scc, ref_cc        (only where the reference sources are installed)
 """
 from __future__ import annotations
 
@@ -89,17 +89,20 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
 
 
 def build_oracle(verbose: bool = False, force: bool = False) -> str:
-    """Test infrastructure: the C restatement, and the reference harness when
-    the reference tree is present."""
-    src = os.path.join(ORACLE, "multistep.c")
+    """Test infrastructure: the C restatement and its generator, and the
+    reference harness when the reference sources are installed
+    (oracle/install_ref.sh into baseline/_ref/multistep, or REF_DIR)."""
+    srcs = [os.path.join(ORACLE, "multistep.c"), os.path.join(ORACLE, "gen.c")]
     out = os.path.join(ORACLE, "liboracle.so")
-    if force or _newer(out, [src]):
-        _run(["gcc", "-O3", "-std=c11", "-fPIC", "-fopenmp", "-shared", "-Wall", src, "-o", out],
-             verbose)
+    if force or _newer(out, srcs):
+        _run(["gcc", "-O3", "-std=c11", "-fPIC", "-fopenmp", "-shared", "-Wall"] + srcs +
+             ["-o", out], verbose)
     ref = os.path.join(ORACLE, "build_ref.sh")
     ref_out = os.path.join(ORACLE, "_ref", "ref_scc")
-    if os.path.isdir(os.environ.get("REF_DIR", "/root/reference/multistep")) and (
-            force or _newer(ref_out, [os.path.join(ORACLE, "ref_harness.cpp"), ref])):
+    ref_dir = os.environ.get("REF_DIR", os.path.join(ROOT, "baseline", "_ref", "multistep"))
+    if os.path.isfile(os.path.join(ref_dir, "scc_main.cpp")) and (
+            force or _newer(ref_out, [os.path.join(ORACLE, "ref_harness.cpp"), ref,
+                                      os.path.join(ref_dir, "scc_main.cpp")])):
         _run(["sh", ref], verbose)
     return out
 

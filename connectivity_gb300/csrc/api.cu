@@ -156,8 +156,10 @@ void graph_free(gb_graph* g) {
 // Builds the pull hints of a graph whose CSR is complete on the device.
 gb_status graph_hints(gb_ctx* c, gb_graph* g) {
   const size_t hb = (size_t)(g->n > 0 ? g->n : 1) * 4;
-  CK(dev_alloc((void**)&g->hint_out, hb, g->pooled, g->pool_stream), "hint allocation");
-  if (!g->symmetric) CK(dev_alloc((void**)&g->hint_in, hb, g->pooled, g->pool_stream), "hint allocation");
+  if (!g->hint_out)
+    CK(dev_alloc((void**)&g->hint_out, hb, g->pooled, g->pool_stream), "hint allocation");
+  if (!g->symmetric && !g->hint_in)
+    CK(dev_alloc((void**)&g->hint_in, hb, g->pooled, g->pool_stream), "hint allocation");
   CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
                      c->stream),
      "hints");
@@ -809,6 +811,28 @@ gb_status gb_graph_destroy(gb_graph* g) {
   cudaSetDevice(g->device);
   graph_free(g);
   delete g;
+  return GB_OK;
+}
+
+gb_status gb_graph_set_hints(gb_ctx* c, gb_graph* g, int32_t on) {
+  if (!c || !g || (on != 0 && on != 1)) return GB_ERR_INVALID;
+  if (c->device != g->device) {
+    gb_set_error("gb_graph_set_hints: %s", "graph and context are on different devices");
+    return GB_ERR_INVALID;
+  }
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  // runs already queued on the context may still read the hints
+  CK(cudaStreamSynchronize(c->stream), "gb_graph_set_hints");
+  if (on) return graph_hints(c, g);
+  gb::dev_free(g->hint_out, g->pooled, g->pool_stream);
+  gb::dev_free(g->hint_in, g->pooled, g->pool_stream);
+  g->hint_out = g->hint_in = nullptr;
+  return GB_OK;
+}
+
+gb_status gb_graph_has_hints(const gb_graph* g, int32_t* on) {
+  if (!g || !on) return GB_ERR_INVALID;
+  *on = g->hint_out != nullptr;
   return GB_OK;
 }
 

@@ -248,28 +248,117 @@ __global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t*
   }
 }
 
-// One warp per vertex: the neighbour of largest degree, first one on ties.
+// The pull hint of a vertex: its neighbour of largest total degree, the
+// first one in adjacency order on ties (-1 without neighbours).  Vertices
+// are taken by degree:
+//   <= 32 neighbours: one thread, four neighbours' loads in flight at a time;
+//   <= 1024: the whole warp, one vertex after another (warp ballot);
+//   more: appended to `heavy` for k_hint_heavy (a block per vertex).
+// Most vertices of a power-law graph have a handful of neighbours, so a warp
+// per vertex (the simple form) leaves most lanes idle.
+constexpr int kHintThread = 32;
+constexpr int kHintWarp = 1024;
+
+__device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& best_d,
+                                            int64_t& best_e) {
+  if (d2 > best_d || (d2 == best_d && e2 >= 0 && (best_e < 0 || e2 < best_e))) {
+    best_d = d2;
+    best_e = e2;
+  }
+}
+
 __global__ void k_hint(int32_t n, const int64_t* off, const int32_t* adj, const int32_t* deg,
-                       int32_t* hint) {
+                       int32_t* hint, int32_t* heavy, int32_t* nheavy) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
+       base += stride) {
+    const int64_t v = base + lane;
+    int64_t s = 0, d = 0;
+    if (v < n) {
+      s = off[v];
+      d = off[v + 1] - s;
+    }
+    if (d <= kHintThread) {
+      int32_t best_d = -1;
+      int64_t best_e = -1;
+      for (int64_t e = 0; e < d; e += 4) {
+        const int32_t a0 = adj[s + e];
+        const int32_t a1 = e + 1 < d ? adj[s + e + 1] : -1;
+        const int32_t a2 = e + 2 < d ? adj[s + e + 2] : -1;
+        const int32_t a3 = e + 3 < d ? adj[s + e + 3] : -1;
+        const int32_t d0 = deg[a0];
+        const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
+        const int32_t d2 = a2 >= 0 ? deg[a2] : -1;
+        const int32_t d3 = a3 >= 0 ? deg[a3] : -1;
+        if (d0 > best_d) { best_d = d0; best_e = e; }
+        if (d1 > best_d) { best_d = d1; best_e = e + 1; }
+        if (d2 > best_d) { best_d = d2; best_e = e + 2; }
+        if (d3 > best_d) { best_d = d3; best_e = e + 3; }
+      }
+      if (v < n) hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
+    } else if (d > kHintWarp) {
+      heavy[atomicAdd(nheavy, 1)] = (int32_t)v;
+    }
+    unsigned mid = __ballot_sync(0xffffffffu, d > kHintThread && d <= kHintWarp);
+    while (mid) {
+      const int j = __ffs(mid) - 1;
+      mid &= mid - 1;
+      const int64_t sj = __shfl_sync(0xffffffffu, s, j);
+      const int64_t dj = __shfl_sync(0xffffffffu, d, j);
+      int32_t best_d = -1;
+      int64_t best_e = -1;
+      for (int64_t e = lane; e < dj; e += 32) {
+        const int32_t dd = deg[adj[sj + e]];
+        if (dd > best_d) { best_d = dd; best_e = e; }
+      }
+      for (int o = 16; o; o >>= 1) {
+        const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
+        const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
+        hint_better(d2, e2, best_d, best_e);
+      }
+      if (lane == 0) hint[base + j] = adj[sj + best_e];
+    }
+  }
+}
+
+// A block per heavy vertex (more than kHintWarp neighbours).
+__global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const int32_t* deg,
+                             int32_t* hint, const int32_t* heavy, const int32_t* nheavy) {
+  __shared__ int32_t sd[32];
+  __shared__ int64_t se[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nh = *nheavy;
+  for (int i = blockIdx.x; i < nh; i += gridDim.x) {
+    const int32_t v = heavy[i];
     const int64_t s = off[v], d = off[v + 1] - s;
     int32_t best_d = -1;
     int64_t best_e = -1;
-    for (int64_t e = lane; e < d; e += 32) {
+    for (int64_t e = threadIdx.x; e < d; e += blockDim.x) {
       const int32_t dd = deg[adj[s + e]];
       if (dd > best_d) { best_d = dd; best_e = e; }
     }
     for (int o = 16; o; o >>= 1) {
       const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
       const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
-      if (d2 > best_d || (d2 == best_d && e2 >= 0 && (best_e < 0 || e2 < best_e))) {
-        best_d = d2;
-        best_e = e2;
-      }
+      hint_better(d2, e2, best_d, best_e);
     }
-    if (lane == 0) hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
+    if (lane == 0) {
+      sd[wid] = best_d;
+      se[wid] = best_e;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      best_d = lane < (int)(blockDim.x >> 5) ? sd[lane] : -1;
+      best_e = lane < (int)(blockDim.x >> 5) ? se[lane] : -1;
+      for (int o = 16; o; o >>= 1) {
+        const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
+        const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
+        hint_better(d2, e2, best_d, best_e);
+      }
+      if (lane == 0) hint[v] = adj[s + best_e];
+    }
+    __syncthreads();
   }
 }
 
@@ -346,6 +435,12 @@ cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* a
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
+}
+
+cudaError_t check_csr_flag(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
+                           int* d_bad, cudaStream_t s) {
+  k_check_csr<<<grid_for((m > n ? m : n) + 1), 256, 0, s>>>(n, m, off, adj, d_bad);
+  return cudaGetLastError();
 }
 
 cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
@@ -498,14 +593,23 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  // scratch: total degrees (n), the heavy list (n) and two list counts
   int32_t* deg = nullptr;
-  cudaError_t e = cudaMallocAsync(&deg, (size_t)n * 4, s);
+  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 2 + 2) * 4, s);
   if (e != cudaSuccess) return e;
+  int32_t* heavy = deg + n;
+  int32_t* nheavy = heavy + n;
+  cudaMemsetAsync(nheavy, 0, 8, s);
   k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
-  const int warp_grid = grid_for((int64_t)n * 32);
-  k_hint<<<warp_grid, 256, 0, s>>>(n, out_off, out_adj, deg, hint_out);
-  if (in_off != nullptr && hint_in != nullptr)
-    k_hint<<<warp_grid, 256, 0, s>>>(n, in_off, in_adj, deg, hint_in);
+  const int g = grid_for(n);
+  k_hint<<<g, 256, 0, s>>>(n, out_off, out_adj, deg, hint_out, heavy, nheavy);
+  k_hint_heavy<<<152 * 2, 1024, 0, s>>>(out_off, out_adj, deg, hint_out, heavy, nheavy);
+  if (in_off != nullptr && hint_in != nullptr) {
+    // the in side reuses the heavy list with its own count; stream order
+    // puts it after the out side's heavy pass has read the list
+    k_hint<<<g, 256, 0, s>>>(n, in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
+    k_hint_heavy<<<152 * 2, 1024, 0, s>>>(in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
+  }
   cudaFreeAsync(deg, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -215,6 +215,10 @@ cudaError_t build_csr(int32_t n, int64_t m, const int32_t* d_src, const int32_t*
 // outside [0, n).  Synchronises the stream.
 cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
                       cudaStream_t s, int* bad);
+// As check_csr, without allocating: ORs 1 into *d_bad (device memory, left
+// as it is when the CSR is good) and does not wait.
+cudaError_t check_csr_flag(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
+                           int* d_bad, cudaStream_t s);
 // Reference pivot: kind 0 = lowest id maximising out*in (> 0), kind 1 =
 // lowest id maximising out (+ in when in_off != null).  -1 when none.
 // Synchronises the stream.

@@ -216,6 +216,13 @@ extern "C" gb_status gb_read_edge_pieces(const char* path, int32_t pieces, int32
     gb_set_error("gb_read_edge: bad header in %s", path);
     return GB_ERR_IO;
   }
+  // every edge takes at least 4 bytes of the body (a blank, an id, a blank,
+  // an id), so a header m above that cannot be met; checked before the
+  // arrays are sized from it
+  if (mm > (long long)((size_t)(base + size - c.p) / 4)) {
+    gb_set_error("gb_read_edge: fewer edges than the header says in %s", path);
+    return GB_ERR_IO;
+  }
   int32_t* s = (int32_t*)std::malloc((size_t)(mm > 0 ? mm : 1) * sizeof(int32_t));
   int32_t* d = (int32_t*)std::malloc((size_t)(mm > 0 ? mm : 1) * sizeof(int32_t));
   if (!s || !d) {

@@ -21,6 +21,13 @@
 //   - the first call on a device sets that device up (cudaGetSymbolAddress of
 //     the array, the kernels' shared-memory attribute and cooperative grid
 //     size); make that first call before any stream capture.
+//   - the CSR is checked on the device before the run (offsets from 0 to m,
+//     non-decreasing; ids in [0, n)), with the check's flag in the same
+//     array, and every pointer must be device memory of the current device:
+//     a bad CSR or a host pointer is GB_ERR_INVALID, and nothing runs on it.
+//   - with stream NULL (the legacy default stream) the call's work waits for,
+//     and holds up, the blocking streams of the device; a caller whose other
+//     threads capture CUDA graphs passes a non-blocking stream of its own.
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -40,8 +47,9 @@ constexpr size_t kArr = al256((size_t)(kNoAllocMaxVertices + 32) * 4);
 constexpr size_t kWords = (size_t)(kNoAllocMaxVertices + 32) / 32 + 2;
 constexpr size_t kBm = al256(kWords * 4);
 constexpr size_t kCtl = al256(sizeof(gb::Ctl));
-constexpr size_t kScratchBytes =
-    kCtl + 15 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) + al256(2 * kNoAllocMaxGrid * 8);
+constexpr size_t kCheck = 256;  // the CSR check's flag
+constexpr size_t kScratchBytes = kCtl + 15 * kArr + 4 * kBm + al256(2 * kNoAllocMaxGrid * 4) +
+                                 al256(2 * kNoAllocMaxGrid * 8) + kCheck;
 
 // The scratch.  Host code must not pass this name to a kernel: on the host
 // it is a stand-in symbol, not a device address; its device address comes
@@ -79,6 +87,18 @@ gb_status setup_device(int dev, DeviceSetup** out) {
   return GB_OK;
 }
 
+// Device memory of device dev (or managed memory): the only memory the run
+// kernels may be given.
+bool on_device(const void* p, int dev) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
 }  // namespace
 
 extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off,
@@ -99,6 +119,11 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     gb_set_error("gb_scc_noalloc: %s", e != cudaSuccess ? cudaGetErrorString(e) : "device index");
     return e == cudaErrorNoDevice ? GB_ERR_NO_DEVICE : GB_ERR_CUDA;
+  }
+  if (!on_device(out_off, dev) || !on_device(in_off, dev) || !on_device(labels, dev) ||
+      (m > 0 && (!on_device(out_adj, dev) || !on_device(in_adj, dev)))) {
+    gb_set_error("gb_scc_noalloc: %s", "CSR and labels must be device memory of the current device");
+    return GB_ERR_INVALID;
   }
   DeviceSetup* d = nullptr;
   gb_status st = setup_device(dev, &d);
@@ -136,12 +161,30 @@ extern "C" gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off
   w.done = (uint32_t*)take(kBm);
   w.blk_i = (int32_t*)take(al256(2 * kNoAllocMaxGrid * 4));
   w.blk_l = (long long*)take(al256(2 * kNoAllocMaxGrid * 8));
+  int* d_bad = (int*)take(kCheck);
   w.ctl = ctl;
   w.n = n;
   w.nwords = (n + 31) / 32;
   w.m = m;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the caller's CSR is checked before any kernel indexes through it
+  static thread_local int h_bad;
+  h_bad = 0;
+  if ((e = cudaMemsetAsync(d_bad, 0, sizeof(int), s)) != cudaSuccess ||
+      (e = gb::check_csr_flag(n, m, out_off, out_adj, d_bad, s)) != cudaSuccess ||
+      (e = gb::check_csr_flag(n, m, in_off, in_adj, d_bad, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&h_bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    gb_set_error("gb_scc_noalloc: %s", cudaGetErrorString(e));
+    return GB_ERR_CUDA;
+  }
+  if (h_bad != 0) {
+    gb_set_error("gb_scc_noalloc: %s",
+                 "CSR check failed: offsets not monotone from 0 to m, or an id outside [0, n)");
+    return GB_ERR_INVALID;
+  }
   // state that must start cleared (the array keeps the previous call's)
   if ((e = cudaMemsetAsync(ctl, 0, sizeof(gb::Ctl), s)) != cudaSuccess ||
       (e = cudaMemsetAsync(w.fvis, 0, (size_t)w.nwords * 4, s)) != cudaSuccess ||

@@ -232,6 +232,17 @@ gb_status gb_graph_device_csr(const gb_graph* g, const int64_t** out_off,
 gb_status gb_graph_pivot(gb_ctx* ctx, const gb_graph* g, int32_t kind, int32_t* pivot,
                          double* avg_degree);
 gb_status gb_graph_destroy(gb_graph* g);
+/* Pull hints: per vertex and direction, the neighbour of largest total
+ * degree (first in adjacency order on ties), an index derived from the CSR
+ * that lets a pull step settle most candidates with one lookup.  Every
+ * gb_graph_from_* / gb_graph_rmat* call builds them (n int32 per direction);
+ * on = 0 frees them and runs then scan in-edges only, on = 1 (re)builds
+ * them.  Labels do not depend on them.  No reference counterpart: the
+ * reference's create_csr (scc_main.cpp:127-191) computes the pivot and the
+ * average degree only, and its pull step (scc_fwbw.cpp:116-149) scans
+ * in-edges.  Waits for the context's queued work first. */
+gb_status gb_graph_set_hints(gb_ctx* ctx, gb_graph* g, int32_t on);
+gb_status gb_graph_has_hints(const gb_graph* g, int32_t* on);
 
 /* ---- runs ------------------------------------------------------------- */
 /* run_scc (multistep/scc_main.cpp:210-317): trim, FW-BW from the pivot,
@@ -261,10 +272,16 @@ gb_status gb_wcc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, cons
  * entries, canonical minimum member ids) are device memory owned by the
  * caller; the work goes on `stream` (NULL: the legacy default stream) and
  * the call returns after it completes.  At most 262144 vertices (more:
- * GB_ERR_CAPACITY, nothing queued).  All calls share the scratch: calls that
- * overlap on the GPU race and must be serialised.  The first call on a
- * device sets that device up (symbol address, kernel attributes); make it
- * before any stream capture. */
+ * GB_ERR_CAPACITY, nothing queued).  The five arrays must be device memory
+ * of the current device, and the CSR is checked on the device before the run
+ * (off[0] = 0, off[n] = m, offsets non-decreasing, ids in [0, n)); a failure
+ * of either is GB_ERR_INVALID and nothing runs on the arrays.  All calls
+ * share the scratch: calls that overlap on the GPU race and must be
+ * serialised.  The first call on a device sets that device up (symbol
+ * address, kernel attributes); make it before any stream capture.  With
+ * stream NULL the work goes on the legacy default stream, which waits for
+ * and holds up the device's blocking streams: a caller whose other threads
+ * capture CUDA graphs passes a non-blocking stream of its own. */
 gb_status gb_scc_noalloc(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
                          const int64_t* in_off, const int32_t* in_adj, int32_t* labels,
                          void* stream);

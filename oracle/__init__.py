@@ -58,12 +58,42 @@ def lib():
         L.orc_scc_tarjan.argtypes = [C.POINTER(Graph), P]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_rmat_edges.argtypes = [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                     C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_void_p),
+                                     C.POINTER(C.c_void_p)]
+        L.orc_rmat_edges.restype = C.c_int
+        L.orc_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def rmat_edges_n(n: int, edge_factor: int, seed: int,
+                 abc: tuple[float, float, float] = (0.57, 0.19, 0.19)):
+    """Seeded R-MAT edge list (oracle/gen.c): the product generator's edges,
+    built independently of it.  Returns (n, src, dst), sorted by (src, dst)."""
+    m = C.c_int64()
+    s, d = C.c_void_p(), C.c_void_p()
+    if lib().orc_rmat_edges(n, edge_factor, seed, abc[0], abc[1], abc[2], C.byref(m),
+                            C.byref(s), C.byref(d)) != 0:
+        raise MemoryError("orc_rmat_edges failed")
+    out = []
+    for p in (s, d):
+        a = np.empty(m.value, np.int32)
+        if m.value:
+            C.memmove(a.ctypes.data, p, m.value * 4)
+        lib().orc_free(p)
+        out.append(a)
+    return n, out[0], out[1]
+
+
+def rmat_edges(scale: int, edge_factor: int = 16, seed: int = 1,
+               abc: tuple[float, float, float] = (0.57, 0.19, 0.19)):
+    """R-MAT with 2^scale vertices (see rmat_edges_n)."""
+    return rmat_edges_n(1 << scale, edge_factor, seed, abc)
 
 
 def build_csr(n: int, src: np.ndarray, dst: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -190,6 +220,14 @@ def ref_run(kind: str, n: int, src: np.ndarray, dst: np.ndarray, reps: int = 1,
             threads: int | None = None) -> tuple[np.ndarray, str, float]:
     """Runs the reference's run_scc / run_cc through the harness.  Returns
     (labels as produced, verify line, best time in seconds)."""
+    lab, line, times = ref_run_times(kind, n, src, dst, reps, threads)
+    return lab, line, min(times)
+
+
+def ref_run_times(kind: str, n: int, src: np.ndarray, dst: np.ndarray, reps: int = 1,
+                  threads: int | None = None) -> tuple[np.ndarray, str, list[float]]:
+    """As ref_run, with the time of every rep (seconds, in order): the CSR is
+    built once and run_scc / run_cc runs reps times on it."""
     exe = REF_SCC if kind == "scc" else REF_CC
     env = dict(os.environ)
     if threads:
@@ -201,8 +239,44 @@ def ref_run(kind: str, n: int, src: np.ndarray, dst: np.ndarray, reps: int = 1,
                            env=env, check=True)
         lab = np.fromfile(lb, dtype=np.int32)
     lines = r.stdout.splitlines()
-    t = float(lines[0].split(":")[1])
-    return lab, lines[1] + "\n", t
+    times = [float(x) for x in lines[2].split(":")[1].split()] if len(lines) > 2 else \
+        [float(lines[0].split(":")[1])]
+    return lab, lines[1] + "\n", times
+
+
+def ref_batch(kind: str, graphs, mode: str = "seq", threads: int | None = None, exe_dir=None):
+    """The reference's run_scc / run_cc once per graph of a batch, in one
+    process (the harness's --batch mode).  graphs: (n, src, dst) with local
+    ids.  mode "seq": one graph after another, each with all threads; "par":
+    one thread per graph over all threads.  Returns (labels per graph as
+    produced, seconds of the whole loop, seconds per graph or None)."""
+    d0 = exe_dir or os.path.join(HERE, "_ref")
+    exe = os.path.join(d0, "ref_scc" if kind == "scc" else "ref_cc")
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    with tempfile.TemporaryDirectory() as d:
+        gb_, lb = os.path.join(d, "g.bin"), os.path.join(d, "l.bin")
+        with open(gb_, "wb") as f:
+            np.array([len(graphs)], np.int64).tofile(f)
+            for n, s, t in graphs:
+                np.array([n, len(s)], np.int64).tofile(f)
+                np.ascontiguousarray(s, np.int32).tofile(f)
+                np.ascontiguousarray(t, np.int32).tofile(f)
+        r = subprocess.run([exe, "--batch", gb_, lb, mode], capture_output=True, text=True,
+                           env=env, check=True)
+        flat = np.fromfile(lb, dtype=np.int32)
+    out, at = [], 0
+    for n, _, _ in graphs:
+        out.append(flat[at:at + n])
+        at += n
+    total, per = None, None
+    for line in r.stdout.splitlines():
+        if line.startswith("batch_seconds:"):
+            total = float(line.split(":")[1])
+        elif line.startswith("graph_seconds:"):
+            per = [float(x) for x in line.split(":")[1].split()]
+    return out, total, per
 
 
 def ref_text(kind: str, graph_path: str) -> tuple[np.ndarray, str]:

@@ -1,14 +1,19 @@
 #!/bin/sh
 # Builds the unmodified reference Multistep code (HPCGraphAnalysis/Connectivity
 # multistep/) into oracle/_ref/ through oracle/ref_harness.cpp.
-# Test infrastructure only; needs the reference tree (default location below,
-# or REF_DIR=...).  Nothing is written outside oracle/_ref/.
+#
+# Test infrastructure only.  The sources are read from $REF_DIR when it is
+# set, else from baseline/_ref/multistep, the git-ignored reference install
+# that oracle/install_ref.sh makes (an unmodified copy of the reference's
+# multistep/ directory, which travels with the working tree to machines that
+# do not hold the reference).  Nothing is written outside oracle/_ref/.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF_DIR=${REF_DIR:-/root/reference/multistep}
+ROOT=$(dirname "$HERE")
+REF_DIR=${REF_DIR:-$ROOT/baseline/_ref/multistep}
 OUT="$HERE/_ref"
 if [ ! -f "$REF_DIR/scc_main.cpp" ]; then
-  echo "reference not found at $REF_DIR; oracle/_ref not built" >&2
+  echo "reference sources not found at $REF_DIR; oracle/_ref not built" >&2
   exit 0
 fi
 mkdir -p "$OUT"

@@ -21,27 +21,48 @@
 // Usage:
 //   ref_scc --text <graph> [out]       the reference main, unchanged
 //   ref_scc --bin <edges.bin> <labels.bin> [reps]
+//   ref_scc --batch <graphs.bin> <labels.bin> seq|par
 // edges.bin: int64 n, int64 m, int32 src[m], int32 dst[m] (directed edges).
 // labels.bin receives int32 labels[n].  Prints the reference's own stdout
-// lines ("Multistep SCC time: ..." / verify line), time = best of reps.
+// lines ("Multistep SCC time: ..." / verify line), time = best of reps, then
+// one more line, "rep_seconds: t1 t2 ...", the time of every rep in order.
+//
+// --batch runs many independent graphs, the reference's equivalent of a
+// batched run: a loop of run_scc / run_cc calls, one per graph.
+// graphs.bin: int64 count, then per graph int64 n, int64 m, int32 src[m],
+// int32 dst[m] (local ids).  "seq": the graphs one after another, each run
+// with all OpenMP threads (the reference as it is); "par": one thread per
+// graph, the graphs spread over all threads (an OpenMP loop over the graphs,
+// whose nested parallel regions then run on one thread).  Prints
+// "batch_seconds: T" (the whole loop) and, for seq, "graph_seconds: t1 ...";
+// labels.bin receives the graphs' labels one after another.  The CSRs are
+// built before the timed loop, as read_edge/create_csr are outside the
+// reference's timer.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <cstdint>
 #include <new>
+#include <vector>
 
 static long long g_fill_bytes = -1;   // allocation size that gets the fill
 static int g_fill_value = 0;          // int pattern written into it
+// per-thread setting, used instead of the global one while it is set (the
+// batch mode's graph-parallel loop runs a different graph on every thread)
+static thread_local long long t_fill_bytes = -1;
+static thread_local int t_fill_value = 0;
 
 void* operator new[](std::size_t sz) {
   void* p = std::malloc(sz ? sz : 1);
   if (!p) throw std::bad_alloc();
-  if (g_fill_bytes >= 0 && (long long)sz == g_fill_bytes) {
-    if (g_fill_value == 0 || sz % sizeof(int) != 0) {
+  const long long fb = t_fill_bytes >= 0 ? t_fill_bytes : g_fill_bytes;
+  const int fv = t_fill_bytes >= 0 ? t_fill_value : g_fill_value;
+  if (fb >= 0 && (long long)sz == fb) {
+    if (fv == 0 || sz % sizeof(int) != 0) {
       std::memset(p, 0, sz);
     } else {
       int* q = static_cast<int*>(p);
-      for (std::size_t i = 0; i < sz / sizeof(int); ++i) q[i] = g_fill_value;
+      for (std::size_t i = 0; i < sz / sizeof(int); ++i) q[i] = fv;
     }
   }
   return p;
@@ -90,8 +111,110 @@ static int read_bin(const char* path, int& n, unsigned& m, int*& srcs, int*& dst
   return 0;
 }
 
+struct BatchGraph {
+  int n = 0;
+  unsigned m = 0;
+  int* out_array = nullptr;
+  unsigned* odl = nullptr;
+#if !defined(REF_CC)
+  int* in_array = nullptr;
+  unsigned* idl = nullptr;
+#endif
+  int root = 0;
+  double avg = 0.0;
+  int* maps = nullptr;
+};
+
+// One graph of the batch: its CSR as create_csr builds it, and the pivot.
+static void batch_prepare(BatchGraph& b, int n, unsigned long long mm, const int* s,
+                          const int* d) {
+  b.n = n;
+#if defined(REF_CC)
+  b.m = (unsigned)(2 * mm);   // read_edge mirrors every edge (cc_main.cpp:102-118)
+  int* srcs = new int[b.m ? b.m : 1];
+  int* dsts = new int[b.m ? b.m : 1];
+  for (unsigned long long i = 0; i < mm; ++i) {
+    srcs[2 * i] = s[i]; dsts[2 * i] = d[i];
+    srcs[2 * i + 1] = d[i]; dsts[2 * i + 1] = s[i];
+  }
+  create_csr(n, b.m, srcs, dsts, b.out_array, b.odl, b.root, b.avg);
+#else
+  b.m = (unsigned)mm;
+  int* srcs = new int[b.m ? b.m : 1];
+  int* dsts = new int[b.m ? b.m : 1];
+  std::memcpy(srcs, s, mm * sizeof(int));
+  std::memcpy(dsts, d, mm * sizeof(int));
+  b.root = -1;
+  create_csr(n, b.m, srcs, dsts, b.out_array, b.in_array, b.odl, b.idl, b.root, b.avg);
+  if (b.root < 0) b.root = 0;   // no degree product > 0 (see the --bin path)
+#endif
+  delete[] srcs;
+  delete[] dsts;
+}
+
+static void batch_run(BatchGraph& b) {
+#if defined(REF_CC)
+  t_fill_bytes = (long long)b.n * (long long)sizeof(int);
+  t_fill_value = b.root;
+  graph g = {b.n, b.m, b.out_array, b.odl};
+  run_cc(g, b.maps, b.root, b.avg);
+#else
+  t_fill_bytes = b.n;
+  t_fill_value = 0;
+  graph g = {b.n, b.m, b.out_array, b.in_array, b.odl, b.idl};
+  run_scc(g, b.maps, b.root, b.avg, 10000);
+#endif
+  t_fill_bytes = -1;
+}
+
+static int batch_main(const char* in_path, const char* out_path, bool par) {
+  FILE* f = std::fopen(in_path, "rb");
+  if (!f) return 1;
+  long long count = 0;
+  if (std::fread(&count, sizeof(long long), 1, f) != 1 || count < 0) { std::fclose(f); return 1; }
+  BatchGraph* gs = new BatchGraph[count > 0 ? count : 1];
+  std::vector<int> s, d;
+  for (long long i = 0; i < count; ++i) {
+    long long hdr[2];
+    if (std::fread(hdr, sizeof(long long), 2, f) != 2) { std::fclose(f); return 1; }
+    const unsigned long long mm = (unsigned long long)hdr[1];
+    s.resize(mm + 1);
+    d.resize(mm + 1);
+    if (std::fread(s.data(), sizeof(int), mm, f) != mm ||
+        std::fread(d.data(), sizeof(int), mm, f) != mm) { std::fclose(f); return 1; }
+    batch_prepare(gs[i], (int)hdr[0], mm, s.data(), d.data());
+  }
+  std::fclose(f);
+  double* per = new double[count > 0 ? count : 1];
+  double t = timer();
+  if (par) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long i = 0; i < count; ++i) batch_run(gs[i]);
+  } else {
+    for (long long i = 0; i < count; ++i) {
+      double ti = timer();
+      batch_run(gs[i]);
+      per[i] = timer() - ti;
+    }
+  }
+  t = timer() - t;
+  std::printf("batch_seconds: %.6f\n", t);
+  if (!par) {
+    std::printf("graph_seconds:");
+    for (long long i = 0; i < count; ++i) std::printf(" %.6f", per[i]);
+    std::printf("\n");
+  }
+  FILE* o = std::fopen(out_path, "wb");
+  if (!o) return 1;
+  for (long long i = 0; i < count; ++i) std::fwrite(gs[i].maps, sizeof(int), (size_t)gs[i].n, o);
+  std::fclose(o);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   setbuf(stdout, NULL);
+  if (argc >= 5 && std::strcmp(argv[1], "--batch") == 0)
+    return batch_main(argv[2], argv[3], std::strcmp(argv[4], "par") == 0);
   if (argc >= 3 && std::strcmp(argv[1], "--text") == 0) {
 #if defined(REF_CC)
     // the text path cannot know the root before create_csr; the fill is the
@@ -119,7 +242,8 @@ int main(int argc, char** argv) {
     return ref_main(argc >= 4 ? 3 : 2, args);
   }
   if (argc < 4 || std::strcmp(argv[1], "--bin") != 0) {
-    std::printf("Usage: %s --text <graph> [out] | --bin <edges.bin> <labels.bin> [reps]\n", argv[0]);
+    std::printf("Usage: %s --text <graph> [out] | --bin <edges.bin> <labels.bin> [reps] | "
+                "--batch <graphs.bin> <labels.bin> seq|par\n", argv[0]);
     return 2;
   }
   int reps = argc >= 5 ? std::atoi(argv[4]) : 1;
@@ -127,6 +251,7 @@ int main(int argc, char** argv) {
   int n; unsigned m; int *srcs, *dsts;
   if (read_bin(argv[2], n, m, srcs, dsts)) { std::printf("cannot read %s\n", argv[2]); return 1; }
   double best = 1e30;
+  double* rep_t = new double[reps];
   int* maps = nullptr;
 #if defined(REF_CC)
   int* out_array; unsigned* odl; int root = 0; double avg;
@@ -140,6 +265,7 @@ int main(int argc, char** argv) {
     run_cc(g, maps, root, avg);
     t = timer() - t;
     g_fill_bytes = -1;
+    rep_t[r] = t;
     if (t < best) best = t;
   }
   std::printf("Multistep CC time: %9.6lf\n", best);
@@ -159,11 +285,16 @@ int main(int argc, char** argv) {
     run_scc(g, maps, root, avg, 10000);
     t = timer() - t;
     g_fill_bytes = -1;
+    rep_t[r] = t;
     if (t < best) best = t;
   }
   std::printf("Multistep SCC time: %9.6lf\n", best);
   scc_verify(g, maps);
 #endif
+  std::printf("rep_seconds:");
+  for (int r = 0; r < reps; ++r) std::printf(" %.6f", rep_t[r]);
+  std::printf("\n");
+  delete[] rep_t;
   FILE* f = std::fopen(argv[3], "wb");
   if (!f) return 1;
   std::fwrite(maps, sizeof(int), (size_t)n, f);

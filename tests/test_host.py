@@ -87,6 +87,13 @@ def test_read_edge_and_errors(tmp_path):
     with pytest.raises(gb.GBError) as e:
         gb.read_edge(str(tmp_path / "missing.txt"))
     assert e.value.status == 6
+    # a header m that the file cannot hold is refused before any array is
+    # sized from it (2^62 * 4 bytes would wrap to 0)
+    for m in (1 << 62, (1 << 62) - 1, 1 << 40, 1000):
+        p.write_text(f"4 {m}\n0 1\n1 2\n")
+        with pytest.raises(gb.GBError) as e:
+            gb.read_edge(str(p))
+        assert e.value.status == 6
 
 
 def _seq_read(text):
@@ -115,6 +122,10 @@ def _seq_read(text):
 
     nn, mm = num(), num()
     if nn is None or mm is None or nn < 0 or nn > 0x7FFFFFFF or mm < 0:
+        return 6, None, None, None
+    # every edge takes at least 4 bytes of the body: a larger m is refused
+    # before the body is read
+    if mm > (len(text) - pos[0]) // 4:
         return 6, None, None, None
     src, dst = [], []
     for _ in range(mm):

@@ -135,3 +135,59 @@ def test_oracle_random_graphs_against_scipy(seed):
     _, lab = csg.connected_components(a, directed=True, connection="weak")
     assert np.array_equal(oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)),
                           oracle.canonical(lab.astype(np.int32)))
+
+
+@pytest.mark.parametrize("n,ef,seed", [(1 << 10, 16, 1), (1 << 14, 16, 1), (3000, 7, 5), (64, 4, 9),
+                                       (1 << 16, 16, 1)])
+def test_oracle_generator_equals_product_generator(n, ef, seed):
+    """oracle/gen.c (bucketed by source, per-bucket sort) gives the product
+    generator's R-MAT edge list (64-bit key radix sort), so the reference arm
+    of the benchmark runs the same graph without loading the product."""
+    a = oracle.rmat_edges_n(n, ef, seed)
+    b = gb.rmat_edges_n(n, ef, seed)
+    assert digest(*a) == digest(*b)
+
+
+def test_pins_cover_the_full_size_workloads():
+    """tests/golden/pins.json holds the reference's label digests and verify
+    lines for the full-size workloads; the generators still give the pinned
+    edge lists where that is cheap to check."""
+    pins = json.load(open(os.path.join(GOLD, "pins.json")))
+    for key in ("rmat_s20_ef16_seed1", "rmat_s22_ef16_seed1", "rmat_s24_ef16_seed1",
+                "grid_1024_seed2", "grid_2048_seed2"):
+        assert key in pins, key
+        e = pins[key]
+        for f in ("edges", "scc_labels", "cc_labels", "scc_verify", "cc_verify"):
+            assert f in e, (key, f)
+        assert e["scc_verify"].endswith("Unassigned 0\n")
+    n, s, d = oracle.rmat_edges(20, 16, 1)
+    assert digest(n, s, d) == pins["rmat_s20_ef16_seed1"]["edges"]
+    n, s, d = gb.grid_edges(1024, 1024 * 1024 // 10, 64, 2)
+    assert digest(n, s, d) == pins["grid_1024_seed2"]["edges"]
+    # the oracle gives the pinned labels at these two sizes
+    import hashlib
+
+    def lab_digest(x):
+        return hashlib.sha256(np.ascontiguousarray(x, "<i4").tobytes()).hexdigest()
+    n, s, d = oracle.rmat_edges(20, 16, 1)
+    assert lab_digest(oracle.scc(oracle.CpuGraph(n, s, d))) == \
+        pins["rmat_s20_ef16_seed1"]["scc_labels"]
+    assert lab_digest(oracle.cc(oracle.CpuGraph(n, s, d, mirror=True))) == \
+        pins["rmat_s20_ef16_seed1"]["cc_labels"]
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference not built")
+@pytest.mark.parametrize("mode", ["seq", "par"])
+def test_reference_batch_mode(mode):
+    """The harness's batch mode (a loop of run_scc / run_cc over many graphs,
+    or one thread per graph) gives every graph's own labels."""
+    gs = [(n, s, d) for _, n, s, d in graphs.edge_cases()]
+    gs += [oracle.rmat_edges_n(n, ef, seed) for n, ef, seed in [(3000, 8, 1), (700, 4, 3)]]
+    for kind in ("scc", "cc"):
+        labs, total, per = oracle.ref_batch(kind, gs, mode, threads=2)
+        assert total is not None and total >= 0
+        assert (per is not None) == (mode == "seq")
+        for (n, s, d), lab in zip(gs, labs):
+            want = (oracle.scc(oracle.CpuGraph(n, s, d)) if kind == "scc"
+                    else oracle.cc(oracle.CpuGraph(n, s, d, mirror=True)))
+            assert np.array_equal(oracle.canonical(lab), want)
