@@ -352,13 +352,24 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # sections of the GPU arm
 # ---------------------------------------------------------------------------
-def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu):
+def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu, ws=1, rank=0):
     """graphs/s of one batched SCC run over BATCH_COUNT resident graphs,
     against back-to-back per-graph runs of a sample of the same graphs, and
-    against the reference's loop of run_scc over a sample."""
+    against the reference's loop of run_scc over a sample.  Under torchrun
+    the batch is sharded over the ranks (one GPU each, no collective): every
+    rank runs the union of its own graphs, and the job's graphs/s is the
+    whole batch over the slowest rank's time."""
     import numpy as np
     import torch
     ns, efs, seeds = gb.batch_sizes(BATCH_COUNT, **BATCH_DIST)
+    shard_info = None
+    if ws > 1:
+        from connectivity_gb300 import shard
+        of, load = shard.plan(shard.graph_costs(ns, ns.astype(np.int64) * efs), ws)
+        idx = shard.members(of, rank)
+        ns, efs, seeds = ns[idx], efs[idx], seeds[idx]
+        shard_info = {"shards": ws, "plan": "gb_shard_plan on vertices + edge-factor x vertices",
+                      "max_over_mean_load": round(float(load.max() / load.mean()), 4)}
     t0 = time.time()
     b = gb.Batch.rmat(ctx, ns, efs, seeds)
     build_s = time.time() - t0
@@ -376,7 +387,7 @@ def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu):
     e1.record(stream)
     torch.cuda.synchronize()
     ctx.sync()
-    t_scc = e0.elapsed_time(e1) / 1e3 / K
+    t_scc = dist_max(e0.elapsed_time(e1) / 1e3 / K)
     batch_lab = labels[:b.n].cpu().numpy()
     wl = torch.empty_like(labels)
     ctx.batch_wcc(b, labels=wl.data_ptr())
@@ -408,15 +419,17 @@ def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu):
     from connectivity_gb300 import tune as gbtune
     tuned = gbtune.tune_batch(ctx, b, 0, reps=2)
     out = {
-        "workload": (f"{b.count:,} R-MAT graphs, vertex counts log-normal (median 2,000, sigma "
-                     f"1.5, clipped 64..500,000), edge factor uniform 4..32 ({b.n:,} vertices, "
-                     f"{b.m:,} edges), one disjoint-union CSR resident in HBM"),
-        "graphs_per_s": round(b.count / t_scc, 1), "ms_per_batch": round(t_scc * 1e3, 3),
+        "workload": (f"{BATCH_COUNT:,} R-MAT graphs, vertex counts log-normal (median 2,000, "
+                     f"sigma 1.5, clipped 64..500,000), edge factor uniform 4..32 ({b.n:,} "
+                     f"vertices, {b.m:,} edges on this rank), one disjoint-union CSR resident "
+                     "in HBM"),
+        "graphs_per_s": round(BATCH_COUNT / t_scc, 1), "ms_per_batch": round(t_scc * 1e3, 3),
+        "sharded": shard_info,
         "steps": K, "gteps": round(b.m / t_scc / 1e9, 2),
         "wcc_graphs_per_s": round(b.count / t_wcc, 1),
         "per_graph_graphs_per_s": round(S / t_alone, 1),
         "per_graph_sample": f"first {S} graphs of the batch, resident, gb_scc_async back to back",
-        "speedup_vs_per_graph": round((b.count / t_scc) / (S / t_alone), 1),
+        "speedup_vs_per_graph": round((BATCH_COUNT / t_scc) / (S / t_alone) / ws, 1),
         "labels_equal_per_graph_runs": bool(same), "build_s": round(build_s, 2),
         "autotuned": {"graphs_per_s": round(b.count / (tuned["ms"] / 1e3), 1),
                       "defaults_graphs_per_s": round(b.count / (tuned["default_ms"] / 1e3), 1),
@@ -919,7 +932,8 @@ def run_gbconn(args):
     if "grid" in sections:
         line["grid"] = grid_section(gb, ctx, side=args.grid_side)
     if "batched" in sections:
-        line["batched"] = batched_section(gb, ctx, stream, 5, args.batch_cpu_sample, want_cpu)
+        line["batched"] = batched_section(gb, ctx, stream, 5, args.batch_cpu_sample, want_cpu,
+                                          ws, rank)
     ctx.close()
     if "served" in sections:
         rates = [r if r == "max" else float(r) for r in args.serve_rates.split(",") if r]

@@ -326,6 +326,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
+        self.device = device
         _check(_lib.gb_ctx_create(device, C.byref(self._h)), "gb_ctx_create")
 
     def close(self) -> None:

@@ -627,3 +627,33 @@ extern "C" gb_status gb_batch_sizes(int32_t count, uint64_t seed, double median,
   }
   return GB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Sharding a batch over devices
+// ---------------------------------------------------------------------------
+// Longest-processing-time-first: graphs in decreasing cost (ties: lower
+// index first) each go to the shard with the least load so far (ties: lower
+// shard).  The largest shard's load is at most the mean load plus the
+// largest single cost.  Deterministic, so every rank of a job computes the
+// same plan without communicating.
+extern "C" gb_status gb_shard_plan(int32_t count, const int64_t* cost, int32_t shards,
+                                   int32_t* shard_of, int64_t* load) {
+  if (count < 0 || shards < 1 || (count > 0 && (!cost || !shard_of))) return GB_ERR_INVALID;
+  for (int32_t i = 0; i < count; ++i)
+    if (cost[i] < 0) return GB_ERR_INVALID;
+  std::vector<int32_t> order((size_t)count);
+  for (int32_t i = 0; i < count; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+  std::vector<int64_t> acc((size_t)shards, 0);
+  for (int32_t i : order) {
+    int32_t best = 0;
+    for (int32_t s = 1; s < shards; ++s)
+      if (acc[(size_t)s] < acc[(size_t)best]) best = s;
+    shard_of[i] = best;
+    acc[(size_t)best] += cost[i];
+  }
+  if (load)
+    for (int32_t s = 0; s < shards; ++s) load[s] = acc[(size_t)s];
+  return GB_OK;
+}

@@ -317,6 +317,17 @@ gb_status gb_batch_wcc(gb_ctx* ctx, const gb_batch* b, int32_t* labels, const gb
 gb_status gb_batch_scc_async(gb_ctx* ctx, const gb_batch* b, int32_t* labels_dev,
                              const gb_opts* opts);
 gb_status gb_batch_destroy(gb_batch* b);
+/* Sharding a batch over devices (one context per device, each running the
+ * union of its graphs; graphs are independent, so no data moves between
+ * shards until the labels are gathered on the host).  cost[g] is graph g's
+ * work (vertices + edges is a fair measure); shard_of[g] receives its shard
+ * and load[s] (or NULL) each shard's total cost.  Largest cost first, each to
+ * the least loaded shard: the heaviest shard is within one graph's cost of
+ * the mean, and the plan is deterministic, so every rank of a job computes
+ * the same one.  No reference counterpart (the reference runs graphs one
+ * after another, multistep/scc_main.cpp:210). */
+gb_status gb_shard_plan(int32_t count, const int64_t* cost, int32_t shards, int32_t* shard_of,
+                        int64_t* load);
 
 /* ---- autotuner ---------------------------------------------------------- */
 /* No counterpart in the reference (its switch constants are fixed,

@@ -80,3 +80,22 @@ def test_batch_device_labels_async(ctx):
     ctx.sync()
     assert np.array_equal(out.cpu().numpy(), want)
     b.close()
+
+
+def test_sharded_batch_on_two_contexts_equals_one_batch(ctx):
+    """Two shards as two contexts on one GPU (run one after the other): every
+    graph's labels equal the single batch's and the oracle's."""
+    from connectivity_gb300 import shard
+    ns, efs, seeds = gb.batch_sizes(300, median=1500.0, n_max=60000)
+    graphs = [gb.rmat_edges_n(int(n), int(e), int(s)) for n, e, s in zip(ns, efs, seeds)]
+    whole = shard.run_shard(ctx, graphs, 0)
+    c2 = [gb.Context(0), gb.Context(0)]
+    parts = shard.run_sharded(c2, graphs, 0)
+    wparts = shard.run_sharded(c2, graphs, 1)
+    for c in c2:
+        c.close()
+    for i, g in enumerate(graphs):
+        assert np.array_equal(parts[i], whole[i])
+        if i % 10 == 0:
+            assert np.array_equal(parts[i], oracle.scc(oracle.CpuGraph(*g)))
+            assert np.array_equal(wparts[i], oracle.cc(oracle.CpuGraph(*g, mirror=True)))

@@ -81,4 +81,5 @@ def test_executable_reports_a_bad_file(tmp_path):
     r = subprocess.run([os.path.join(BIN, "scc"), str(p)], capture_output=True, text=True,
                        timeout=120)
     assert r.returncode != 0
-    assert "GB_ERR_INVALID" in r.stderr
+    # gb_status_string(GB_ERR_INVALID) and the reader's detail
+    assert "invalid argument" in r.stderr and "[0, n)" in r.stderr
