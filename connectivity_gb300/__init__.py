@@ -114,6 +114,7 @@ _sig("gb_graph_rmat_n", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_do
 _sig("gb_graph_info", C.c_int32, [_P, _I32P, _I64P, _I32P])
 _sig("gb_graph_set_hints", C.c_int32, [_P, _P, C.c_int32])
 _sig("gb_graph_has_hints", C.c_int32, [_P, _I32P])
+_sig("gb_graph_hints_to_host", C.c_int32, [_P, _P, _P])
 _sig("gb_graph_from_file2", C.c_int32, [_P, C.c_char_p, C.c_int32, C.POINTER(_P)])
 _sig("gb_write_binary", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
 _sig("gb_write_text", C.c_int32, [C.c_char_p, C.c_int32, C.c_int64, _P, _P])
@@ -497,6 +498,13 @@ class Graph:
     def set_hints(self, ctx: Context, on: bool) -> None:
         """Builds (on) or frees (off) the graph's pull hints."""
         _check(_lib.gb_graph_set_hints(ctx._h, self._h, 1 if on else 0), "gb_graph_set_hints")
+
+    def hints(self) -> tuple[np.ndarray, np.ndarray | None]:
+        """The pull hints (out side, in side) on the host."""
+        ho = np.empty(self.n, np.int32)
+        hi = None if self.symmetric else np.empty(self.n, np.int32)
+        _check(_lib.gb_graph_hints_to_host(self._h, _ptr(ho), _ptr(hi)), "gb_graph_hints_to_host")
+        return ho, hi
 
     @property
     def has_hints(self) -> bool:

@@ -781,6 +781,16 @@ gb_status gb_graph_csr_to_host(const gb_graph* g, int64_t* out_off, int32_t* out
   return GB_OK;
 }
 
+gb_status gb_graph_hints_to_host(const gb_graph* g, int32_t* hint_out, int32_t* hint_in) {
+  if (!g || !g->hint_out) return GB_ERR_INVALID;
+  CK(cudaSetDevice(g->device), "cudaSetDevice");
+  if (hint_out && g->n)
+    CK(cudaMemcpy(hint_out, g->hint_out, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
+  if (hint_in && g->n && g->hint_in)
+    CK(cudaMemcpy(hint_in, g->hint_in, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
+  return GB_OK;
+}
+
 gb_status gb_graph_device_csr(const gb_graph* g, const int64_t** out_off, const int32_t** out_adj,
                               const int64_t** in_off, const int32_t** in_adj) {
   if (!g) return GB_ERR_INVALID;

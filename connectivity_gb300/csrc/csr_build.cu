@@ -249,15 +249,19 @@ __global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t*
 }
 
 // The pull hint of a vertex: its neighbour of largest total degree, the
-// first one in adjacency order on ties (-1 without neighbours).  Vertices
-// are taken by degree:
-//   <= 32 neighbours: one thread, four neighbours' loads in flight at a time;
-//   <= 1024: the whole warp, one vertex after another (warp ballot);
-//   more: appended to `heavy` for k_hint_heavy (a block per vertex).
-// Most vertices of a power-law graph have a handful of neighbours, so a warp
-// per vertex (the simple form) leaves most lanes idle.
-constexpr int kHintThread = 32;
-constexpr int kHintWarp = 1024;
+// first one in adjacency order on ties (-1 without neighbours).
+//
+// A warp takes 32 consecutive vertices.  Their edges (of vertices with at
+// most kHintWarp neighbours) are numbered by a warp scan of the degrees and
+// walked 32 at a time, so lane k reads edge k of the run: the 32 vertices'
+// adjacency is one contiguous range of the CSR, and the reads coalesce.
+// Each edge finds its vertex by a binary search over the scan (in shared
+// memory) and folds (degree << 32 | ~index) into that vertex's slot with a
+// shared-memory atomicMax: the largest degree wins, then the smallest
+// index.  Vertices with more neighbours go to `heavy` for k_hint_heavy (a
+// block per vertex), so no warp walks a hub's edges alone.
+constexpr int kHintWarp = 4096;
+constexpr int kHintBlock = 256;
 
 __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& best_d,
                                             int64_t& best_e) {
@@ -267,58 +271,59 @@ __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& bes
   }
 }
 
-__global__ void k_hint(int32_t n, const int64_t* off, const int32_t* adj, const int32_t* deg,
-                       int32_t* hint, int32_t* heavy, int32_t* nheavy) {
-  const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-       base += stride) {
+__global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* off,
+                                                     const int32_t* adj, const int32_t* deg,
+                                                     int32_t* hint, int32_t* heavy,
+                                                     int32_t* nheavy) {
+  constexpr int W = kHintBlock / 32;
+  __shared__ int64_t s_start[W][32];
+  __shared__ int32_t s_pre[W][32];
+  __shared__ unsigned long long s_best[W][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t wstride = (int64_t)gridDim.x * W * 32;
+  for (int64_t base = ((int64_t)blockIdx.x * W + wid) * 32; base < n; base += wstride) {
     const int64_t v = base + lane;
     int64_t s = 0, d = 0;
     if (v < n) {
       s = off[v];
       d = off[v + 1] - s;
     }
-    if (d <= kHintThread) {
-      int32_t best_d = -1;
-      int64_t best_e = -1;
-      for (int64_t e = 0; e < d; e += 4) {
-        const int32_t a0 = adj[s + e];
-        const int32_t a1 = e + 1 < d ? adj[s + e + 1] : -1;
-        const int32_t a2 = e + 2 < d ? adj[s + e + 2] : -1;
-        const int32_t a3 = e + 3 < d ? adj[s + e + 3] : -1;
-        const int32_t d0 = deg[a0];
-        const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
-        const int32_t d2 = a2 >= 0 ? deg[a2] : -1;
-        const int32_t d3 = a3 >= 0 ? deg[a3] : -1;
-        if (d0 > best_d) { best_d = d0; best_e = e; }
-        if (d1 > best_d) { best_d = d1; best_e = e + 1; }
-        if (d2 > best_d) { best_d = d2; best_e = e + 2; }
-        if (d3 > best_d) { best_d = d3; best_e = e + 3; }
-      }
-      if (v < n) hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
-    } else if (d > kHintWarp) {
+    const bool is_heavy = d > kHintWarp;
+    if (is_heavy) {
       heavy[atomicAdd(nheavy, 1)] = (int32_t)v;
+      d = 0;  // walked by k_hint_heavy
     }
-    unsigned mid = __ballot_sync(0xffffffffu, d > kHintThread && d <= kHintWarp);
-    while (mid) {
-      const int j = __ffs(mid) - 1;
-      mid &= mid - 1;
-      const int64_t sj = __shfl_sync(0xffffffffu, s, j);
-      const int64_t dj = __shfl_sync(0xffffffffu, d, j);
-      int32_t best_d = -1;
-      int64_t best_e = -1;
-      for (int64_t e = lane; e < dj; e += 32) {
-        const int32_t dd = deg[adj[sj + e]];
-        if (dd > best_d) { best_d = dd; best_e = e; }
-      }
-      for (int o = 16; o; o >>= 1) {
-        const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
-        const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
-        hint_better(d2, e2, best_d, best_e);
-      }
-      if (lane == 0) hint[base + j] = adj[sj + best_e];
+    // exclusive scan of the degrees over the warp
+    int32_t inc = (int32_t)d;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
     }
+    const int32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    s_start[wid][lane] = s;
+    s_pre[wid][lane] = inc - (int32_t)d;
+    s_best[wid][lane] = 0ull;
+    __syncwarp();
+    for (int32_t e = lane; e < total; e += 32) {
+      // the last vertex whose run starts at or before e
+      int j = 0;
+      for (int step = 16; step; step >>= 1)
+        if (s_pre[wid][j + step] <= e) j += step;
+      const int32_t k = e - s_pre[wid][j];
+      const int32_t dd = deg[adj[s_start[wid][j] + k]];
+      atomicMax(&s_best[wid][j], ((unsigned long long)(uint32_t)dd << 32) |
+                                     (unsigned long long)(0xffffffffu - (uint32_t)k));
+    }
+    __syncwarp();
+    if (v < n && !is_heavy) {
+      if (d == 0) {
+        hint[v] = -1;
+      } else {
+        const uint32_t k = 0xffffffffu - (uint32_t)(s_best[wid][lane] & 0xffffffffull);
+        hint[v] = adj[s + k];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -602,12 +607,12 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
   cudaMemsetAsync(nheavy, 0, 8, s);
   k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
   const int g = grid_for(n);
-  k_hint<<<g, 256, 0, s>>>(n, out_off, out_adj, deg, hint_out, heavy, nheavy);
+  k_hint<<<g, kHintBlock, 0, s>>>(n, out_off, out_adj, deg, hint_out, heavy, nheavy);
   k_hint_heavy<<<152 * 2, 1024, 0, s>>>(out_off, out_adj, deg, hint_out, heavy, nheavy);
   if (in_off != nullptr && hint_in != nullptr) {
     // the in side reuses the heavy list with its own count; stream order
     // puts it after the out side's heavy pass has read the list
-    k_hint<<<g, 256, 0, s>>>(n, in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
+    k_hint<<<g, kHintBlock, 0, s>>>(n, in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
     k_hint_heavy<<<152 * 2, 1024, 0, s>>>(in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
   }
   cudaFreeAsync(deg, s);

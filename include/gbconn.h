@@ -243,6 +243,9 @@ gb_status gb_graph_destroy(gb_graph* g);
  * in-edges.  Waits for the context's queued work first. */
 gb_status gb_graph_set_hints(gb_ctx* ctx, gb_graph* g, int32_t on);
 gb_status gb_graph_has_hints(const gb_graph* g, int32_t* on);
+/* Copies the hints to host arrays of n entries (hint_in ignored when NULL or
+ * for a symmetric graph); GB_ERR_INVALID when the graph has none. */
+gb_status gb_graph_hints_to_host(const gb_graph* g, int32_t* hint_out, int32_t* hint_in);
 
 /* ---- runs ------------------------------------------------------------- */
 /* run_scc (multistep/scc_main.cpp:210-317): trim, FW-BW from the pivot,

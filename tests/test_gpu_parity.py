@@ -413,3 +413,43 @@ def test_balanced_push_same_work(ctx, kind):
     assert np.array_equal(lt, lb)
     assert st_b.m_visit_fw == st_t.m_visit_fw and st_b.m_visit_bw == st_t.m_visit_bw
     assert st_b.pull_steps == 0 and st_t.pull_steps == 0
+
+
+def _hints_want(n, off, adj, deg):
+    """The hint rule restated: the neighbour of largest total degree, the
+    first in adjacency order on ties, -1 without neighbours."""
+    want = np.full(n, -1, np.int64)
+    d = np.diff(off)
+    nz = np.flatnonzero(d > 0)
+    if nz.size:
+        k = np.arange(adj.size, dtype=np.int64) - np.repeat(off[:-1], d)
+        key = deg[adj].astype(np.int64) * (1 << 32) + ((1 << 32) - 1 - k)
+        best = np.maximum.reduceat(key, off[nz])
+        kk = (1 << 32) - 1 - (best & ((1 << 32) - 1))
+        want[nz] = adj[off[nz] + kk]
+    return want.astype(np.int32)
+
+
+@pytest.mark.parametrize("case", ["rmat16", "rmat20", "hub", "star"])
+def test_pull_hints_follow_the_rule(ctx, case):
+    if case == "rmat16":
+        n, s, d = gb.rmat_edges(16, 16, 1)
+    elif case == "rmat20":
+        n, s, d = gb.rmat_edges(20, 16, 1)
+    elif case == "hub":
+        # hubs above the block-per-vertex cutoff next to degree-1 vertices
+        n = 20000
+        r = np.random.default_rng(1)
+        s = np.concatenate([np.zeros(9000, np.int32), np.full(5000, 7, np.int32),
+                            r.integers(0, n, 30000).astype(np.int32)])
+        d = np.concatenate([np.arange(1, 9001, dtype=np.int32), r.integers(0, n, 5000).astype(np.int32),
+                            r.integers(0, n, 30000).astype(np.int32)])
+    else:
+        n, s, d = [c for c in graphs.edge_cases() if c[0] == "star"][0][1:]
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    oo, oa, io, ia = g.to_host()
+    deg = np.minimum(np.diff(oo) + np.diff(io), 0x7fffffff)
+    ho, hi = g.hints()
+    assert np.array_equal(ho, _hints_want(n, oo, oa, deg))
+    assert np.array_equal(hi, _hints_want(n, io, ia, deg))
+    g.close()
