@@ -56,7 +56,7 @@ class Opts(C.Structure):
         ("vert_cutoff", C.c_int32), ("t_block", C.c_int32), ("t_grid", C.c_int32),
         ("k_pull", C.c_int32), ("alpha", C.c_float), ("beta", C.c_float),
         ("max_steps", C.c_int32), ("grid_blocks", C.c_int32), ("trim_pairs", C.c_int32),
-        ("fwbw_rounds", C.c_int32), ("expand_mode", C.c_int32),
+        ("fwbw_rounds", C.c_int32), ("expand_mode", C.c_int32), ("small_path", C.c_int32),
     ]
 
 
@@ -128,6 +128,8 @@ for _n in ("gb_batch_scc", "gb_batch_wcc"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
 _sig("gb_batch_scc_async", C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
 _sig("gb_batch_destroy", C.c_int32, [_P])
+for _n in ("gb_scc_edges", "gb_wcc_edges"):
+    _sig(_n, C.c_int32, [_P, C.c_int32, C.c_int64, _P, _P, _P, C.POINTER(Opts)])
 _sig("gb_tune", C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.POINTER(Opts), _P])
 _sig("gb_tune_batch", C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.POINTER(Opts), _P])
 
@@ -392,6 +394,28 @@ class Context:
         return self._run(_lib.gb_wcc, "gb_wcc", g, labels, o, stats)
 
     cc = wcc
+
+    def _edges(self, fn, name, n, src, dst, labels, o):
+        if labels is None:
+            labels = np.empty(n, np.int32)
+        if isinstance(src, np.ndarray):
+            s = np.ascontiguousarray(src, np.int32)
+            d = np.ascontiguousarray(dst, np.int32)
+            m, sp, dp = s.size, _ptr(s), _ptr(d)
+        else:  # device pointers (ints) and their length as (ptr, m)
+            (sp, m), (dp, _) = src, dst
+            sp, dp = C.c_void_p(sp), C.c_void_p(dp)
+        lp = _ptr(labels) if isinstance(labels, np.ndarray) else C.c_void_p(int(labels))
+        _check(fn(self._h, n, m, sp, dp, lp, C.byref(o or opts())), name)
+        return labels
+
+    def scc_edges(self, n: int, src, dst, labels=None, o: Opts | None = None):
+        """SCC labels straight from an edge list (gb_scc_edges)."""
+        return self._edges(_lib.gb_scc_edges, "gb_scc_edges", n, src, dst, labels, o)
+
+    def wcc_edges(self, n: int, src, dst, labels=None, o: Opts | None = None):
+        """WCC labels straight from an edge list (gb_wcc_edges)."""
+        return self._edges(_lib.gb_wcc_edges, "gb_wcc_edges", n, src, dst, labels, o)
 
     def scc_async(self, g: "Graph", labels_dev: int, o: Opts | None = None) -> None:
         _check(_lib.gb_scc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),

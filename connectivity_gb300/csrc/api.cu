@@ -268,6 +268,74 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
   return GB_OK;
 }
 
+// True when a run of g with options o takes the one-block path (small.cu).
+bool use_small(const gb_graph* g, const gb_opts* o) {
+  if (g->n > gb::kSmallMaxN || g->m >= (1ll << 31)) return false;
+  if (!o) return true;
+  return o->small_path != 0 && o->canonical != 0;
+}
+
+// A graph of at most kSmallMaxN vertices: one thread block runs the whole
+// pipeline (small.cu).  Same stream order, error latch and events as a run
+// of the cooperative kernel; the statistics hold the times only.
+gb_status run_small(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
+                    const gb_opts* o, gb_stats* st, bool wait) {
+  const bool dev_labels = is_device_ptr(labels);
+  if (!wait && !dev_labels) {
+    gb_set_error("run: the asynchronous form needs device labels%s", "");
+    return GB_ERR_INVALID;
+  }
+  gb_status s = ensure_ws(c, g->n);
+  if (s != GB_OK) return s;
+  int32_t* dl = dev_labels ? labels : c->w.label;
+  cudaStream_t sm = c->stream;
+  CK(cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), sm), "memset");
+  cudaEvent_t* ev = c->ev[c->runs % gb_ctx::kRing];
+  CK(cudaMemsetAsync(c->d_tphase + 4 * (c->runs % gb_ctx::kRing), 0,
+                     4 * sizeof(unsigned long long), sm),
+     "memset");
+  c->runs++;
+  cudaEventRecord(ev[0], sm);
+  gb::SmallDesc d{};
+  d.n = g->n;
+  d.m = g->m;
+  d.out_off = g->out_off;
+  d.out_adj = g->out_adj;
+  d.in_off = g->symmetric ? nullptr : g->in_off;
+  d.in_adj = g->symmetric ? nullptr : g->in_adj;
+  d.labels = dl;
+  const int32_t max_steps = o && o->max_steps > 0 ? o->max_steps : (1 << 30);
+  CK(gb::launch_small(kind == gb::kSCC ? 0 : 1, d, nullptr, 1, g->n, max_steps, &c->d_ctl->err,
+                      sm),
+     "kernel launch");
+  cudaEventRecord(ev[1], sm);
+  cudaEventRecord(ev[4], sm);
+  CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
+  if (!dev_labels)
+    CK(cudaMemcpyAsync(labels, dl, (size_t)g->n * 4, cudaMemcpyDeviceToHost, sm), "labels copy");
+  CK(cudaMemcpyAsync(&c->h_ctl->err, &c->d_ctl->err, 2 * sizeof(int), cudaMemcpyDeviceToHost, sm),
+     "status copy");
+  if (!wait) return GB_OK;
+  CK(cudaStreamSynchronize(sm), "run");
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    float tot = 0.f;
+    if (cudaEventElapsedTime(&tot, ev[0], ev[4]) == cudaSuccess) st->ms_total = tot;
+    st->pivot = -1;
+    st->grid_blocks = 1;
+    st->err_where = c->h_ctl->err_where;
+  }
+  *c->h_sticky = 0;
+  cudaMemsetAsync(c->d_sticky, 0, 2 * sizeof(int), sm);
+  const int err = c->h_ctl->err;
+  if (err != 0) {
+    gb_set_error("run: %s", err == gb::kErrIterLimit ? "a loop of the one-block path hit its step cap"
+                                                     : "device error in the one-block path");
+    return (gb_status)err;
+  }
+  return GB_OK;
+}
+
 gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
                          const gb_opts* o, gb_stats* st, bool wait, const gb::BatchView* bv) {
   if (!c || !g) {
@@ -284,6 +352,7 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
   }
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   if (g->n == 0) return GB_OK;
+  if (bv == nullptr && use_small(g, o)) return run_small(c, g, kind, labels, o, st, wait);
   gb_status s = ensure_ws(c, g->n);
   if (s != GB_OK) return s;
   const bool dev_labels = is_device_ptr(labels);
@@ -381,6 +450,7 @@ void gb_opts_default(gb_opts* o) {
   o->trim_pairs = 0;
   o->fwbw_rounds = 1;
   o->expand_mode = 0;
+  o->small_path = 1;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {
@@ -855,6 +925,93 @@ gb_status gb_wcc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o
 gb_status gb_cc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
   return gb::run_graph(c, g, gb::kWCC, labels, o, st, true, nullptr);
 }
+}  // extern "C"
+
+namespace {
+// SCC / WCC of an edge list: small graphs take the one-block path straight
+// from the edges (no CSR build by radix sort, one launch); others get a
+// device graph that is built, run and freed.
+gb_status run_edges(gb_ctx* c, gb::RunKind kind, int32_t n, int64_t m, const int32_t* src,
+                    const int32_t* dst, int32_t* labels, const gb_opts* o) {
+  if (!c || n < 0 || m < 0 || (m > 0 && (!src || !dst)) || (n > 0 && !labels)) {
+    gb_set_error("run from edges: %s", "bad argument");
+    return GB_ERR_INVALID;
+  }
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (n == 0) return GB_OK;
+  gb_opts d;
+  gb_opts_default(&d);
+  if (!o) o = &d;
+  if (n > gb::kSmallMaxN || m >= (1ll << 31) || !o->small_path || !o->canonical) {
+    gb_graph* g = nullptr;
+    gb_status s = gb_graph_from_edges(c, n, m, src, dst, &g);
+    if (s != GB_OK) return s;
+    s = gb::run_graph(c, g, kind, labels, o, nullptr, true, nullptr);
+    gb_graph_destroy(g);
+    return s;
+  }
+  cudaStream_t sm = c->stream;
+  const bool dev_edges = m == 0 || is_device_ptr(src);
+  const bool dev_labels = is_device_ptr(labels);
+  // one stream-ordered allocation: the edges (from host memory), the SCC
+  // CSR built by the block (2m ints) and the labels (for host labels)
+  const size_t edge_b = dev_edges ? 0 : (size_t)m * 8;
+  const size_t scr_b = kind == gb::kSCC ? (size_t)m * 8 : 0;
+  const size_t lab_b = dev_labels ? 0 : (size_t)n * 4;
+  char* buf = nullptr;
+  if (edge_b + scr_b + lab_b > 0)
+    CK(cudaMallocAsync((void**)&buf, edge_b + scr_b + lab_b, sm), "edge staging");
+  gb::SmallDesc sd{};
+  sd.n = n;
+  sd.m = m;
+  sd.src = src;
+  sd.dst = dst;
+  cudaError_t e = cudaSuccess;
+  if (!dev_edges) {
+    int32_t* ds = reinterpret_cast<int32_t*>(buf);
+    e = cudaMemcpyAsync(ds, src, (size_t)m * 4, cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ds + m, dst, (size_t)m * 4, cudaMemcpyHostToDevice, sm);
+    sd.src = ds;
+    sd.dst = ds + m;
+  }
+  sd.adj_scratch = scr_b ? reinterpret_cast<int32_t*>(buf + edge_b) : nullptr;
+  sd.labels = dev_labels ? labels : reinterpret_cast<int32_t*>(buf + edge_b + scr_b);
+  const int32_t max_steps = o->max_steps > 0 ? o->max_steps : (1 << 30);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), sm);
+  if (e == cudaSuccess)
+    e = gb::launch_small(kind == gb::kSCC ? 0 : 1, sd, nullptr, 1, n, max_steps, &c->d_ctl->err,
+                         sm);
+  if (e == cudaSuccess && !dev_labels)
+    e = cudaMemcpyAsync(labels, sd.labels, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&c->h_ctl->err, &c->d_ctl->err, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                        sm);
+  if (buf) cudaFreeAsync(buf, sm);
+  const cudaError_t e2 = cudaStreamSynchronize(sm);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "run from edges");
+  const int err = c->h_ctl->err;
+  if (err != 0) {
+    gb_set_error("run from edges: %s", err == gb::kErrInvalid ? "vertex id outside [0, n)"
+                                                              : "a loop hit its step cap");
+    return (gb_status)err;
+  }
+  return GB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+gb_status gb_scc_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src, const int32_t* dst,
+                       int32_t* labels, const gb_opts* o) {
+  return run_edges(c, gb::kSCC, n, m, src, dst, labels, o);
+}
+gb_status gb_wcc_edges(gb_ctx* c, int32_t n, int64_t m, const int32_t* src, const int32_t* dst,
+                       int32_t* labels, const gb_opts* o) {
+  return run_edges(c, gb::kWCC, n, m, src, dst, labels, o);
+}
+
 gb_status gb_scc_async(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o) {
   return gb::run_graph(c, g, gb::kSCC, labels, o, nullptr, false, nullptr);
 }

@@ -256,9 +256,10 @@ __global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t*
 // walked 32 at a time, so lane k reads edge k of the run: the 32 vertices'
 // adjacency is one contiguous range of the CSR, and the reads coalesce.
 // Each edge finds its vertex by a binary search over the scan (in shared
-// memory) and folds (degree << 32 | ~index) into that vertex's slot with a
-// shared-memory atomicMax: the largest degree wins, then the smallest
-// index.  Vertices with more neighbours go to `heavy` for k_hint_heavy (a
+// memory); keys (degree << 32 | ~index) are reduced per vertex by a
+// segmented warp maximum, and the last lane of each vertex folds the result
+// into the vertex's slot in shared memory: the largest degree wins, then the
+// smallest index.  Vertices with more neighbours go to `heavy` for k_hint_heavy (a
 // block per vertex), so no warp walks a hub's edges alone.
 constexpr int kHintWarp = 4096;
 constexpr int kHintBlock = 256;
@@ -304,15 +305,32 @@ __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* o
     s_pre[wid][lane] = inc - (int32_t)d;
     s_best[wid][lane] = 0ull;
     __syncwarp();
-    for (int32_t e = lane; e < total; e += 32) {
+    for (int32_t e0 = 0; e0 < total; e0 += 32) {
+      const int32_t e = e0 + lane;
+      const bool act = e < total;
       // the last vertex whose run starts at or before e
       int j = 0;
       for (int step = 16; step; step >>= 1)
         if (s_pre[wid][j + step] <= e) j += step;
-      const int32_t k = e - s_pre[wid][j];
-      const int32_t dd = deg[adj[s_start[wid][j] + k]];
-      atomicMax(&s_best[wid][j], ((unsigned long long)(uint32_t)dd << 32) |
-                                     (unsigned long long)(0xffffffffu - (uint32_t)k));
+      unsigned long long key = 0ull;
+      if (act) {
+        const int32_t k = e - s_pre[wid][j];
+        const int32_t dd = deg[adj[s_start[wid][j] + k]];
+        key = ((unsigned long long)(uint32_t)dd << 32) |
+              (unsigned long long)(0xffffffffu - (uint32_t)k);
+      } else {
+        j = 32;  // a segment of its own, never written
+      }
+      // lanes of one vertex are adjacent: a segmented maximum over the warp,
+      // then the segment's last lane folds it into the vertex's slot
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, key, o);
+        const int yj = __shfl_up_sync(0xffffffffu, j, o);
+        if (lane >= o && yj == j && y > key) key = y;
+      }
+      const int nj = __shfl_down_sync(0xffffffffu, j, 1);
+      if (act && (lane == 31 || nj != j) && key > s_best[wid][j]) s_best[wid][j] = key;
+      __syncwarp();
     }
     __syncwarp();
     if (v < n && !is_heavy) {

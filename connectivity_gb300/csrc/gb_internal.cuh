@@ -17,6 +17,7 @@ constexpr unsigned kFull = 0xffffffffu;
 // Error codes written by kernels; equal to the gb_status values of gbconn.h.
 enum : int {
   kErrNone = 0,
+  kErrInvalid = 1,     // an input id outside [0, n)
   kErrTimeout = 4,     // a grid barrier wait hit its time / spin limit
   kErrIterLimit = 5,   // a fixed-point loop hit its step cap
   kErrCapacity = 9,    // an append would overflow its array
@@ -227,6 +228,35 @@ cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_of
 // Copies the first device error of a run into sticky[0..1] (code, site)
 // unless an earlier one is already there.
 cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
+
+// Small graphs, one thread block per graph (small.cu).  A graph of at most
+// kSmallMaxN vertices keeps its per-vertex state in shared memory.
+constexpr int32_t kSmallMaxN = 6144;
+struct SmallDesc {
+  int32_t n;
+  int32_t id_base;          // subtracted from every adjacency entry (batch unions)
+  int64_t m;
+  // CSR form (out_off != null): n + 1 absolute offsets per side, adjacency
+  // holding ids id_base .. id_base + n - 1; in_off null = symmetric graph
+  const int64_t* out_off;
+  const int32_t* out_adj;
+  const int64_t* in_off;
+  const int32_t* in_adj;
+  // edge form (out_off == null): m local ids each; SCC builds its CSR into
+  // adj_scratch (2m ints), WCC needs no scratch
+  const int32_t* src;
+  const int32_t* dst;
+  int32_t* adj_scratch;
+  int32_t* labels;          // n outputs: smallest member id per component
+};
+// Dynamic shared memory of a block for graphs of at most max_n vertices.
+size_t small_smem_bytes(int32_t max_n);
+// kind 0 = SCC, 1 = WCC.  One block per graph: `count` descriptors from
+// `many` (device memory), or `one` when many is null (count 1).  A failure
+// (an id outside [0, n) in edge form: kErrInvalid; a loop past max_steps:
+// kErrIterLimit) is written to *err with atomicCAS from 0.
+cudaError_t launch_small(int kind, const SmallDesc& one, const SmallDesc* many, int count,
+                         int32_t max_n, int32_t max_steps, int* err, cudaStream_t s);
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
 // Reference-layout CSR (32-bit offsets) from device-readable host memory into
 // an int64-offset device CSR, checked on the way (*d_bad |= 1 on a bad CSR).

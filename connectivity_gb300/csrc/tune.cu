@@ -5,10 +5,11 @@
 // walks the vertex; t_grid: every block takes a slice), the in-edges a
 // thread scans in a pull step before the candidate moves to a warp (k_pull),
 // the direction-switch factors (alpha: push -> pull, beta: pull -> push),
-// the number of resident blocks the cooperative kernel uses, and the push
+// the number of resident blocks the cooperative kernel uses, the push
 // scheme of the searches: the degree tiers (warp, block, grid slice) or the
 // global edge balance of the Kokkos variant's "manhattan global" FW-BW
-// (kokkos_scc/fwbw_manhattan_global.cpp:186-289).  The search is
+// (kokkos_scc/fwbw_manhattan_global.cpp:186-289), and for a graph of at
+// most 6144 vertices the one-block path against the cooperative grid.  The search is
 // coordinate descent from the defaults: each tunable in turn tries its
 // candidate values with the others held, and a value is kept when it beats
 // the best time so far by more than 2 %; two passes.  Every time is the
@@ -32,7 +33,7 @@ namespace {
 
 struct Param {
   int which;  // 0 t_block, 1 t_grid, 2 k_pull, 3 alpha, 4 beta, 5 grid_blocks (fraction),
-              // 6 expand_mode
+              // 6 expand_mode, 7 small_path
   std::vector<double> values;
 };
 
@@ -45,6 +46,7 @@ void set_param(gb_opts& o, int which, double v, int grid) {
     case 4: o.beta = (float)v; break;
     case 5: o.grid_blocks = v >= 1.0 ? 0 : std::max(1, (int)(grid * v)); break;
     case 6: o.expand_mode = (int32_t)v; break;
+    case 7: o.small_path = (int32_t)v; break;
   }
 }
 
@@ -56,6 +58,7 @@ double get_param(const gb_opts& o, int which, int grid) {
     case 3: return o.alpha;
     case 4: return o.beta;
     case 6: return o.expand_mode;
+    case 7: return o.small_path;
     default: return o.grid_blocks <= 0 ? 1.0 : (double)o.grid_blocks / grid;
   }
 }
@@ -90,6 +93,7 @@ gb_status time_runs(gb_ctx* c, const gb_opts& o, int reps, Run run, double* ms) 
 template <class Run>
 gb_status tune(gb_ctx* c, int reps, Run run, gb_opts* best, double* ms_out) {
   const std::vector<Param> params = {
+      {7, {0, 1}},  // one thread block (graphs of at most 6144 vertices) or the grid
       {0, {128, 512, 2048}},
       {1, {8192, 32768, 131072}},
       {2, {1, 2, 4}},

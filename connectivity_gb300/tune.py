@@ -16,7 +16,7 @@ from . import Batch, Context, Graph, Opts, opts
 # (vertices, edge factor) of the classes tuned by default
 CLASSES = [(1 << 10, 8), (1 << 14, 16), (1 << 18, 16), (1 << 22, 16), (1 << 24, 16)]
 
-TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode")
+TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode", "small_path")
 
 
 def opts_to_dict(o: Opts) -> dict:
@@ -44,6 +44,36 @@ def tune_batch(ctx: Context, b: Batch, kind: int = 0, reps: int = 3) -> dict:
     o, ms, dms = ctx.tune(b, kind, reps)
     return {"count": b.count, "n": b.n, "m": b.m, "ms": ms, "default_ms": dms,
             "opts": opts_to_dict(o)}
+
+
+# vertex-count ranges of the batch size classes: [lo, hi)
+SIZE_CLASSES = [(0, 1000), (1000, 10000), (10000, 100000), (100000, 1 << 31)]
+
+
+def tune_batch_by_class(ctx: Context, ns, efs, seeds, kind: int = 0, reps: int = 2,
+                        classes=SIZE_CLASSES) -> dict:
+    """Per-size-class tuning of a batch: the graphs of each vertex-count
+    class as a batch of their own, tuned (gb_tune_batch), against the
+    defaults on the same sub-batch.  When the defaults are within a few
+    percent of the tuned options in every class, options chosen per class
+    inside one merged run cannot gain more than that."""
+    import numpy as np
+    ns = np.asarray(ns)
+    out = {"classes": []}
+    for lo, hi in classes:
+        idx = np.flatnonzero((ns >= lo) & (ns < hi))
+        if idx.size == 0:
+            continue
+        b = Batch.rmat(ctx, ns[idx], np.asarray(efs)[idx], np.asarray(seeds)[idx])
+        o, ms, dms = ctx.tune(b, kind, reps)
+        out["classes"].append({"n_range": [int(lo), int(hi)], "graphs": int(idx.size),
+                               "vertices": int(b.n), "edges": int(b.m),
+                               "default_ms": round(dms, 4), "tuned_ms": round(ms, 4),
+                               "gain": round(1.0 - ms / dms, 4) if dms > 0 else 0.0,
+                               "opts": opts_to_dict(o)})
+        b.close()
+    out["max_gain"] = max((c["gain"] for c in out["classes"]), default=0.0)
+    return out
 
 
 def save(table: dict, path: str) -> None:

@@ -101,6 +101,14 @@ typedef struct gb_opts {
                           the Kokkos variant's manhattan-global FW-BW
                           (kokkos_scc/fwbw_manhattan_global.cpp:186-289).
                           An autotuner candidate. */
+  int32_t small_path;  /* 1 (default): a graph of at most 6144 vertices runs
+                          in one thread block with all its per-vertex state
+                          in shared memory (trim to the fixed point, FW-BW,
+                          colour rounds; WCC by union-find), no cooperative
+                          grid; 0: always the cooperative run kernel.  Needs
+                          canonical = 1 (otherwise the cooperative kernel
+                          runs); the statistics then hold the times only.
+                          No reference counterpart. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);
@@ -260,6 +268,18 @@ gb_status gb_wcc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts*
                  gb_stats* stats);
 gb_status gb_cc(gb_ctx* ctx, const gb_graph* g, int32_t* labels, const gb_opts* opts,
                 gb_stats* stats);
+/* From an edge list to labels in one call (read_edge's arrays, scc_main.cpp:
+ * 94-125, straight into run_scc / run_cc, scc_main.cpp:210 and cc_main.cpp:
+ * 184): src / dst hold m ids in [0, n) (host or device memory), labels n
+ * entries (host or device).  A graph of at most 6144 vertices (small_path,
+ * the default) runs in one thread block that builds its own CSR in shared
+ * memory and scratch from the stream-ordered pool: one launch, no radix
+ * sort.  Larger graphs are built as a device graph, run and freed.  Waits
+ * for the result.  GB_ERR_INVALID: an id outside [0, n). */
+gb_status gb_scc_edges(gb_ctx* ctx, int32_t n, int64_t m, const int32_t* src, const int32_t* dst,
+                       int32_t* labels, const gb_opts* opts);
+gb_status gb_wcc_edges(gb_ctx* ctx, int32_t n, int64_t m, const int32_t* src, const int32_t* dst,
+                       int32_t* labels, const gb_opts* opts);
 /* As gb_scc / gb_wcc but without waiting: labels must be device memory; the
  * status is collected by gb_ctx_sync. */
 gb_status gb_scc_async(gb_ctx* ctx, const gb_graph* g, int32_t* labels_dev, const gb_opts* opts);

@@ -3,7 +3,8 @@ step cap that runs out.  Every fixed-point loop of the run kernel checks the
 cap in lockstep on all blocks; the block that stops sets the error word,
 whose bit in the grid-barrier word releases every other block.  The host
 must read GB_ERR_ITER_LIMIT, and the same context must then give correct
-labels."""
+labels.  The one-block path (graphs of at most 6144 vertices) caps its
+loops the same way."""
 from __future__ import annotations
 
 import numpy as np
@@ -26,7 +27,7 @@ def test_step_cap_reports_iter_limit_then_context_recovers(ctx, case, kind):
     fn = ctx.scc if kind == "scc" else ctx.wcc
     for _ in range(2):
         with pytest.raises(gb.GBError) as e:
-            fn(g, o=gb.opts(max_steps=2))
+            fn(g, o=gb.opts(max_steps=2, small_path=0))
         assert e.value.status == 5, str(e.value)  # GB_ERR_ITER_LIMIT
         lab = fn(g)
         want = (oracle.scc(oracle.CpuGraph(n, s, d)) if kind == "scc"
@@ -42,11 +43,11 @@ def test_step_cap_in_async_runs_is_reported_by_sync(ctx):
     n, s, d = CASES["cycle_1000"]
     g = gb.Graph.from_edges(ctx, n, s, d)
     out = torch.empty(n, dtype=torch.int32, device="cuda")
-    ctx.scc_async(g, out.data_ptr(), gb.opts(max_steps=2))
+    ctx.scc_async(g, out.data_ptr(), gb.opts(max_steps=2, small_path=0))
     with pytest.raises(gb.GBError) as e:
         ctx.sync()
     assert e.value.status == 5
-    ctx.scc_async(g, out.data_ptr(), gb.opts())
+    ctx.scc_async(g, out.data_ptr(), gb.opts(small_path=0))
     ctx.sync()
     assert out.cpu().numpy().tolist() == [0] * n
     g.close()
@@ -65,3 +66,23 @@ def test_step_cap_in_a_batch(ctx):
     for i, (n, s, d) in enumerate(parts):
         assert np.array_equal(lab[vbase[i]:vbase[i + 1]], oracle.scc(oracle.CpuGraph(n, s, d)))
     b.close()
+
+
+@pytest.mark.parametrize("case", ["path_1000", "cycle_1000"])
+def test_step_cap_in_the_one_block_path(ctx, case):
+    """The one-block path's loops (trim, searches, colour rounds) stop at
+    the cap with GB_ERR_ITER_LIMIT, from a device graph and from edges; the
+    next run on the same context is correct."""
+    n, s, d = CASES[case]
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    want = oracle.scc(oracle.CpuGraph(n, s, d))
+    for _ in range(2):
+        with pytest.raises(gb.GBError) as e:
+            ctx.scc(g, o=gb.opts(max_steps=2, small_path=1))
+        assert e.value.status == 5
+        with pytest.raises(gb.GBError) as e:
+            ctx.scc_edges(n, s, d, o=gb.opts(max_steps=2))
+        assert e.value.status == 5
+        assert np.array_equal(ctx.scc(g), want)
+        assert np.array_equal(ctx.scc_edges(n, s, d), want)
+    g.close()

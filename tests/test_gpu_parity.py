@@ -12,6 +12,14 @@ from tests import graphs
 
 pytestmark = pytest.mark.gpu
 
+
+def opts(**kw):
+    """Options of a run of the cooperative kernel: this file tests that
+    kernel on small graphs too (the one-block path, which small graphs take
+    by default, has its own tests in test_gpu_small.py)."""
+    kw.setdefault("small_path", 0)
+    return gb.opts(**kw)
+
 CASES = graphs.edge_cases()
 
 VARIANTS = {
@@ -44,7 +52,7 @@ def _wcc_want(n, s, d):
 def test_scc_edge_cases(ctx, case, variant):
     name, n, s, d = case
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab, st = ctx.scc(g, o=gb.opts(**VARIANTS[variant]), stats=True)
+    lab, st = ctx.scc(g, o=opts(**VARIANTS[variant]), stats=True)
     want = _scc_want(n, s, d)
     assert np.array_equal(lab, want), name
     assert gb.scc_verify(lab) == gb.scc_verify(want)
@@ -56,7 +64,7 @@ def test_scc_edge_cases(ctx, case, variant):
 def test_wcc_edge_cases(ctx, case, variant):
     name, n, s, d = case
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab = ctx.wcc(g, o=gb.opts(**VARIANTS[variant]))
+    lab = ctx.wcc(g, o=opts(**VARIANTS[variant]))
     want = _wcc_want(n, s, d)
     assert np.array_equal(lab, want), name
     assert gb.cc_verify(lab) == gb.cc_verify(want)
@@ -66,9 +74,9 @@ def test_reference_golden_vector(ctx):
     # multistep/test.graph: SCC {0,1},{2}; CC one component
     n, s, d = graphs.test_graph()
     g = gb.Graph.from_edges(ctx, n, s, d)
-    assert ctx.scc(g).tolist() == [0, 0, 2]
-    assert ctx.wcc(g).tolist() == [0, 0, 0]
-    assert gb.scc_verify(ctx.scc(g)) == "Num SCCs: 2, Nontrivial: 1, Max SCC: 2, Unassigned 0\n"
+    assert ctx.scc(g, o=opts()).tolist() == [0, 0, 2]
+    assert ctx.wcc(g, o=opts()).tolist() == [0, 0, 0]
+    assert gb.scc_verify(ctx.scc(g, o=opts())) == "Num SCCs: 2, Nontrivial: 1, Max SCC: 2, Unassigned 0\n"
 
 
 @pytest.mark.parametrize("scale,ef", [(10, 16), (12, 4), (14, 16), (16, 16), (16, 32), (18, 8)])
@@ -77,7 +85,7 @@ def test_reference_golden_vector(ctx):
 def test_rmat_scc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab = ctx.scc(g, o=gb.opts(**VARIANTS[variant]))
+    lab = ctx.scc(g, o=opts(**VARIANTS[variant]))
     want = _scc_want(n, s, d)
     assert np.array_equal(lab, want)
 
@@ -87,7 +95,7 @@ def test_rmat_scc(ctx, scale, ef, variant):
 def test_rmat_wcc(ctx, scale, ef, variant):
     n, s, d = graphs.rmat(scale, ef)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    assert np.array_equal(ctx.wcc(g, o=gb.opts(**VARIANTS[variant])), _wcc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(g, o=opts(**VARIANTS[variant])), _wcc_want(n, s, d))
 
 
 @pytest.mark.parametrize("side", [16, 64, 128])
@@ -95,7 +103,7 @@ def test_rmat_wcc(ctx, scale, ef, variant):
 def test_grid_scc(ctx, side, variant):
     n, s, d = graphs.grid(side)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab = ctx.scc(g, o=gb.opts(**VARIANTS[variant]))
+    lab = ctx.scc(g, o=opts(**VARIANTS[variant]))
     want = _scc_want(n, s, d)
     assert np.array_equal(lab, want)
 
@@ -106,7 +114,7 @@ def test_grid_1024_scc(ctx, trim):
     colour rounds with local continuation against the oracle."""
     n, s, d = graphs.grid(1024)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab, st = ctx.scc(g, o=gb.opts(trim_level=trim), stats=True)
+    lab, st = ctx.scc(g, o=opts(trim_level=trim), stats=True)
     assert st.colour_rounds > 10  # the colour phase does the work here
     assert np.array_equal(lab, _scc_want(n, s, d))
 
@@ -115,7 +123,7 @@ def test_grid_1024_scc(ctx, trim):
 def test_grid_wcc(ctx, side):
     n, s, d = graphs.grid(side)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(g, o=opts()), _wcc_want(n, s, d))
 
 
 def test_device_rmat_matches_host_generator(ctx):
@@ -132,14 +140,14 @@ def test_from_csr_and_pivot(ctx):
     n, s, d = graphs.rmat(12, 16, 3)
     cg = oracle.CpuGraph(n, s, d)
     g = gb.Graph.from_csr(ctx, n, cg.out_off, cg.out_adj, cg.in_off, cg.in_adj)
-    assert np.array_equal(ctx.scc(g), _scc_want(n, s, d))
+    assert np.array_equal(ctx.scc(g, o=opts()), _scc_want(n, s, d))
     assert ctx.pivot(g, 0)[0] == cg.pivot_scc()[0]
     mg = oracle.CpuGraph(n, s, d, mirror=True)
     assert ctx.pivot(g, 1)[0] == mg.pivot_cc()[0]
     # symmetric CSR (cc's mirrored graph) gives the same WCC
     sg = gb.Graph.from_csr(ctx, n, mg.out_off, mg.out_adj)
     assert sg.symmetric
-    assert np.array_equal(ctx.wcc(sg), _wcc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(sg, o=opts()), _wcc_want(n, s, d))
 
 
 def test_reference_shaped_dropins():
@@ -228,7 +236,7 @@ def test_device_labels_and_async(ctx):
 def test_raw_labels_partition(ctx):
     n, s, d = graphs.rmat(14, 16, 13)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    raw = ctx.scc(g, o=gb.opts(canonical=0))
+    raw = ctx.scc(g, o=opts(canonical=0))
     assert np.array_equal(gb.canonicalize(raw), _scc_want(n, s, d))
 
 
@@ -243,16 +251,16 @@ def test_bad_edges_rejected(ctx):
 def test_repeat_runs_identical(ctx):
     n, s, d = graphs.rmat(16, 16, 21)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    first = ctx.scc(g)
+    first = ctx.scc(g, o=opts())
     for _ in range(5):
-        assert np.array_equal(ctx.scc(g), first)
+        assert np.array_equal(ctx.scc(g, o=opts()), first)
 
 
 def test_rmat_s20_scc_and_wcc(ctx):
     n, s, d = graphs.rmat(20, 16, 1)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    assert np.array_equal(ctx.scc(g), _scc_want(n, s, d))
-    assert np.array_equal(ctx.wcc(g), _wcc_want(n, s, d))
+    assert np.array_equal(ctx.scc(g, o=opts()), _scc_want(n, s, d))
+    assert np.array_equal(ctx.wcc(g, o=opts()), _wcc_want(n, s, d))
 
 
 def _hub_graph(core=300, up=4000, down=3000, seed=12):
@@ -286,12 +294,12 @@ def test_searches_together_from_hub_pivot(ctx):
     n, s, d = _hub_graph()
     g = gb.Graph.from_edges(ctx, n, s, d)
     piv, _ = ctx.pivot(g, 0)
-    lab, st = ctx.scc(g, stats=True)
+    lab, st = ctx.scc(g, stats=True, o=opts())
     assert np.array_equal(lab, _scc_want(n, s, d))
     # the pivot is a hub, so the two searches ran together: the forward set
     # holds the core and the downstream region, the component the core only
     assert st.n_fwbw == 300 and st.n_visit_fw == 300 + 3000
-    assert np.array_equal(ctx.scc(g, o=gb.opts(trim_level=2)), lab)
+    assert np.array_equal(ctx.scc(g, o=opts(trim_level=2)), lab)
 
 
 def _planted_pairs(npairs, nrest, seed):
@@ -332,8 +340,8 @@ def test_trim_pairs_planted(ctx, trim):
     n, s, d = _planted_pairs(500, 3000, 11)
     g = gb.Graph.from_edges(ctx, n, s, d)
     want = _scc_want(n, s, d)
-    lab0, st0 = ctx.scc(g, o=gb.opts(trim_level=trim), stats=True)
-    lab1, st1 = ctx.scc(g, o=gb.opts(trim_level=trim, trim_pairs=1), stats=True)
+    lab0, st0 = ctx.scc(g, o=opts(trim_level=trim), stats=True)
+    lab1, st1 = ctx.scc(g, o=opts(trim_level=trim, trim_pairs=1), stats=True)
     assert np.array_equal(lab0, want) and np.array_equal(lab1, want)
     sizes = np.bincount(want, minlength=n)
     found = st1.n_trim - st0.n_trim
@@ -350,10 +358,10 @@ def test_trim_pairs_only_pairs(ctx):
     d = np.concatenate([u + 1, u])
     n = 2 * npairs
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab, st = ctx.scc(g, o=gb.opts(trim_pairs=1), stats=True)
+    lab, st = ctx.scc(g, o=opts(trim_pairs=1), stats=True)
     assert np.array_equal(lab, np.repeat(u, 2))
     assert st.n_trim == n and st.n_fwbw == 0 and st.colour_rounds == 0
-    lab0, st0 = ctx.scc(g, o=gb.opts(trim_level=0), stats=True)
+    lab0, st0 = ctx.scc(g, o=opts(trim_level=0), stats=True)
     assert np.array_equal(lab0, lab) and st0.n_trim == 0
 
 
@@ -377,8 +385,8 @@ def test_repivot_rounds_take_the_next_components(ctx, kind):
     g = gb.Graph.from_edges(ctx, n, s, d)
     fn = ctx.scc if kind == "scc" else ctx.wcc
     want = _scc_want(n, s, d) if kind == "scc" else _wcc_want(n, s, d)
-    lab1, st1 = fn(g, o=gb.opts(fwbw_rounds=1), stats=True)
-    lab4, st4 = fn(g, o=gb.opts(fwbw_rounds=4), stats=True)
+    lab1, st1 = fn(g, o=opts(fwbw_rounds=1), stats=True)
+    lab4, st4 = fn(g, o=opts(fwbw_rounds=4), stats=True)
     assert np.array_equal(lab1, want) and np.array_equal(lab4, want)
     assert st1.fwbw_rounds == 1 and st4.fwbw_rounds == 4
     sizes = np.sort(np.bincount(want))[::-1]
@@ -393,7 +401,7 @@ def test_repivot_stops_when_little_is_left(ctx):
     rounds take the rest), whatever the option asks for."""
     n, s, d = graphs.rmat(10, 16)
     g = gb.Graph.from_edges(ctx, n, s, d)
-    lab, st = ctx.scc(g, o=gb.opts(fwbw_rounds=50), stats=True)
+    lab, st = ctx.scc(g, o=opts(fwbw_rounds=50), stats=True)
     assert np.array_equal(lab, _scc_want(n, s, d))
     assert st.fwbw_rounds == 1
 
@@ -406,8 +414,8 @@ def test_balanced_push_same_work(ctx, kind):
     n, s, d = graphs.rmat(16, 16)
     g = gb.Graph.from_edges(ctx, n, s, d)
     fn = ctx.scc if kind == "scc" else ctx.wcc
-    o_t = gb.opts(alpha=1e-9)
-    o_b = gb.opts(alpha=1e-9, expand_mode=1)
+    o_t = opts(alpha=1e-9)
+    o_b = opts(alpha=1e-9, expand_mode=1)
     lt, st_t = fn(g, o=o_t, stats=True)
     lb, st_b = fn(g, o=o_b, stats=True)
     assert np.array_equal(lt, lb)
