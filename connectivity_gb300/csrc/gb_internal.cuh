@@ -232,6 +232,9 @@ cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
 // Small graphs, one thread block per graph (small.cu).  A graph of at most
 // kSmallMaxN vertices keeps its per-vertex state in shared memory.
 constexpr int32_t kSmallMaxN = 6144;
+// edges up to which a device graph takes the one-block path by default (an
+// edge list always does: it saves the CSR build)
+constexpr int64_t kSmallAutoEdges = 40960;
 struct SmallDesc {
   int32_t n;
   int32_t id_base;          // subtracted from every adjacency entry (batch unions)

@@ -12,6 +12,13 @@
 // request's labels are the ones it gets alone (the batch path guarantees
 // it); latency is completion minus arrival on the server clock.
 //
+// A merged set of up to kSmallWave small requests (at most kSmallMaxN
+// vertices each) skips the union build: each such request runs in one
+// thread block straight from its uploaded edges (small.cu), all of them in
+// one launch, so at low and moderate load a request costs one short launch
+// instead of a radix-sort CSR build and a cooperative run.  Larger sets, and
+// the large requests of any set, take the union path.
+//
 // The reference has no serving; its equivalent is one run_scc / run_cc call
 // per request (multistep/scc_main.cpp:210, cc_main.cpp:184).
 #include <algorithm>
@@ -97,7 +104,14 @@ struct Part {
   size_t h_bad_cap = 0;
   int32_t* d_labels = nullptr;
   gb_batch* batch = nullptr;
+  int32_t nlarge = 0;             // requests on the union path (listed first)
+  gb::SmallDesc* d_descs = nullptr;  // the one-block requests
+  int32_t* d_scratch = nullptr;      // their CSRs (SCC)
 };
+
+// Small requests of one merged set run one block each when there are at
+// most this many (two waves of one block per SM); more go to the union.
+constexpr int32_t kSmallWave = 304;
 
 struct Flight {
   Part part[2];
@@ -159,6 +173,11 @@ void part_release(gb_server* sv, Part& p) {
   if (p.d_vb) cudaFreeAsync(p.d_vb, s);
   if (p.d_labels) cudaFreeAsync(p.d_labels, s);
   if (p.d_bad) cudaFreeAsync(p.d_bad, s);
+  if (p.d_descs) cudaFreeAsync(p.d_descs, s);
+  if (p.d_scratch) cudaFreeAsync(p.d_scratch, s);
+  p.d_descs = nullptr;
+  p.d_scratch = nullptr;
+  p.nlarge = 0;
   p.d_bad = nullptr;
   p.d_src = p.d_dst = nullptr;
   p.d_eb = p.d_vb = nullptr;
@@ -167,8 +186,21 @@ void part_release(gb_server* sv, Part& p) {
   p.n = p.m = 0;
 }
 
-// Copies the admitted requests' edges to the device (copy stream).
+// Copies the admitted requests' edges to the device (copy stream).  The
+// requests that take the union path come first.
 gb_status part_upload(gb_server* sv, Part& p) {
+  int32_t nsmall = 0;
+  if (sv->opts.small_path && sv->opts.canonical)
+    for (Req* r : p.reqs)
+      if (r->n <= gb::kSmallMaxN && r->m < (1ll << 31)) ++nsmall;
+  if (nsmall > 0 && nsmall <= kSmallWave) {
+    std::stable_partition(p.reqs.begin(), p.reqs.end(), [](const Req* r) {
+      return !(r->n <= gb::kSmallMaxN && r->m < (1ll << 31));
+    });
+    p.nlarge = (int32_t)p.reqs.size() - nsmall;
+  } else {
+    p.nlarge = (int32_t)p.reqs.size();
+  }
   p.vbase.assign(1, 0);
   p.ebase.assign(1, 0);
   for (Req* r : p.reqs) {
@@ -247,20 +279,59 @@ gb_status part_launch(gb_server* sv, Part& p, int kind) {
   }
   if (cudaMemcpyAsync(p.h_bad, p.d_bad, (size_t)count * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return GB_ERR_CUDA;
-  // grow the context workspace ahead of need, so it is rarely reallocated
-  if (p.n > c->cap_n) {
-    int64_t want = std::max<int64_t>(p.n, (int64_t)c->cap_n * 3 / 2);
+  // grow the context workspace (the union run's) ahead of need, so it is
+  // rarely reallocated
+  const int64_t n_union = p.vbase[(size_t)p.nlarge];
+  if (p.nlarge > 0 && n_union > c->cap_n) {
+    int64_t want = std::max<int64_t>(n_union, (int64_t)c->cap_n * 3 / 2);
     if (want > 0x7fffffffll) want = 0x7fffffffll;
     gb_status ws = gb::reserve_workspace(c, (int32_t)want);
     if (ws != GB_OK) return ws;
   }
-  gb_status st = gb::batch_create(c, count, p.vbase.data(), p.m, p.d_src, p.d_dst, false, true,
-                                  &p.batch);
-  if (st != GB_OK) return st;
   if (cudaMallocAsync(&p.d_labels, (size_t)(p.n > 0 ? p.n : 1) * 4, s) != cudaSuccess) return GB_ERR_OOM;
-  st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels, &sv->opts, nullptr,
-                     false);
-  if (st != GB_OK) return st;
+  if (p.nlarge > 0) {
+    gb_status st = gb::batch_create(c, p.nlarge, p.vbase.data(), p.ebase[(size_t)p.nlarge],
+                                    p.d_src, p.d_dst, false, true, &p.batch);
+    if (st != GB_OK) return st;
+    st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels, &sv->opts,
+                       nullptr, false);
+    if (st != GB_OK) return st;
+  }
+  if (p.nlarge < count) {
+    // one block per small request, from its edges (global ids: id_base)
+    const int32_t ns = count - p.nlarge;
+    const int64_t e0 = p.ebase[(size_t)p.nlarge];
+    const int64_t ms = p.m - e0;
+    if (kind == 0 && ms > 0 &&
+        cudaMallocAsync(&p.d_scratch, (size_t)ms * 8, s) != cudaSuccess)
+      return GB_ERR_OOM;
+    std::vector<gb::SmallDesc> h((size_t)ns);
+    int32_t max_n = 1;
+    for (int32_t i = 0; i < ns; ++i) {
+      const size_t g = (size_t)(p.nlarge + i);
+      gb::SmallDesc& d = h[(size_t)i];
+      d.n = (int32_t)(p.vbase[g + 1] - p.vbase[g]);
+      d.id_base = (int32_t)p.vbase[g];
+      d.m = p.ebase[g + 1] - p.ebase[g];
+      d.src = p.d_src + p.ebase[g];
+      d.dst = p.d_dst + p.ebase[g];
+      d.adj_scratch = kind == 0 ? p.d_scratch + 2 * (p.ebase[g] - e0) : nullptr;
+      d.labels = p.d_labels + p.vbase[g];
+      max_n = std::max(max_n, d.n);
+    }
+    if (cudaMallocAsync(&p.d_descs, (size_t)ns * sizeof(gb::SmallDesc), s) != cudaSuccess)
+      return GB_ERR_OOM;
+    // (pageable source: the copy is staged before the call returns)
+    if (cudaMemcpyAsync(p.d_descs, h.data(), (size_t)ns * sizeof(gb::SmallDesc),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), s) != cudaSuccess)
+      return GB_ERR_CUDA;
+    const int32_t max_steps = sv->opts.max_steps > 0 ? sv->opts.max_steps : (1 << 30);
+    if (gb::launch_small(kind, h[0], p.d_descs, ns, max_n, max_steps, &c->d_ctl->err, s) !=
+            cudaSuccess ||
+        gb::launch_latch(c->d_ctl, c->d_sticky, s) != cudaSuccess)
+      return GB_ERR_CUDA;
+  }
   if (p.n > 0 &&
       cudaMemcpyAsync(p.h_labels, p.d_labels, (size_t)p.n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return GB_ERR_CUDA;

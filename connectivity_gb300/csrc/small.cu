@@ -130,7 +130,7 @@ __device__ int32_t block_argmax(long long key, int32_t id, int32_t* ctl) {
     if (k2 > key || (k2 == key && i2 < id)) { key = k2; id = i2; }
   }
   long long* rk = reinterpret_cast<long long*>(ctl + cRed);  // kSW long longs
-  int32_t* ri = ctl + cRed + 2 * kSW;                          // beyond them: cScan area
+  int32_t* ri = ctl + cRed + 2 * kSW;                          // then kSW ids
   __syncthreads();
   if (lane == 0) { rk[wid] = key; ri[wid] = id; }
   __syncthreads();
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
     for (int v = tid; v < n; v += kST) lab[v] = v;
     __syncthreads();
     for (long long e = tid; e < D.m; e += kST) {
-      const int32_t a = D.src[e], b = D.dst[e];
+      const int32_t a = D.src[e] - D.id_base, b = D.dst[e] - D.id_base;
       if ((unsigned)a >= (unsigned)n || (unsigned)b >= (unsigned)n) {
         ctl[cBad] = 1;
         continue;
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
     }
     __syncthreads();
     for (long long e = tid; e < D.m; e += kST) {
-      const int32_t a = D.src[e], b = D.dst[e];
+      const int32_t a = D.src[e] - D.id_base, b = D.dst[e] - D.id_base;
       if ((unsigned)a >= (unsigned)n || (unsigned)b >= (unsigned)n) {
         ctl[cBad] = 1;
         continue;
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
     int32_t* so = D.adj_scratch;
     int32_t* si = D.adj_scratch + D.m;
     for (long long e = tid; e < D.m; e += kST) {
-      const int32_t a = D.src[e], b = D.dst[e];
+      const int32_t a = D.src[e] - D.id_base, b = D.dst[e] - D.id_base;
       so[atomicAdd(&cnt_o[a], 1)] = b;
       si[atomicAdd(&cnt_i[b], 1)] = a;
     }

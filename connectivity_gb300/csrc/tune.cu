@@ -93,7 +93,7 @@ gb_status time_runs(gb_ctx* c, const gb_opts& o, int reps, Run run, double* ms) 
 template <class Run>
 gb_status tune(gb_ctx* c, int reps, Run run, gb_opts* best, double* ms_out) {
   const std::vector<Param> params = {
-      {7, {0, 1}},  // one thread block (graphs of at most 6144 vertices) or the grid
+      {7, {0, 1, 2}},  // the grid, automatic, one thread block (at most 6144 vertices)
       {0, {128, 512, 2048}},
       {1, {8192, 32768, 131072}},
       {2, {1, 2, 4}},

@@ -101,14 +101,16 @@ typedef struct gb_opts {
                           the Kokkos variant's manhattan-global FW-BW
                           (kokkos_scc/fwbw_manhattan_global.cpp:186-289).
                           An autotuner candidate. */
-  int32_t small_path;  /* 1 (default): a graph of at most 6144 vertices runs
-                          in one thread block with all its per-vertex state
-                          in shared memory (trim to the fixed point, FW-BW,
-                          colour rounds; WCC by union-find), no cooperative
-                          grid; 0: always the cooperative run kernel.  Needs
-                          canonical = 1 (otherwise the cooperative kernel
-                          runs); the statistics then hold the times only.
-                          No reference counterpart. */
+  int32_t small_path;  /* graphs of at most 6144 vertices can run in one
+                          thread block with all their per-vertex state in
+                          shared memory (trim to the fixed point, FW-BW,
+                          colour rounds; WCC by union-find), with no
+                          cooperative grid.  1 (default): for a device graph
+                          of at most 40960 edges, and for every such edge
+                          list (gb_scc_edges, served requests); 2: whenever
+                          the graph fits; 0: never.  Needs canonical = 1;
+                          the statistics then hold the times only.  No
+                          reference counterpart. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);

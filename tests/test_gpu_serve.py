@@ -104,3 +104,24 @@ def test_server_rejects_oversize_and_bad_arguments():
         sv.submit(gb.Server.SCC, 0, np.zeros(0, np.int32), np.zeros(0, np.int32))
     sv.close()
     sctx.close()
+
+
+@pytest.mark.parametrize("small_path", [1, 0])
+@pytest.mark.parametrize("count,max_graphs", [(40, 64), (700, 700)])
+def test_served_one_block_and_union_paths(ctx, small_path, count, max_graphs):
+    """Merged sets that mix small requests (one block each) with large ones
+    (the union), and sets with more small requests than one launch wave
+    (all on the union), all arriving at once: every request gets its labels
+    alone."""
+    reqs = requests(count, seed=21, median=1500.0, n_max=40000)
+    sctx = gb.Context(0)
+    sv = gb.Server(sctx, max_graphs=max_graphs)
+    sv.set_opts(gb.opts(small_path=small_path))
+    ids = [sv.submit(k, n, s, d, arrival_ns=0) for k, n, s, d in reqs]
+    sv.start()
+    for i, (rid, r) in enumerate(zip(ids, reqs)):
+        lab, _ = sv.wait(rid)
+        if i % 7 == 0 or r[1] > 6144:
+            assert np.array_equal(lab, alone(ctx, *r)), i
+    sv.close()
+    sctx.close()

@@ -28,7 +28,7 @@ def _check_all(ctx, kind, n, s, d):
     want = _want(kind, n, s, d)
     g = gb.Graph.from_edges(ctx, n, s, d)
     run = ctx.scc if kind == "scc" else ctx.wcc
-    lab, st = run(g, o=gb.opts(small_path=1), stats=True)
+    lab, st = run(g, o=gb.opts(small_path=2), stats=True)
     assert np.array_equal(lab, want)
     assert st.grid_blocks == 1  # the one-block path ran
     edges = ctx.scc_edges if kind == "scc" else ctx.wcc_edges
@@ -104,7 +104,7 @@ def test_boundary_sizes(ctx):
     for n in (MAX_N, MAX_N + 1):
         _, s, d = gb.rmat_edges_n(n, 8, 9)
         g = gb.Graph.from_edges(ctx, n, s, d)
-        lab, st = ctx.scc(g, stats=True)
+        lab, st = ctx.scc(g, o=gb.opts(small_path=2), stats=True)
         assert np.array_equal(lab, _want("scc", n, s, d))
         assert (st.grid_blocks == 1) == (n <= MAX_N)
         assert np.array_equal(ctx.scc_edges(n, s, d), lab)
@@ -147,3 +147,16 @@ def test_async_and_canonical_off_use_the_grid(ctx):
     ctx.sync()
     assert out.cpu().tolist() == [0, 0, 2]
     g.close()
+
+
+def test_automatic_choice_by_edges(ctx):
+    """small_path 1 (the default) takes the one-block path for a device graph
+    of at most 40960 edges and the grid above; both give the same labels."""
+    for ef, want_small in ((4, True), (32, False)):
+        _, s, d = gb.rmat_edges_n(3000, ef, 13)
+        g = gb.Graph.from_edges(ctx, 3000, s, d)
+        assert (s.size <= 40960) == want_small
+        lab, st = ctx.scc(g, stats=True)
+        assert (st.grid_blocks == 1) == want_small
+        assert np.array_equal(lab, _want("scc", 3000, s, d))
+        g.close()
