@@ -434,6 +434,10 @@ def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu, ws=1, rank=0):
         "autotuned": {"graphs_per_s": round(b.count / (tuned["ms"] / 1e3), 1),
                       "defaults_graphs_per_s": round(b.count / (tuned["default_ms"] / 1e3), 1),
                       "opts": tuned["opts"]},
+        # the graphs of each vertex-count class as a batch of their own,
+        # tuned against the defaults: the most that options chosen per size
+        # class could gain inside one merged run
+        "per_class_tuning": gbtune.tune_batch_by_class(ctx, ns, efs, seeds, 0, reps=2),
     }
     if want_cpu and cpu_sample > 0:
         import oracle
