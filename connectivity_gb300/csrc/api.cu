@@ -271,9 +271,10 @@ gb_status finish_run(gb_ctx* c, const gb_graph* g, gb_stats* st) {
 // True when a run of g with options o takes the one-block path (small.cu).
 // small_path 1 (automatic) takes it while the graph has at most
 // kSmallAutoEdges edges: above that the one block's passes over the edges
-// cost more than the cooperative grid's steps (measured on GB300: 103
-// against 214 us at 2,000 vertices and 25,000 edges, 235 against 222 us at
-// 6,000 and 73,000); 2 takes it whenever the graph fits.
+// cost more than the cooperative grid's steps (measured on GB300, SCC:
+// 101 against 215 us at 2,000 vertices and 25,000 edges, 173 against
+// 220 us at 4,000 and 52,000, 233 against 222 us at 6,000 and 73,000);
+// 2 takes it whenever the graph fits.
 bool use_small(const gb_graph* g, const gb_opts* o) {
   if (g->n > gb::kSmallMaxN || g->m >= (1ll << 31)) return false;
   const int32_t mode = o ? o->small_path : 1;

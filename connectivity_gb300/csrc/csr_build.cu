@@ -249,19 +249,19 @@ __global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t*
 }
 
 // The pull hint of a vertex: its neighbour of largest total degree, the
-// first one in adjacency order on ties (-1 without neighbours).
-//
-// A warp takes 32 consecutive vertices.  Their edges (of vertices with at
-// most kHintWarp neighbours) are numbered by a warp scan of the degrees and
-// walked 32 at a time, so lane k reads edge k of the run: the 32 vertices'
-// adjacency is one contiguous range of the CSR, and the reads coalesce.
-// Each edge finds its vertex by a binary search over the scan (in shared
-// memory); keys (degree << 32 | ~index) are reduced per vertex by a
-// segmented warp maximum, and the last lane of each vertex folds the result
-// into the vertex's slot in shared memory: the largest degree wins, then the
-// smallest index.  Vertices with more neighbours go to `heavy` for k_hint_heavy (a
-// block per vertex), so no warp walks a hub's edges alone.
-constexpr int kHintWarp = 4096;
+// first one in adjacency order on ties (-1 without neighbours).  Vertices
+// are taken in three tiers by degree, each spread evenly over the grid:
+//   <= kHintThread neighbours: one thread, four loads in flight at a time
+//      (most vertices of a power-law graph);
+//   <= kHintWarp: appended to `mid`, then a warp per vertex in k_hint_mid,
+//      warps taking the list's vertices in turn;
+//   more: appended to `heavy`, then a block per vertex in k_hint_heavy.
+// Walking the middle tier inside the pass that finds it (a warp over the
+// middle vertices among its own 32) or cutting the adjacency into
+// warp-sized pieces of 32 consecutive vertices leaves long tails: R-MAT
+// puts its high-degree vertices at neighbouring ids.
+constexpr int kHintThread = 32;
+constexpr int kHintWarp = 2048;
 constexpr int kHintBlock = 256;
 
 __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& best_d,
@@ -274,74 +274,65 @@ __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& bes
 
 __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* off,
                                                      const int32_t* adj, const int32_t* deg,
-                                                     int32_t* hint, int32_t* heavy,
+                                                     int32_t* hint, int32_t* mid,
+                                                     int32_t* nmid, int32_t* heavy,
                                                      int32_t* nheavy) {
-  constexpr int W = kHintBlock / 32;
-  __shared__ int64_t s_start[W][32];
-  __shared__ int32_t s_pre[W][32];
-  __shared__ unsigned long long s_best[W][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t wstride = (int64_t)gridDim.x * W * 32;
-  for (int64_t base = ((int64_t)blockIdx.x * W + wid) * 32; base < n; base += wstride) {
-    const int64_t v = base + lane;
-    int64_t s = 0, d = 0;
-    if (v < n) {
-      s = off[v];
-      d = off[v + 1] - s;
-    }
-    const bool is_heavy = d > kHintWarp;
-    if (is_heavy) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+    const int64_t s = off[v], d = off[v + 1] - s;
+    if (d > kHintWarp) {
       heavy[atomicAdd(nheavy, 1)] = (int32_t)v;
-      d = 0;  // walked by k_hint_heavy
-    }
-    // exclusive scan of the degrees over the warp
-    int32_t inc = (int32_t)d;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += y;
-    }
-    const int32_t total = __shfl_sync(0xffffffffu, inc, 31);
-    s_start[wid][lane] = s;
-    s_pre[wid][lane] = inc - (int32_t)d;
-    s_best[wid][lane] = 0ull;
-    __syncwarp();
-    for (int32_t e0 = 0; e0 < total; e0 += 32) {
-      const int32_t e = e0 + lane;
-      const bool act = e < total;
-      // the last vertex whose run starts at or before e
-      int j = 0;
-      for (int step = 16; step; step >>= 1)
-        if (s_pre[wid][j + step] <= e) j += step;
-      unsigned long long key = 0ull;
-      if (act) {
-        const int32_t k = e - s_pre[wid][j];
-        const int32_t dd = deg[adj[s_start[wid][j] + k]];
-        key = ((unsigned long long)(uint32_t)dd << 32) |
-              (unsigned long long)(0xffffffffu - (uint32_t)k);
-      } else {
-        j = 32;  // a segment of its own, never written
+    } else if (d > kHintThread) {
+      mid[atomicAdd(nmid, 1)] = (int32_t)v;
+    } else {
+      int32_t best_d = -1;
+      int64_t best_e = -1;
+      for (int64_t e = 0; e < d; e += 4) {
+        const int32_t a0 = adj[s + e];
+        const int32_t a1 = e + 1 < d ? adj[s + e + 1] : -1;
+        const int32_t a2 = e + 2 < d ? adj[s + e + 2] : -1;
+        const int32_t a3 = e + 3 < d ? adj[s + e + 3] : -1;
+        const int32_t d0 = deg[a0];
+        const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
+        const int32_t d2 = a2 >= 0 ? deg[a2] : -1;
+        const int32_t d3 = a3 >= 0 ? deg[a3] : -1;
+        if (d0 > best_d) { best_d = d0; best_e = e; }
+        if (d1 > best_d) { best_d = d1; best_e = e + 1; }
+        if (d2 > best_d) { best_d = d2; best_e = e + 2; }
+        if (d3 > best_d) { best_d = d3; best_e = e + 3; }
       }
-      // lanes of one vertex are adjacent: a segmented maximum over the warp,
-      // then the segment's last lane folds it into the vertex's slot
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, key, o);
-        const int yj = __shfl_up_sync(0xffffffffu, j, o);
-        if (lane >= o && yj == j && y > key) key = y;
-      }
-      const int nj = __shfl_down_sync(0xffffffffu, j, 1);
-      if (act && (lane == 31 || nj != j) && key > s_best[wid][j]) s_best[wid][j] = key;
-      __syncwarp();
+      hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
     }
-    __syncwarp();
-    if (v < n && !is_heavy) {
-      if (d == 0) {
-        hint[v] = -1;
-      } else {
-        const uint32_t k = 0xffffffffu - (uint32_t)(s_best[wid][lane] & 0xffffffffull);
-        hint[v] = adj[s + k];
-      }
+  }
+}
+
+// A warp per middle-tier vertex, the list spread over every warp.
+__global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, const int32_t* adj,
+                                                         const int32_t* deg, int32_t* hint,
+                                                         const int32_t* mid,
+                                                         const int32_t* nmid) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int32_t nm = *nmid;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nm; i += warps) {
+    const int32_t v = mid[i];
+    const int64_t s = off[v], d = off[v + 1] - s;
+    int32_t best_d = -1;
+    int64_t best_e = -1;
+    for (int64_t e = lane; e < d; e += 64) {
+      const int32_t a0 = adj[s + e];
+      const int32_t a1 = e + 32 < d ? adj[s + e + 32] : -1;
+      const int32_t d0 = deg[a0];
+      const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
+      if (d0 > best_d) { best_d = d0; best_e = e; }
+      if (d1 > best_d) { best_d = d1; best_e = e + 32; }
     }
-    __syncwarp();
+    for (int o = 16; o; o >>= 1) {
+      const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
+      const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
+      hint_better(d2, e2, best_d, best_e);
+    }
+    if (lane == 0) hint[v] = adj[s + best_e];
   }
 }
 
@@ -616,22 +607,29 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  // scratch: total degrees (n), the heavy list (n) and two list counts
+  // scratch: total degrees (n), the middle and heavy lists (n each) and
+  // their counts, one pair per side
   int32_t* deg = nullptr;
-  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 2 + 2) * 4, s);
+  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 3 + 4) * 4, s);
   if (e != cudaSuccess) return e;
-  int32_t* heavy = deg + n;
-  int32_t* nheavy = heavy + n;
-  cudaMemsetAsync(nheavy, 0, 8, s);
+  int32_t* mid = deg + n;
+  int32_t* heavy = mid + n;
+  int32_t* cnt = heavy + n;  // [0] mid out, [1] heavy out, [2] mid in, [3] heavy in
+  cudaMemsetAsync(cnt, 0, 16, s);
   k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
   const int g = grid_for(n);
-  k_hint<<<g, kHintBlock, 0, s>>>(n, out_off, out_adj, deg, hint_out, heavy, nheavy);
-  k_hint_heavy<<<152 * 2, 1024, 0, s>>>(out_off, out_adj, deg, hint_out, heavy, nheavy);
-  if (in_off != nullptr && hint_in != nullptr) {
-    // the in side reuses the heavy list with its own count; stream order
-    // puts it after the out side's heavy pass has read the list
-    k_hint<<<g, kHintBlock, 0, s>>>(n, in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
-    k_hint_heavy<<<152 * 2, 1024, 0, s>>>(in_off, in_adj, deg, hint_in, heavy, nheavy + 1);
+  const int gw = 152 * 8;  // 8 blocks of 8 warps per SM for the list passes
+  for (int side = 0; side < 2; ++side) {
+    const int64_t* off = side == 0 ? out_off : in_off;
+    const int32_t* adj = side == 0 ? out_adj : in_adj;
+    int32_t* hint = side == 0 ? hint_out : hint_in;
+    if (off == nullptr || hint == nullptr) continue;
+    // (the in side reuses the lists after the out side's passes, in stream
+    // order)
+    k_hint<<<g, kHintBlock, 0, s>>>(n, off, adj, deg, hint, mid, cnt + 2 * side, heavy,
+                                    cnt + 2 * side + 1);
+    k_hint_mid<<<gw, kHintBlock, 0, s>>>(off, adj, deg, hint, mid, cnt + 2 * side);
+    k_hint_heavy<<<152 * 2, 1024, 0, s>>>(off, adj, deg, hint, heavy, cnt + 2 * side + 1);
   }
   cudaFreeAsync(deg, s);
   e = cudaGetLastError();

@@ -234,7 +234,7 @@ cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s);
 constexpr int32_t kSmallMaxN = 6144;
 // edges up to which a device graph takes the one-block path by default (an
 // edge list always does: it saves the CSR build)
-constexpr int64_t kSmallAutoEdges = 40960;
+constexpr int64_t kSmallAutoEdges = 65536;
 struct SmallDesc {
   int32_t n;
   int32_t id_base;          // subtracted from every adjacency entry (batch unions)

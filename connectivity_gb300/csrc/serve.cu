@@ -12,12 +12,12 @@
 // request's labels are the ones it gets alone (the batch path guarantees
 // it); latency is completion minus arrival on the server clock.
 //
-// A merged set of up to kSmallWave small requests (at most kSmallMaxN
-// vertices each) skips the union build: each such request runs in one
-// thread block straight from its uploaded edges (small.cu), all of them in
-// one launch, so at low and moderate load a request costs one short launch
-// instead of a radix-sort CSR build and a cooperative run.  Larger sets, and
-// the large requests of any set, take the union path.
+// A merged set of up to kSmallWave requests that are all small (at most
+// kSmallMaxN vertices and kSmallAutoEdges edges each) skips the union
+// build: each request runs in one thread block straight from its uploaded
+// edges (small.cu), all of them in one launch, so at low and moderate load a
+// request costs one short launch instead of a radix-sort CSR build and a
+// cooperative run.  Any other set takes the union path as a whole.
 //
 // The reference has no serving; its equivalent is one run_scc / run_cc call
 // per request (multistep/scc_main.cpp:210, cc_main.cpp:184).
@@ -109,8 +109,8 @@ struct Part {
   int32_t* d_scratch = nullptr;      // their CSRs (SCC)
 };
 
-// Small requests of one merged set run one block each when there are at
-// most this many (two waves of one block per SM); more go to the union.
+// A set of small requests runs one block each when it has at most this
+// many (two waves of one block per SM); a larger set goes to the union.
 constexpr int32_t kSmallWave = 304;
 
 struct Flight {
@@ -189,18 +189,14 @@ void part_release(gb_server* sv, Part& p) {
 // Copies the admitted requests' edges to the device (copy stream).  The
 // requests that take the union path come first.
 gb_status part_upload(gb_server* sv, Part& p) {
-  int32_t nsmall = 0;
-  if (sv->opts.small_path && sv->opts.canonical)
-    for (Req* r : p.reqs)
-      if (r->n <= gb::kSmallMaxN && r->m < (1ll << 31)) ++nsmall;
-  if (nsmall > 0 && nsmall <= kSmallWave) {
-    std::stable_partition(p.reqs.begin(), p.reqs.end(), [](const Req* r) {
-      return !(r->n <= gb::kSmallMaxN && r->m < (1ll << 31));
-    });
-    p.nlarge = (int32_t)p.reqs.size() - nsmall;
-  } else {
-    p.nlarge = (int32_t)p.reqs.size();
-  }
+  // all small and few: one block each; otherwise one union run for all
+  // (a union run and a one-block launch of the same set would run one
+  // after the other, and the set's latency would be their sum)
+  bool all_small = sv->opts.small_path && sv->opts.canonical &&
+                   (int32_t)p.reqs.size() <= kSmallWave;
+  for (const Req* r : p.reqs)
+    if (!(r->n <= gb::kSmallMaxN && r->m <= gb::kSmallAutoEdges)) all_small = false;
+  p.nlarge = all_small ? 0 : (int32_t)p.reqs.size();
   p.vbase.assign(1, 0);
   p.ebase.assign(1, 0);
   for (Req* r : p.reqs) {

@@ -106,7 +106,7 @@ typedef struct gb_opts {
                           shared memory (trim to the fixed point, FW-BW,
                           colour rounds; WCC by union-find), with no
                           cooperative grid.  1 (default): for a device graph
-                          of at most 40960 edges, and for every such edge
+                          of at most 65536 edges, and for every such edge
                           list (gb_scc_edges, served requests); 2: whenever
                           the graph fits; 0: never.  Needs canonical = 1;
                           the statistics then hold the times only.  No
