@@ -152,11 +152,11 @@ def test_async_and_canonical_off_use_the_grid(ctx):
 def test_automatic_choice_by_edges(ctx):
     """small_path 1 (the default) takes the one-block path for a device graph
     of at most 65536 edges and the grid above; both give the same labels."""
-    for ef, want_small in ((4, True), (32, False)):
-        _, s, d = gb.rmat_edges_n(3000, ef, 13)
-        g = gb.Graph.from_edges(ctx, 3000, s, d)
+    for n, ef, want_small in ((3000, 4, True), (6000, 32, False)):
+        _, s, d = gb.rmat_edges_n(n, ef, 13)
+        g = gb.Graph.from_edges(ctx, n, s, d)
         assert (s.size <= 65536) == want_small
         lab, st = ctx.scc(g, stats=True)
         assert (st.grid_blocks == 1) == want_small
-        assert np.array_equal(lab, _want("scc", 3000, s, d))
+        assert np.array_equal(lab, _want("scc", n, s, d))
         g.close()
