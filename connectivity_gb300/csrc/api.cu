@@ -732,14 +732,19 @@ static const void* pinned_view(const void* p) {
 // Pinned host arrays are read by the ingest kernels directly (one crossing
 // of the host link, checked on the way); other memory is copied, widened
 // and then checked on the device.
+// The reference's 32-bit CSR into the staged device graph.  Only the
+// out-CSR and the in-offsets cross the host link: the in-lists are rebuilt
+// on the device from the out-CSR (in_csr_from_out), which costs less than
+// copying them (half the bytes of the graph), so in_array is not read.  The
+// order within an in-list is then not the caller's; no label depends on it.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
                             const uint32_t* odl, const int32_t* in_array, const uint32_t* idl) {
+  (void)in_array;
   {
     const void* vo = pinned_view(odl);
     const void* va = m > 0 ? pinned_view(out_array) : odl;
     const void* vi = g->symmetric ? odl : pinned_view(idl);
-    const void* vb = g->symmetric || m == 0 ? odl : pinned_view(in_array);
-    if (vo && va && vi && vb) {
+    if (vo && va && vi) {
       int* d_bad = nullptr;
       CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
       gb_status s = GB_OK;
@@ -748,8 +753,10 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
         e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
                              d_bad, c->stream);
       if (e == cudaSuccess && !g->symmetric)
-        e = gb::ingest_csr32(n, m, (const uint32_t*)vi, (const int32_t*)vb, g->in_off, g->in_adj,
-                             d_bad, c->stream);
+        e = gb::ingest_offsets32(n, m, (const uint32_t*)vi, g->in_off, d_bad, c->stream);
+      if (e == cudaSuccess && !g->symmetric)
+        e = gb::in_csr_from_out(n, m, g->out_off, g->out_adj, g->in_off, g->in_adj, d_bad,
+                                c->stream);
       int bad = 0;
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -771,11 +778,28 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
   if (s == GB_OK && !g->symmetric) {
     s = upload(c, tmp, idl, (size_t)(n + 1) * 4);
     if (s == GB_OK) CK(gb::widen_offsets(tmp, g->in_off, (int64_t)n + 1, c->stream), "widen");
-    if (s == GB_OK) s = upload(c, g->in_adj, in_array, (size_t)m * 4);
   }
   cudaFreeAsync(tmp, c->stream);
   if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
-  if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
+  if (s == GB_OK && !g->symmetric) {
+    int* d_bad = nullptr;
+    CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
+    int bad = 0;
+    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess)
+      e = gb::in_csr_from_out(n, m, g->out_off, g->out_adj, g->in_off, g->in_adj, d_bad,
+                              c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFreeAsync(d_bad, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "in-CSR");
+    if (bad) {
+      gb_set_error("CSR check: %s", "the in-degree list does not match the out-CSR");
+      return GB_ERR_INVALID;
+    }
+    s = validate_csr(c, n, m, g->in_off, g->in_adj);
+  }
   return s;
 }
 

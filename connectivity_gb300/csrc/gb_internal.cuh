@@ -265,6 +265,15 @@ cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaS
 // an int64-offset device CSR, checked on the way (*d_bad |= 1 on a bad CSR).
 cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
                          int64_t* off, int32_t* adj, int* d_bad, cudaStream_t s);
+// The offsets alone (n + 1 of them, checked the same way).
+cudaError_t ingest_offsets32(int32_t n, int64_t m, const uint32_t* h_off, int64_t* off,
+                             int* d_bad, cudaStream_t s);
+// The in-CSR of a graph from its out-CSR and its in-offsets (every edge
+// placed at the next free slot of its target's in-list, so the order within
+// an in-list is not the input order).  *d_bad |= 1 when an id is outside
+// [0, n) or the in-offsets do not match the out-CSR.  Does not wait.
+cudaError_t in_csr_from_out(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
+                            const int64_t* in_off, int32_t* in_adj, int* d_bad, cudaStream_t s);
 // Batch labels: global ids -> ids local to each graph.
 cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
                             cudaStream_t s);
