@@ -6,6 +6,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "../../include/gbconn.h"
 #include "api_internal.h"
@@ -59,7 +60,8 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(2 * G * 8);
+  const size_t hs = align256((size_t)2 * gb::kHubWords * 4);
+  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(2 * G * 8) + hs;
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -90,6 +92,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.done = (uint32_t*)take(bm);
   w.blk_i = (int32_t*)take(align256(2 * G * 4));
   w.blk_l = (long long*)take(align256(2 * G * 8));
+  w.hubsnap = (uint32_t*)take(hs);
   w.ctl = c->d_ctl;
   c->cap_n = n;
   return GB_OK;
@@ -148,9 +151,12 @@ void graph_free(gb_graph* g) {
   dev_free(g->in_adj, g->pooled, s);
   dev_free(g->hint_out, g->pooled, s);
   dev_free(g->hint_in, g->pooled, s);
+  dev_free(g->hubs, g->pooled, s);
   g->out_off = g->in_off = nullptr;
   g->out_adj = g->in_adj = nullptr;
   g->hint_out = g->hint_in = nullptr;
+  g->hubs = nullptr;
+  g->nhubs = 0;
 }
 
 // Builds the pull hints of a graph whose CSR is complete on the device.
@@ -163,6 +169,12 @@ gb_status graph_hints(gb_ctx* c, gb_graph* g) {
   CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
                      c->stream),
      "hints");
+  if (!g->hubs)
+    CK(dev_alloc((void**)&g->hubs, (size_t)gb::kHubMax * 4, g->pooled, g->pool_stream),
+       "hub allocation");
+  CK(gb::build_hubs(g->n, g->out_off, g->symmetric ? nullptr : g->in_off, g->hint_out,
+                    g->hint_in, g->hubs, &g->nhubs, c->stream),
+     "hubs");
   return GB_OK;
 }
 }  // namespace gb
@@ -386,6 +398,10 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
     gv.in = kind == gb::kSCC ? gv.out : gb::Csr{nullptr, nullptr, nullptr};
   } else {
     gv.in = {g->in_off, g->in_adj, g->hint_in};
+  }
+  if (g->hint_out && g->hubs && g->nhubs > 0) {
+    gv.hubs = g->hubs;
+    gv.nhubs = g->nhubs;
   }
   gv.batch = gb::BatchView{};
   cudaStream_t sm = c->stream;
@@ -732,19 +748,14 @@ static const void* pinned_view(const void* p) {
 // Pinned host arrays are read by the ingest kernels directly (one crossing
 // of the host link, checked on the way); other memory is copied, widened
 // and then checked on the device.
-// The reference's 32-bit CSR into the staged device graph.  Only the
-// out-CSR and the in-offsets cross the host link: the in-lists are rebuilt
-// on the device from the out-CSR (in_csr_from_out), which costs less than
-// copying them (half the bytes of the graph), so in_array is not read.  The
-// order within an in-list is then not the caller's; no label depends on it.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
                             const uint32_t* odl, const int32_t* in_array, const uint32_t* idl) {
-  (void)in_array;
   {
     const void* vo = pinned_view(odl);
     const void* va = m > 0 ? pinned_view(out_array) : odl;
     const void* vi = g->symmetric ? odl : pinned_view(idl);
-    if (vo && va && vi) {
+    const void* vb = g->symmetric || m == 0 ? odl : pinned_view(in_array);
+    if (vo && va && vi && vb) {
       int* d_bad = nullptr;
       CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
       gb_status s = GB_OK;
@@ -753,10 +764,8 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
         e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
                              d_bad, c->stream);
       if (e == cudaSuccess && !g->symmetric)
-        e = gb::ingest_offsets32(n, m, (const uint32_t*)vi, g->in_off, d_bad, c->stream);
-      if (e == cudaSuccess && !g->symmetric)
-        e = gb::in_csr_from_out(n, m, g->out_off, g->out_adj, g->in_off, g->in_adj, d_bad,
-                                c->stream);
+        e = gb::ingest_csr32(n, m, (const uint32_t*)vi, (const int32_t*)vb, g->in_off, g->in_adj,
+                             d_bad, c->stream);
       int bad = 0;
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -778,28 +787,11 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
   if (s == GB_OK && !g->symmetric) {
     s = upload(c, tmp, idl, (size_t)(n + 1) * 4);
     if (s == GB_OK) CK(gb::widen_offsets(tmp, g->in_off, (int64_t)n + 1, c->stream), "widen");
+    if (s == GB_OK) s = upload(c, g->in_adj, in_array, (size_t)m * 4);
   }
   cudaFreeAsync(tmp, c->stream);
   if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
-  if (s == GB_OK && !g->symmetric) {
-    int* d_bad = nullptr;
-    CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
-    int bad = 0;
-    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
-    if (e == cudaSuccess)
-      e = gb::in_csr_from_out(n, m, g->out_off, g->out_adj, g->in_off, g->in_adj, d_bad,
-                              c->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFreeAsync(d_bad, c->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "in-CSR");
-    if (bad) {
-      gb_set_error("CSR check: %s", "the in-degree list does not match the out-CSR");
-      return GB_ERR_INVALID;
-    }
-    s = validate_csr(c, n, m, g->in_off, g->in_adj);
-  }
+  if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
   return s;
 }
 
@@ -889,6 +881,18 @@ gb_status gb_graph_hints_to_host(const gb_graph* g, int32_t* hint_out, int32_t* 
     CK(cudaMemcpy(hint_out, g->hint_out, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
   if (hint_in && g->n && g->hint_in)
     CK(cudaMemcpy(hint_in, g->hint_in, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
+  // hints that name a hub by rank become vertex ids again
+  std::vector<int32_t> hubs((size_t)(g->nhubs > 0 ? g->nhubs : 1));
+  if (g->nhubs > 0)
+    CK(cudaMemcpy(hubs.data(), g->hubs, (size_t)g->nhubs * 4, cudaMemcpyDeviceToHost), "download");
+  for (int32_t* h : {hint_out, g->hint_in ? hint_in : nullptr}) {
+    if (!h) continue;
+    for (int32_t v = 0; v < g->n; ++v)
+      if (h[v] <= -2) {
+        const int32_t r = -(h[v] + 2);
+        h[v] = r < g->nhubs ? hubs[(size_t)r] : -1;
+      }
+  }
   return GB_OK;
 }
 
@@ -937,7 +941,10 @@ gb_status gb_graph_set_hints(gb_ctx* c, gb_graph* g, int32_t on) {
   if (on) return graph_hints(c, g);
   gb::dev_free(g->hint_out, g->pooled, g->pool_stream);
   gb::dev_free(g->hint_in, g->pooled, g->pool_stream);
+  gb::dev_free(g->hubs, g->pooled, g->pool_stream);
   g->hint_out = g->hint_in = nullptr;
+  g->hubs = nullptr;
+  g->nhubs = 0;
   return GB_OK;
 }
 

@@ -8,13 +8,13 @@
 // region, as in the reference), followed by an offsets kernel that writes
 // off[v] at every boundary of the sorted keys.
 #include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
 #include <cub/device/device_select.cuh>
 
 #include "gb_internal.cuh"
 #include "gen_common.h"
 
 #include <cstring>
+#include <vector>
 
 namespace gb {
 namespace {
@@ -458,15 +458,10 @@ cudaError_t check_csr_flag(int32_t n, int64_t m, const int64_t* off, const int32
   return cudaGetLastError();
 }
 
-cudaError_t ingest_offsets32(int32_t n, int64_t m, const uint32_t* h_off, int64_t* off,
-                             int* d_bad, cudaStream_t s) {
-  k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_off, off, n, m, d_bad);
-  return cudaGetLastError();
-}
-
 cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
                          int64_t* off, int32_t* adj, int* d_bad, cudaStream_t s) {
-  cudaError_t e = ingest_offsets32(n, m, h_off, off, d_bad, s);
+  k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_off, off, n, m, d_bad);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || m == 0) return e;
   k_ingest_adj<<<grid_for(m / 4 + 1), 256, 0, s>>>(h_adj, adj, m, n, d_bad);
   return cudaGetLastError();
@@ -693,86 +688,83 @@ cudaError_t rmat_edges_device(int32_t n, int edge_factor, uint64_t seed, gb_rmat
   return cudaGetLastError();
 }
 
-// ---- the in-CSR from the out-CSR ------------------------------------------
-// head[off[u]] = u + 1 for every vertex with out-edges; an inclusive maximum
-// scan then gives every edge its source + 1 (sources rise with the edge
-// index).
-// (offsets outside [0, m) are skipped: the ingest check reports them)
-__global__ void k_src_heads(int32_t n, int64_t m, const int64_t* off, int32_t* head) {
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
-       u += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = off[u];
-    if (off[u + 1] > o && o >= 0 && o < m) head[o] = (int32_t)u + 1;
-  }
+// ---- hubs ---------------------------------------------------------------------
+constexpr int kDegBins = 4096;  // degrees above are counted in the last bin
+
+__global__ void k_deg_hist(int32_t n, const int32_t* deg, unsigned int* hist) {
+  __shared__ unsigned int h[kDegBins];
+  for (int i = threadIdx.x; i < kDegBins; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&h[min(deg[v], kDegBins - 1)], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kDegBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-struct MaxI32 {
-  __device__ __forceinline__ int32_t operator()(int32_t a, int32_t b) const { return a > b ? a : b; }
-};
-
-// Edge e = (src[e] - 1) -> adj[e] is placed at the next free slot of its
-// target's in-list.  A target outside [0, n), or a slot outside [0, m) (an
-// in-degree list that does not match the out-CSR), is not written and marks
-// *bad.
-__global__ void k_in_scatter(int32_t n, int64_t m, const int32_t* srcp1, const int32_t* adj,
-                             unsigned long long* cursor, int32_t* in_adj, int* bad) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t v = adj[e];
-    if ((uint32_t)v >= (uint32_t)n) {
-      atomicOr(bad, 1);
-      continue;
+__global__ void k_pick_hubs(int32_t n, const int32_t* deg, int32_t dmin, int32_t* nh,
+                            int32_t* hub_ids, int32_t* rank) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    if (deg[v] < dmin) continue;
+    const int32_t r = atomicAdd(nh, 1);
+    if (r < kHubMax) {
+      hub_ids[r] = (int32_t)v;
+      rank[v] = r;
     }
-    const unsigned long long pos = atomicAdd(&cursor[v], 1ull);
-    if (pos < (unsigned long long)m) in_adj[pos] = srcp1[e] - 1;
-    else atomicOr(bad, 1);
   }
 }
 
-// Every in-list filled exactly: cursor[v] == in_off[v + 1].
-__global__ void k_in_check(int32_t n, const unsigned long long* cursor, const int64_t* in_off,
-                           int* bad) {
+__global__ void k_encode_hints(int32_t n, int32_t* hint, const int32_t* rank) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x)
-    if (cursor[v] != (unsigned long long)in_off[v + 1]) atomicOr(bad, 1);
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t h = hint[v];
+    if (h >= 0) {
+      const int32_t r = rank[h];
+      if (r >= 0) hint[v] = -(r + 2);
+    }
+  }
 }
 
-__global__ void k_copy_cursor(int32_t n, const int64_t* in_off, unsigned long long* cursor) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x)
-    cursor[v] = (unsigned long long)in_off[v];
-}
-
-cudaError_t in_csr_from_out(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
-                            const int64_t* in_off, int32_t* in_adj, int* d_bad, cudaStream_t s) {
-  if (n <= 0 || m <= 0) return cudaSuccess;
-  size_t scan_bytes = 0;
-  cudaError_t e = cub::DeviceScan::InclusiveScan(nullptr, scan_bytes, (const int32_t*)nullptr,
-                                                 (int32_t*)nullptr, MaxI32(), m, s);
+// The hubs are the vertices of largest total degree: a degree histogram
+// picks the smallest degree d for which at most kHubMax vertices reach it
+// (at least 1), and every vertex from d up takes a rank (in no particular
+// order; only the first kHubMax when the top bin alone holds more).
+cudaError_t build_hubs(int32_t n, const int64_t* out_off, const int64_t* in_off, int32_t* hint_out,
+                       int32_t* hint_in, int32_t* hub_ids, int32_t* nhubs, cudaStream_t s) {
+  *nhubs = 0;
+  if (n <= 0) return cudaSuccess;
+  int32_t* deg = nullptr;
+  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 2 + kDegBins + 1) * 4, s);
   if (e != cudaSuccess) return e;
-  // one allocation: heads, then sources (m ints each), cursors (n), scan scratch
-  const size_t hb = (size_t)m * 4, cb = (size_t)n * 8;
-  char* buf = nullptr;
-  e = cudaMallocAsync((void**)&buf, 2 * hb + cb + scan_bytes + 256, s);
+  int32_t* rank = deg + n;
+  unsigned int* hist = reinterpret_cast<unsigned int*>(rank + n);
+  int32_t* nh = reinterpret_cast<int32_t*>(hist + kDegBins);
+  std::vector<unsigned int> h(kDegBins);
+  int32_t cnt = 0;
+  e = cudaMemsetAsync(hist, 0, (kDegBins + 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(rank, 0xff, (size_t)n * 4, s);
+  if (e == cudaSuccess) {
+    k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
+    k_deg_hist<<<152 * 2, 1024, 0, s>>>(n, deg, hist);
+    e = cudaMemcpyAsync(h.data(), hist, kDegBins * 4, cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) {
+    int32_t dmin = kDegBins - 1;
+    long long above = h[kDegBins - 1];
+    while (dmin > 1 && above + h[dmin - 1] <= kHubMax) above += h[--dmin];
+    k_pick_hubs<<<grid_for(n), 256, 0, s>>>(n, deg, dmin, nh, hub_ids, rank);
+    if (hint_out) k_encode_hints<<<grid_for(n), 256, 0, s>>>(n, hint_out, rank);
+    if (hint_in) k_encode_hints<<<grid_for(n), 256, 0, s>>>(n, hint_in, rank);
+    e = cudaMemcpyAsync(&cnt, nh, 4, cudaMemcpyDeviceToHost, s);
+  }
+  cudaFreeAsync(deg, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return e;
-  int32_t* head = reinterpret_cast<int32_t*>(buf);
-  int32_t* srcp1 = reinterpret_cast<int32_t*>(buf + hb);
-  unsigned long long* cursor = reinterpret_cast<unsigned long long*>(
-      buf + ((2 * hb + 7) & ~size_t(7)));
-  void* scratch = buf + ((2 * hb + 7) & ~size_t(7)) + cb;
-  e = cudaMemsetAsync(head, 0, hb, s);
-  if (e == cudaSuccess) {
-    k_src_heads<<<grid_for(n), 256, 0, s>>>(n, m, out_off, head);
-    e = cub::DeviceScan::InclusiveScan(scratch, scan_bytes, head, srcp1, MaxI32(), m, s);
-  }
-  if (e == cudaSuccess) {
-    k_copy_cursor<<<grid_for(n), 256, 0, s>>>(n, in_off, cursor);
-    k_in_scatter<<<152 * 16, 256, 0, s>>>(n, m, srcp1, out_adj, cursor, in_adj, d_bad);
-    k_in_check<<<grid_for(n), 256, 0, s>>>(n, cursor, in_off, d_bad);
-    e = cudaGetLastError();
-  }
-  cudaFreeAsync(buf, s);
-  return e;
+  *nhubs = cnt < kHubMax ? cnt : kHubMax;
+  return cudaGetLastError();
 }
 
 }  // namespace gb

@@ -196,11 +196,7 @@ gb_status gb_graph_from_csr(gb_ctx* ctx, int32_t n, int64_t m, const int64_t* ou
                             const int32_t* in_adj, gb_graph** g);
 /* From the reference's own CSR layout (graph struct, scc_main.cpp:75-86):
  * 32-bit unsigned offsets out_degree_list[n+1] / in_degree_list[n+1].
- * in_* may be NULL (symmetric graph of cc_main.cpp:72-79).  Only the
- * out-CSR and in_degree_list are read: the in-lists are rebuilt on the
- * device from the out-CSR (half the bytes over the host link), so their
- * order within a vertex is not in_array's; an in_degree_list that does not
- * match the out-CSR is GB_ERR_INVALID. */
+ * in_* may be NULL (symmetric graph of cc_main.cpp:72-79). */
 gb_status gb_graph_from_csr32(gb_ctx* ctx, int32_t n, uint32_t m, const int32_t* out_array,
                               const uint32_t* out_degree_list, const int32_t* in_array,
                               const uint32_t* in_degree_list, gb_graph** g);
@@ -422,11 +418,8 @@ gb_status gb_server_destroy(gb_server* server);
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
  * fields passed one by one and scc_maps owned by the caller (n ints).  Uses
  * a library-owned context on the calling thread's current CUDA device
- * (created at the first call) and keeps the graph's device buffers for
- * reuse.  avg_degree is accepted for parity; the direction switch uses exact
- * edge counts.  As in gb_graph_from_csr32, in_array is not read: the
- * in-lists are rebuilt on the device from the out-CSR and in_degree_list,
- * which costs less than moving them over the host link. */
+ * (created at the first call) and keeps the graph's device buffers for reuse.  avg_degree is accepted for parity;
+ * the direction switch uses exact edge counts. */
 gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_array,
                      const unsigned* out_degree_list, const unsigned* in_degree_list,
                      int* scc_maps, int max_deg_vert, double avg_degree, int vert_cutoff);

@@ -461,32 +461,3 @@ def test_pull_hints_follow_the_rule(ctx, case):
     assert np.array_equal(ho, _hints_want(n, oo, oa, deg))
     assert np.array_equal(hi, _hints_want(n, io, ia, deg))
     g.close()
-
-
-@pytest.mark.parametrize("pinned", [False, True])
-def test_reference_dropin_rebuilds_the_in_lists(pinned):
-    """gb_run_scc reads the out-CSR and the in-degree list and rebuilds the
-    in-lists on the device: an in_array of garbage gives the same labels,
-    and an in-degree list that does not match the out-CSR (monotone, ending
-    at m, but with two vertices' degrees moved) is refused."""
-    torch = pytest.importorskip("torch")
-    pin = ((lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy())
-           if pinned else (lambda a: np.ascontiguousarray(a)))
-    n, s, d = graphs.rmat(13, 16, 31)
-    cg = oracle.CpuGraph(n, s, d)
-    odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
-    oa = pin(cg.out_adj)
-    junk = pin(np.full(cg.in_adj.size, 7, np.int32))
-    lab = gb.run_scc_ref(n, oa, junk, odl, idl)
-    assert np.array_equal(lab, _scc_want(n, s, d))
-    deg = np.diff(cg.in_off)
-    i = int(np.flatnonzero(deg > 1)[0])
-    j = i + 1 + int(np.flatnonzero(deg[i + 1:] >= 0)[0])
-    bad = cg.in_off.copy()
-    bad[i + 1:j + 1] -= 1  # vertex i loses an in-edge, vertex j gains one
-    assert (np.diff(bad) >= 0).all() and bad[-1] == cg.in_off[-1]
-    with pytest.raises(gb.GBError) as e:
-        gb.run_scc_ref(n, oa, junk, odl, pin(bad.astype(np.uint32)))
-    assert e.value.status == gb.GB_ERR_INVALID
-    # and the next call with the right list works
-    assert np.array_equal(gb.run_scc_ref(n, oa, junk, odl, idl), lab)
