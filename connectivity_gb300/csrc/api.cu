@@ -6,7 +6,6 @@
 #include <cstring>
 #include <mutex>
 #include <new>
-#include <vector>
 
 #include "../../include/gbconn.h"
 #include "api_internal.h"
@@ -60,8 +59,7 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   const size_t nw = nv / 32 + 2;
   const size_t arr = align256(nv * 4), bm = align256(nw * 4);
   const size_t G = (size_t)(c->grid > 0 ? c->grid : 1);
-  const size_t hs = align256((size_t)2 * gb::kHubWords * 4);
-  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(2 * G * 8) + hs;
+  const size_t total = 15 * arr + 4 * bm + align256(2 * G * 4) + align256(2 * G * 8);
   char* p = nullptr;
   CK(cudaMalloc(&p, total), "workspace allocation");
   c->ws = p;
@@ -92,7 +90,6 @@ gb_status ensure_ws(gb_ctx* c, int32_t n) {
   w.done = (uint32_t*)take(bm);
   w.blk_i = (int32_t*)take(align256(2 * G * 4));
   w.blk_l = (long long*)take(align256(2 * G * 8));
-  w.hubsnap = (uint32_t*)take(hs);
   w.ctl = c->d_ctl;
   c->cap_n = n;
   return GB_OK;
@@ -151,12 +148,9 @@ void graph_free(gb_graph* g) {
   dev_free(g->in_adj, g->pooled, s);
   dev_free(g->hint_out, g->pooled, s);
   dev_free(g->hint_in, g->pooled, s);
-  dev_free(g->hubs, g->pooled, s);
   g->out_off = g->in_off = nullptr;
   g->out_adj = g->in_adj = nullptr;
   g->hint_out = g->hint_in = nullptr;
-  g->hubs = nullptr;
-  g->nhubs = 0;
 }
 
 // Builds the pull hints of a graph whose CSR is complete on the device.
@@ -169,12 +163,6 @@ gb_status graph_hints(gb_ctx* c, gb_graph* g) {
   CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
                      c->stream),
      "hints");
-  if (!g->hubs)
-    CK(dev_alloc((void**)&g->hubs, (size_t)gb::kHubMax * 4, g->pooled, g->pool_stream),
-       "hub allocation");
-  CK(gb::build_hubs(g->n, g->out_off, g->symmetric ? nullptr : g->in_off, g->hint_out,
-                    g->hint_in, g->hubs, &g->nhubs, c->stream),
-     "hubs");
   return GB_OK;
 }
 }  // namespace gb
@@ -398,10 +386,6 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
     gv.in = kind == gb::kSCC ? gv.out : gb::Csr{nullptr, nullptr, nullptr};
   } else {
     gv.in = {g->in_off, g->in_adj, g->hint_in};
-  }
-  if (g->hint_out && g->hubs && g->nhubs > 0) {
-    gv.hubs = g->hubs;
-    gv.nhubs = g->nhubs;
   }
   gv.batch = gb::BatchView{};
   cudaStream_t sm = c->stream;
@@ -881,18 +865,6 @@ gb_status gb_graph_hints_to_host(const gb_graph* g, int32_t* hint_out, int32_t* 
     CK(cudaMemcpy(hint_out, g->hint_out, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
   if (hint_in && g->n && g->hint_in)
     CK(cudaMemcpy(hint_in, g->hint_in, (size_t)g->n * 4, cudaMemcpyDeviceToHost), "download");
-  // hints that name a hub by rank become vertex ids again
-  std::vector<int32_t> hubs((size_t)(g->nhubs > 0 ? g->nhubs : 1));
-  if (g->nhubs > 0)
-    CK(cudaMemcpy(hubs.data(), g->hubs, (size_t)g->nhubs * 4, cudaMemcpyDeviceToHost), "download");
-  for (int32_t* h : {hint_out, g->hint_in ? hint_in : nullptr}) {
-    if (!h) continue;
-    for (int32_t v = 0; v < g->n; ++v)
-      if (h[v] <= -2) {
-        const int32_t r = -(h[v] + 2);
-        h[v] = r < g->nhubs ? hubs[(size_t)r] : -1;
-      }
-  }
   return GB_OK;
 }
 
@@ -941,10 +913,7 @@ gb_status gb_graph_set_hints(gb_ctx* c, gb_graph* g, int32_t on) {
   if (on) return graph_hints(c, g);
   gb::dev_free(g->hint_out, g->pooled, g->pool_stream);
   gb::dev_free(g->hint_in, g->pooled, g->pool_stream);
-  gb::dev_free(g->hubs, g->pooled, g->pool_stream);
   g->hint_out = g->hint_in = nullptr;
-  g->hubs = nullptr;
-  g->nhubs = 0;
   return GB_OK;
 }
 

@@ -37,8 +37,6 @@ struct gb_graph {
   int32_t* in_adj = nullptr;
   int32_t* hint_out = nullptr;  // pull hints (null for the drop-in staging graph)
   int32_t* hint_in = nullptr;
-  int32_t* hubs = nullptr;      // vertex of each hub rank (kHubMax entries), with the hints
-  int32_t nhubs = 0;
   bool pooled = false;          // arrays from the stream-ordered pool
   cudaStream_t pool_stream = nullptr;
 };

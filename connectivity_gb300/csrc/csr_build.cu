@@ -14,7 +14,6 @@
 #include "gen_common.h"
 
 #include <cstring>
-#include <vector>
 
 namespace gb {
 namespace {
@@ -685,85 +684,6 @@ cudaError_t rmat_edges_device(int32_t n, int edge_factor, uint64_t seed, gb_rmat
   *d_src = src;
   *d_dst = dst;
   *m_out = k;
-  return cudaGetLastError();
-}
-
-// ---- hubs ---------------------------------------------------------------------
-constexpr int kDegBins = 4096;  // degrees above are counted in the last bin
-
-__global__ void k_deg_hist(int32_t n, const int32_t* deg, unsigned int* hist) {
-  __shared__ unsigned int h[kDegBins];
-  for (int i = threadIdx.x; i < kDegBins; i += blockDim.x) h[i] = 0u;
-  __syncthreads();
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(&h[min(deg[v], kDegBins - 1)], 1u);
-  __syncthreads();
-  for (int i = threadIdx.x; i < kDegBins; i += blockDim.x)
-    if (h[i]) atomicAdd(&hist[i], h[i]);
-}
-
-__global__ void k_pick_hubs(int32_t n, const int32_t* deg, int32_t dmin, int32_t* nh,
-                            int32_t* hub_ids, int32_t* rank) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    if (deg[v] < dmin) continue;
-    const int32_t r = atomicAdd(nh, 1);
-    if (r < kHubMax) {
-      hub_ids[r] = (int32_t)v;
-      rank[v] = r;
-    }
-  }
-}
-
-__global__ void k_encode_hints(int32_t n, int32_t* hint, const int32_t* rank) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t h = hint[v];
-    if (h >= 0) {
-      const int32_t r = rank[h];
-      if (r >= 0) hint[v] = -(r + 2);
-    }
-  }
-}
-
-// The hubs are the vertices of largest total degree: a degree histogram
-// picks the smallest degree d for which at most kHubMax vertices reach it
-// (at least 1), and every vertex from d up takes a rank (in no particular
-// order; only the first kHubMax when the top bin alone holds more).
-cudaError_t build_hubs(int32_t n, const int64_t* out_off, const int64_t* in_off, int32_t* hint_out,
-                       int32_t* hint_in, int32_t* hub_ids, int32_t* nhubs, cudaStream_t s) {
-  *nhubs = 0;
-  if (n <= 0) return cudaSuccess;
-  int32_t* deg = nullptr;
-  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 2 + kDegBins + 1) * 4, s);
-  if (e != cudaSuccess) return e;
-  int32_t* rank = deg + n;
-  unsigned int* hist = reinterpret_cast<unsigned int*>(rank + n);
-  int32_t* nh = reinterpret_cast<int32_t*>(hist + kDegBins);
-  std::vector<unsigned int> h(kDegBins);
-  int32_t cnt = 0;
-  e = cudaMemsetAsync(hist, 0, (kDegBins + 1) * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(rank, 0xff, (size_t)n * 4, s);
-  if (e == cudaSuccess) {
-    k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
-    k_deg_hist<<<152 * 2, 1024, 0, s>>>(n, deg, hist);
-    e = cudaMemcpyAsync(h.data(), hist, kDegBins * 4, cudaMemcpyDeviceToHost, s);
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) {
-    int32_t dmin = kDegBins - 1;
-    long long above = h[kDegBins - 1];
-    while (dmin > 1 && above + h[dmin - 1] <= kHubMax) above += h[--dmin];
-    k_pick_hubs<<<grid_for(n), 256, 0, s>>>(n, deg, dmin, nh, hub_ids, rank);
-    if (hint_out) k_encode_hints<<<grid_for(n), 256, 0, s>>>(n, hint_out, rank);
-    if (hint_in) k_encode_hints<<<grid_for(n), 256, 0, s>>>(n, hint_in, rank);
-    e = cudaMemcpyAsync(&cnt, nh, 4, cudaMemcpyDeviceToHost, s);
-  }
-  cudaFreeAsync(deg, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return e;
-  *nhubs = cnt < kHubMax ? cnt : kHubMax;
   return cudaGetLastError();
 }
 

@@ -156,7 +156,6 @@ struct Work {
   int32_t* blk_i;         // per-block scratch (2 x grid size: counts, then pivot ids)
   unsigned long long* tphase;  // this run's 4 phase-boundary device times, or null
   long long* blk_l;       // per-block scratch (2 x grid size: pivot keys, then edge sums)
-  uint32_t* hubsnap;      // 2 x kHubWords: each search's hub snapshot, or null
   Ctl* ctl;
 };
 
@@ -174,21 +173,12 @@ struct BatchView {
 
 // One graph (or a batch union) as the kernels see it.  `in` is null for a
 // symmetric CSR.
-// Hubs: the vertices of largest total degree, at most kHubMax of them,
-// numbered by rank.  A hint that names a hub holds -(rank + 2) instead of
-// the vertex id (-1 still means no hint), so a pull step can test it in a
-// snapshot of the hubs' visited bits kept in shared memory.
-constexpr int32_t kHubMax = 65536;
-constexpr int32_t kHubWords = kHubMax / 32;
-
 struct GraphView {
   int32_t n;
   int64_t m;
   Csr out;
   Csr in;
   BatchView batch;
-  const int32_t* hubs;    // vertex of each hub rank (nhubs of them), or null
-  int32_t nhubs;
 };
 
 // Kind of run.
@@ -283,10 +273,6 @@ cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, cons
 cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s);
-// The hubs of a graph (hub_ids: kHubMax entries; *nhubs receives their
-// count) and its hints re-encoded to name hubs by rank.  Synchronises.
-cudaError_t build_hubs(int32_t n, const int64_t* out_off, const int64_t* in_off, int32_t* hint_out,
-                       int32_t* hint_in, int32_t* hub_ids, int32_t* nhubs, cudaStream_t s);
 // Seeded R-MAT edge list on the device for n vertices: edge_factor * n
 // candidate edges at scale ceil(log2 n), ids >= n, self-loops and duplicates
 // dropped, sorted by (src, dst); *d_src / *d_dst are cudaMallocAsync'd.

@@ -363,9 +363,7 @@ constexpr int kTodo = 384;
 // Dynamic shared memory of the cooperative kernels: two staging buffers and
 // one pull backlog per warp.
 constexpr int kWarpSmem = 2 * kWB + kTodo;
-// after the warps' buffers: the hub snapshots of the (at most two) pulling
-// searches, kHubWords words each
-constexpr int kDynSmem = kWarps * kWarpSmem * 4 + 2 * kHubWords * 4;
+constexpr int kDynSmem = kWarps * kWarpSmem * 4;
 // a warp's shared memory also holds the ids of 16 bitmap words
 static_assert(kWB * 2 + kTodo >= 16 * 32, "warp shared memory too small for 16 words");
 
@@ -476,10 +474,6 @@ struct Smem {
   }
   __device__ __forceinline__ int32_t* todo(int warp) {
     return stage_base + warp * kWarpSmem + 2 * kWB;
-  }
-  // search k's snapshot of the hubs' visited bits (bit r: hub of rank r)
-  __device__ __forceinline__ uint32_t* hub(int k) {
-    return reinterpret_cast<uint32_t*>(stage_base + kWarps * kWarpSmem) + k * kHubWords;
   }
 };
 extern __shared__ __align__(16) int32_t g_dyn_smem[];
@@ -1608,20 +1602,6 @@ struct ReachSpec {
   int stat_slot;
 };
 
-// Whether hint h of a pull candidate is reached: a vertex id is looked up in
-// the visited bitmap, a hub (h <= -2, rank -(h + 2)) in the step's snapshot
-// of the hubs' bits, which sits in shared memory.  A hub reached after the
-// snapshot was taken reads as not reached, which only sends the candidate
-// to the edge pass.
-__device__ __forceinline__ bool hint_hit(const uint32_t* vis, const uint32_t* snap, int32_t h) {
-  if (h >= 0) return bit_get_l1(vis, h);
-  if (h <= -2 && snap != nullptr) {
-    const int32_t r = -(h + 2);
-    return (snap[r >> 5] >> (r & 31)) & 1u;
-  }
-  return false;
-}
-
 constexpr int kPullU = 4;  // backlog candidates per thread per edge pass
 constexpr int kPullA = 8;  // candidates per thread per hint pass
 
@@ -1739,8 +1719,7 @@ __device__ __forceinline__ int pull_kt(const Args& A) {
 template <int NC>
 __device__ void pull_thread(const ReachSpec& R, const Args& A, Work& w, Smem& sm, Tally& ty,
                             const int32_t* cand_cur, int32_t ncur, int32_t* cand_next,
-                            long long qhi, Slot* o, int pp, int dir, int32_t* wl, int32_t* bl,
-                            const uint32_t* snap) {
+                            long long qhi, Slot* o, int pp, int dir, int32_t* wl, int32_t* bl) {
   Ctl* c = w.ctl;
   const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
   const int warp = t >> 5, lane = t & 31;
@@ -1798,8 +1777,8 @@ __device__ void pull_thread(const ReachSpec& R, const Args& A, Work& w, Smem& sm
       for (int j = 0; j < kPullA; ++j) unv[j] = v[j] >= 0 && !bit_get_l1(R.vis, v[j]);
 #pragma unroll
       for (int j = 0; j < kPullA; ++j) {
-        const bool hinted = unv[j] && (hint_hit(R.vis, snap, h0[j]) ||
-                                       hint_hit(R.vis, snap, h1[j]));
+        const bool hinted = unv[j] && ((h0[j] >= 0 && bit_get_l1(R.vis, h0[j])) ||
+                                       (h1[j] >= 0 && bit_get_l1(R.vis, h1[j])));
         if (v[j] >= 0) ty.list++;
         if (hinted) bit_set_red(R.vis, v[j]);
         stage_push(sf, hinted, v[j], 0ull, of, c);
@@ -2056,36 +2035,6 @@ __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const
     __syncthreads();
     if (flags[0] == 0) break;
     const bool any_pull = flags[1] != 0;
-    // the hub snapshots of the pulling searches: the grid reads the hubs'
-    // visited bits (complete at the step boundary) into global words, and
-    // after one grid barrier every block copies them to shared memory
-    const bool snaps = any_pull && A.g.hubs != nullptr && w.hubsnap != nullptr && ns <= 2;
-    if (snaps) {
-      const int32_t nh = A.g.nhubs < kHubMax ? A.g.nhubs : kHubMax;
-      const int nwh = (nh + 31) >> 5;
-      for (int k = 0; k < ns; ++k) {
-        const Search& q = S[k];
-        if (!q.active || !q.pull) continue;
-        uint32_t* gs = w.hubsnap + k * kHubWords;
-        for (long long wi = (long long)b * T + t; wi < nwh; wi += (long long)G * T) {
-          uint32_t word = 0u;
-#pragma unroll 8
-          for (int j = 0; j < 32; ++j) {
-            const long long r = wi * 32 + j;
-            if (r < nh && bit_get(q.R.vis, __ldg(A.g.hubs + r))) word |= 1u << j;
-          }
-          gs[wi] = word;
-        }
-      }
-      if (!grid_barrier(c, 208)) return false;
-      for (int k = 0; k < ns; ++k) {
-        const Search& q = S[k];
-        if (!q.active || !q.pull) continue;
-        uint32_t* hs = sm.hub(k);
-        for (int wi = t; wi < nwh; wi += T) hs[wi] = __ldcg(w.hubsnap + k * kHubWords + wi);
-      }
-      __syncthreads();
-    }
     for (int k = 0; k < ns; ++k) {
       const Search& q = S[k];
       if (!q.active) continue;
@@ -2112,7 +2061,7 @@ __device__ bool reach_multi(Search* S, int ns, int* flags /* shared, 2 */, const
                      rv, sk, tn, sm, c, ty);
       } else {
         pull_thread<NC>(q.R, A, w, sm, ty, q.cand_cur, q.ncur, q.cand[q.cn], q.qhi, o, q.pp,
-                        q.dir, q.wl, q.bl, snaps ? sm.hub(k) : nullptr);
+                        q.dir, q.wl, q.bl);
       }
     }
     if (any_pull) {
