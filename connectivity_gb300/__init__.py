@@ -101,6 +101,7 @@ _sig("gb_ctx_set_stream", C.c_int32, [_P, _P])
 _sig("gb_ctx_stream", _P, [_P])
 _sig("gb_ctx_sync", C.c_int32, [_P])
 _sig("gb_ctx_phase_times", C.c_int32, [_P, C.c_int32, _P])
+_sig("gb_ctx_set_class_opts", C.c_int32, [_P, C.c_int32, _P, _P])
 _sig("gb_ctx_reach_trace", C.c_int32, [_P, _P, _P, _P, C.c_int32])
 _sig("gb_ctx_reach_trace2", C.c_int32, [_P, _P, _P, _P, _P, C.c_int32])
 _sig("gb_ctx_block_times", C.c_int32, [_P, _P, C.c_int32])
@@ -197,6 +198,12 @@ def _take(p: C.c_void_p, count: int, dtype) -> np.ndarray:
         out = np.frombuffer(buf, dtype=dtype).copy()
     _lib.gb_free_host(p)
     return out
+
+
+def _optp(o):
+    """The options argument: o by reference, or NULL (the context's class
+    table, else the defaults)."""
+    return C.byref(o) if o is not None else None
 
 
 def opts(**kw) -> Opts:
@@ -343,6 +350,16 @@ class Context:
         except Exception:
             pass
 
+    def set_class_opts(self, n_max, option_list) -> None:
+        """Options per size class for runs given no options: entry i covers
+        graphs of at most n_max[i] vertices (rising); the last covers the
+        rest.  Empty lists remove the table."""
+        nm = np.ascontiguousarray(n_max, np.int64)
+        arr = (Opts * max(1, len(option_list)))(*option_list)
+        _check(_lib.gb_ctx_set_class_opts(self._h, nm.size, _ptr(nm) if nm.size else None,
+                                          C.cast(arr, C.c_void_p) if option_list else None),
+               "gb_ctx_set_class_opts")
+
     def set_stream(self, stream_handle: int | None) -> None:
         _check(_lib.gb_ctx_set_stream(self._h, C.c_void_p(stream_handle or 0)), "set_stream")
 
@@ -382,7 +399,7 @@ class Context:
         if labels is None:
             labels = np.empty(g.n, np.int32)
         ptr = _ptr(labels) if isinstance(labels, np.ndarray) else C.c_void_p(int(labels))
-        _check(fn(self._h, g._h, ptr, C.byref(o or opts()), C.byref(st)), name)
+        _check(fn(self._h, g._h, ptr, _optp(o), C.byref(st)), name)
         return (labels, st) if want_stats else labels
 
     def scc(self, g: "Graph", labels=None, o: Opts | None = None, stats: bool = False):
@@ -406,7 +423,7 @@ class Context:
             (sp, m), (dp, _) = src, dst
             sp, dp = C.c_void_p(sp), C.c_void_p(dp)
         lp = _ptr(labels) if isinstance(labels, np.ndarray) else C.c_void_p(int(labels))
-        _check(fn(self._h, n, m, sp, dp, lp, C.byref(o or opts())), name)
+        _check(fn(self._h, n, m, sp, dp, lp, _optp(o)), name)
         return labels
 
     def scc_edges(self, n: int, src, dst, labels=None, o: Opts | None = None):
@@ -418,11 +435,11 @@ class Context:
         return self._edges(_lib.gb_wcc_edges, "gb_wcc_edges", n, src, dst, labels, o)
 
     def scc_async(self, g: "Graph", labels_dev: int, o: Opts | None = None) -> None:
-        _check(_lib.gb_scc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+        _check(_lib.gb_scc_async(self._h, g._h, C.c_void_p(labels_dev), _optp(o)),
                "gb_scc_async")
 
     def wcc_async(self, g: "Graph", labels_dev: int, o: Opts | None = None) -> None:
-        _check(_lib.gb_wcc_async(self._h, g._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+        _check(_lib.gb_wcc_async(self._h, g._h, C.c_void_p(labels_dev), _optp(o)),
                "gb_wcc_async")
 
     def batch_scc(self, b: "Batch", labels=None, o: Opts | None = None, stats: bool = False):
@@ -433,7 +450,7 @@ class Context:
         return self._run(_lib.gb_batch_wcc, "gb_batch_wcc", b, labels, o, stats)
 
     def batch_scc_async(self, b: "Batch", labels_dev: int, o: Opts | None = None) -> None:
-        _check(_lib.gb_batch_scc_async(self._h, b._h, C.c_void_p(labels_dev), C.byref(o or opts())),
+        _check(_lib.gb_batch_scc_async(self._h, b._h, C.c_void_p(labels_dev), _optp(o)),
                "gb_batch_scc_async")
 
     def tune(self, target, kind: int = 0, reps: int = 3) -> tuple["Opts", float, float]:

@@ -416,8 +416,17 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
 
 }  // namespace
 
+const gb_opts* gb::class_opts(const gb_ctx* c, int64_t n) {
+  if (!c || c->cls_n.empty()) return nullptr;
+  for (size_t i = 0; i < c->cls_n.size(); ++i)
+    if (n <= c->cls_n[i]) return &c->cls_opts[i];
+  return &c->cls_opts.back();
+}
+
 gb_status gb::run_graph(gb_ctx* c, const gb_graph* g, RunKind kind, int32_t* labels,
                         const gb_opts* o, gb_stats* st, bool wait, const BatchView* bv) {
+  // a run given no options takes the context's options for its size class
+  if (!o && c && g) o = class_opts(c, g->n);
   return run_graph_impl(c, g, kind, labels, o, st, wait, bv);
 }
 
@@ -923,6 +932,19 @@ gb_status gb_graph_has_hints(const gb_graph* g, int32_t* on) {
   return GB_OK;
 }
 
+gb_status gb_ctx_set_class_opts(gb_ctx* c, int32_t count, const int64_t* n_max,
+                                const gb_opts* opts) {
+  if (!c || count < 0 || (count > 0 && (!n_max || !opts))) return GB_ERR_INVALID;
+  for (int32_t i = 1; i < count; ++i)
+    if (n_max[i] <= n_max[i - 1]) {
+      gb_set_error("gb_ctx_set_class_opts: %s", "class bounds must rise");
+      return GB_ERR_INVALID;
+    }
+  c->cls_n.assign(n_max, n_max + count);
+  c->cls_opts.assign(opts, opts + count);
+  return GB_OK;
+}
+
 gb_status gb_scc(gb_ctx* c, const gb_graph* g, int32_t* labels, const gb_opts* o, gb_stats* st) {
   return gb::run_graph(c, g, gb::kSCC, labels, o, st, true, nullptr);
 }
@@ -948,6 +970,7 @@ gb_status run_edges(gb_ctx* c, gb::RunKind kind, int32_t n, int64_t m, const int
   if (n == 0) return GB_OK;
   gb_opts d;
   gb_opts_default(&d);
+  if (!o) o = gb::class_opts(c, n);
   if (!o) o = &d;
   if (n > gb::kSmallMaxN || m >= (1ll << 31) || !o->small_path || !o->canonical) {
     gb_graph* g = nullptr;

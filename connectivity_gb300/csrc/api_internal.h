@@ -2,12 +2,17 @@
 // layouts of the opaque handles and the run / allocation helpers.
 #pragma once
 #include <cstdint>
+#include <vector>
 
 #include "../../include/gbconn.h"
 #include "gb_internal.cuh"
 
 struct gb_ctx {
   int device = 0;
+  // options per size class for runs given no options (gb_ctx_set_class_opts):
+  // entry i covers graphs of at most cls_n[i] vertices, ascending
+  std::vector<int64_t> cls_n;
+  std::vector<gb_opts> cls_opts;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   int grid = 0;                 // cooperative grid (all resident blocks)
@@ -58,6 +63,9 @@ gb_status graph_alloc(gb_graph* g, bool with_in);
 void graph_free(gb_graph* g);
 gb_status graph_hints(gb_ctx* c, gb_graph* g);
 gb_status validate_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* off, const int32_t* adj);
+// The context's options for a graph (or union) of n vertices from its class
+// table, or null when it has none.
+const gb_opts* class_opts(const gb_ctx* c, int64_t n);
 // One run over a graph; bv != null runs a batch union and returns labels
 // local to each graph.
 gb_status run_graph(gb_ctx* c, const gb_graph* g, RunKind kind, int32_t* labels,

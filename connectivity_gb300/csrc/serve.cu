@@ -133,6 +133,8 @@ int64_t request_bytes(int32_t n, int64_t m) {
 struct gb_server {
   gb_ctx* ctx = nullptr;
   gb_opts opts{};   // options of the merged runs
+  bool opts_set = false;  // set by gb_server_set_opts; otherwise the context's
+                          // class table (if any) picks per merged set
   cudaStream_t copy = nullptr;
   int64_t budget = 0;
   int32_t max_graphs = 0;
@@ -289,8 +291,9 @@ gb_status part_launch(gb_server* sv, Part& p, int kind) {
     gb_status st = gb::batch_create(c, p.nlarge, p.vbase.data(), p.ebase[(size_t)p.nlarge],
                                     p.d_src, p.d_dst, false, true, &p.batch);
     if (st != GB_OK) return st;
-    st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels, &sv->opts,
-                       nullptr, false);
+    const gb_opts* po = sv->opts_set ? nullptr : gb::class_opts(c, p.vbase[(size_t)p.nlarge]);
+    st = gb::batch_run(c, p.batch, kind == 0 ? gb::kSCC : gb::kWCC, p.d_labels,
+                       po ? po : &sv->opts, nullptr, false);
     if (st != GB_OK) return st;
   }
   if (p.nlarge < count) {
@@ -474,6 +477,7 @@ gb_status gb_server_set_opts(gb_server* sv, const gb_opts* o) {
   std::lock_guard<std::mutex> lk(sv->mu);
   if (sv->started) return GB_ERR_INVALID;
   sv->opts = *o;
+  sv->opts_set = true;
   return GB_OK;
 }
 

@@ -4,17 +4,27 @@ The device autotuner (``gb_tune`` / ``gb_tune_batch``) times runs of one
 graph or batch and returns the best options for it.  This module runs it on
 one seeded R-MAT graph per size class and keeps the winners in a JSON table;
 ``opts_for`` then picks the options of the class nearest a graph's size (by
-log2 of the vertex count).  Labels never depend on the options.
+log2 of the vertex count), and ``install`` gives a context the table, so its
+runs without options use their class's options.  Labels never depend on the
+options.
+
+    python -m connectivity_gb300.tune [out.json]
+
+tunes every class on the current GPU and writes the table (by default over
+tables/classes_scc.json, the table ``install`` reads).
 """
 from __future__ import annotations
 
 import json
 import math
+import os
+import sys
 
 from . import Batch, Context, Graph, Opts, opts
 
 # (vertices, edge factor) of the classes tuned by default
-CLASSES = [(1 << 10, 8), (1 << 14, 16), (1 << 18, 16), (1 << 22, 16), (1 << 24, 16)]
+CLASSES = [(1 << 10, 8), (1 << 12, 16), (1 << 14, 16), (1 << 16, 16), (1 << 18, 16),
+           (1 << 20, 16), (1 << 22, 16), (1 << 24, 16)]
 
 TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode", "small_path")
 
@@ -86,6 +96,30 @@ def load(path: str) -> dict:
         return json.load(f)
 
 
+DEFAULT_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tables",
+                             "classes_scc.json")
+
+
+def class_bounds(table: dict) -> list[int]:
+    """Upper vertex bound of each class: the geometric midpoint to the next
+    class (the last class takes every larger graph)."""
+    ns = [int(c["n"]) for c in table.get("classes", [])]
+    out = []
+    for i, n in enumerate(ns):
+        out.append(int(math.sqrt(n * ns[i + 1])) if i + 1 < len(ns) else (1 << 62))
+    return out
+
+
+def install(ctx: Context, table: dict | None = None) -> None:
+    """Gives ctx the table's options per size class (gb_ctx_set_class_opts):
+    its runs that are given no options then use them.  Default: the committed
+    table (tables/classes_scc.json)."""
+    if table is None:
+        table = load(DEFAULT_TABLE)
+    classes = table.get("classes", [])
+    ctx.set_class_opts(class_bounds(table), [dict_to_opts(c["opts"]) for c in classes])
+
+
 def opts_for(table: dict, n: int) -> Opts:
     """Options of the class whose vertex count is nearest n on a log scale
     (the defaults when the table is empty)."""
@@ -95,3 +129,20 @@ def opts_for(table: dict, n: int) -> Opts:
     ln = math.log2(max(n, 1))
     best = min(classes, key=lambda c: abs(math.log2(max(c["n"], 1)) - ln))
     return dict_to_opts(best["opts"])
+
+
+def main(argv: list[str]) -> None:
+    out = argv[0] if argv else DEFAULT_TABLE
+    ctx = Context(0)
+    table = tune_classes(ctx, 0)
+    table["how"] = ("gb_tune on one seeded R-MAT graph per class (a=0.57 b=0.19 c=0.19, seed 1), "
+                    "coordinate descent from the defaults, best of 3 device-timed runs per option set")
+    os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
+    save(table, out)
+    for c in table["classes"]:
+        print(f"n={c['n']:>9} default {c['default_ms']:.4f} ms  tuned {c['ms']:.4f} ms  {c['opts']}")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -163,6 +163,16 @@ gb_status gb_ctx_sync(gb_ctx* ctx);
  * (CUDA events).  Waits for the context's stream.  Lets a caller time every
  * phase of a run of asynchronous calls. */
 gb_status gb_ctx_phase_times(gb_ctx* ctx, int32_t count, double* ms);
+/* Options per size class for the runs of this context that are given no
+ * options (opts NULL in gb_scc, gb_wcc, the batch runs, gb_scc_edges, and the
+ * merged runs of a server whose options were not set): entry i applies to a
+ * graph (or batch union, or merged set) of at most n_max[i] vertices; the
+ * last entry also covers larger ones.  n_max rises.  count 0 removes the
+ * table.  A table comes from the autotuner run over seeded graphs of each
+ * class (connectivity_gb300/tune.py writes one).  No reference counterpart:
+ * the reference's switch constants are fixed (scc_main.cpp:64-65). */
+gb_status gb_ctx_set_class_opts(gb_ctx* ctx, int32_t count, const int64_t* n_max,
+                                const gb_opts* opts);
 /* Diagnostic: the step trace of the context's last completed run (its last
  * 128 records), oldest first: device time (ns) at the start of each step,
  * the step's input count, and a mode.  Reachability steps: bit 0 pull step,

@@ -41,3 +41,28 @@ def test_tune_batch_and_classes(ctx, tmp_path):
     back = tune.load(tmp_path / "t.json")
     assert [c["n"] for c in back["classes"]] == [1 << 10, 1 << 13]
     b.close()
+
+
+def test_class_table_applies_to_runs_without_options(ctx):
+    """A context's class table gives runs without options their class's
+    options (here: the one-block path off for small graphs, on for larger
+    ones); runs given options keep them; labels never change."""
+    c2 = gb.Context(0)
+    n, s, d = graphs.rmat(11, 8, 2)  # 2,048 vertices
+    g = gb.Graph.from_edges(c2, n, s, d)
+    want = oracle.scc(oracle.CpuGraph(n, s, d))
+    assert c2.scc(g, stats=True)[1].grid_blocks == 1  # no table: the one-block path
+    c2.set_class_opts([4096, 1 << 62], [gb.opts(small_path=0), gb.opts()])
+    lab, st = c2.scc(g, stats=True)
+    assert st.grid_blocks > 1 and np.array_equal(lab, want)
+    assert c2.scc(g, o=gb.opts(small_path=2), stats=True)[1].grid_blocks == 1
+    assert np.array_equal(c2.scc_edges(n, s, d), want)
+    with pytest.raises(gb.GBError):
+        c2.set_class_opts([10, 5], [gb.opts(), gb.opts()])
+    c2.set_class_opts([], [])
+    assert c2.scc(g, stats=True)[1].grid_blocks == 1
+    # the committed table, installed
+    tune.install(c2)
+    assert np.array_equal(c2.scc(g), want)
+    g.close()
+    c2.close()
