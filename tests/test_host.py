@@ -286,6 +286,8 @@ def test_tune_table_lookup():
     assert (o.t_grid, o.k_pull, o.grid_blocks, o.expand_mode) == (131072, 4, 76, 1)
     back = tune.dict_to_opts(tune.opts_to_dict(o))
     assert back.beta == 100.0 and back.expand_mode == 1
+    # options outside the tuned set keep their defaults
+    assert (back.trim_level, back.fwbw_rounds, back.trim_pairs) == (1, 1, 0)
     # class bounds: geometric midpoints, the last class open-ended
     assert tune.class_bounds(table) == [1 << 15, 1 << 62]
     assert tune.class_bounds({}) == []
@@ -303,5 +305,3 @@ def test_committed_class_table():
         assert c["ms"] <= c["default_ms"]
     b = tune.class_bounds(table)
     assert all(x < y for x, y in zip(b, b[1:]))
-    # options outside the tuned set keep their defaults
-    assert (back.trim_level, back.fwbw_rounds, back.trim_pairs) == (1, 1, 0)
