@@ -15,7 +15,9 @@ value : the CSR and its pull hints already resident in HBM, labels written
         its hints freed (what gb_run_scc, which builds no hints, runs).
 e2e   : the reference-shaped C-ABI call gb_run_scc (the run_scc signature
         with the reference's 32-bit CSR layout) on pinned host buffers: every
-        step copies the CSR host->device and the labels device->host.
+        step reads the out-CSR and both offset arrays from host memory
+        (the in-lists are derived on the device) and writes the labels
+        device->host; e2e.copy_in_lists: the same with both CSRs read.
 wcc   : WCC (run_cc on the mirrored graph) of the same graph: gb_wcc device
         resident, and gb_run_cc end to end on the mirrored 32-bit CSR.
 Parity: the canonical labels' SHA-256 and the verify lines are compared with
@@ -396,20 +398,24 @@ def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu, ws=1, rank=0):
     for _ in range(K):
         ctx.batch_wcc(b, labels=wl.data_ptr())
     t_wcc = (time.perf_counter() - t0) / K
-    # per-graph launches: every graph in turn (the first `S`), resident
+    # per-graph launches: every graph in turn (the first `S`), resident, with
+    # the committed size-class options (each graph's own class)
+    from connectivity_gb300 import tune as gbtune
+    gbtune.install(ctx)
     S = min(2000, b.count)
     gs = [gb.Graph.rmat_n(ctx, int(ns[i]), int(efs[i]), int(seeds[i])) for i in range(S)]
     outs = [torch.empty(max(g.n, 1), dtype=torch.int32, device="cuda") for g in gs]
     for g, lab in zip(gs[:20], outs[:20]):
-        ctx.scc_async(g, lab.data_ptr(), o)
+        ctx.scc_async(g, lab.data_ptr())
     ctx.sync()
     e0.record(stream)
     for g, lab in zip(gs, outs):
-        ctx.scc_async(g, lab.data_ptr(), o)
+        ctx.scc_async(g, lab.data_ptr())
     e1.record(stream)
     torch.cuda.synchronize()
     ctx.sync()
     t_alone = e0.elapsed_time(e1) / 1e3
+    ctx.set_class_opts([], [])
     same = all(np.array_equal(outs[i][:gs[i].n].cpu().numpy(),
                               batch_lab[b.vbase[i]:b.vbase[i + 1]]) for i in range(S))
     for g in gs:
@@ -428,7 +434,8 @@ def batched_section(gb, ctx, stream, steps, cpu_sample, want_cpu, ws=1, rank=0):
         "steps": K, "gteps": round(b.m / t_scc / 1e9, 2),
         "wcc_graphs_per_s": round(b.count / t_wcc, 1),
         "per_graph_graphs_per_s": round(S / t_alone, 1),
-        "per_graph_sample": f"first {S} graphs of the batch, resident, gb_scc_async back to back",
+        "per_graph_sample": (f"first {S} graphs of the batch, resident, gb_scc_async back to back "
+                             "with each graph's size-class options (the committed table)"),
         "speedup_vs_per_graph": round((BATCH_COUNT / t_scc) / (S / t_alone) / ws, 1),
         "labels_equal_per_graph_runs": bool(same), "build_s": round(build_s, 2),
         "autotuned": {"graphs_per_s": round(b.count / (tuned["ms"] / 1e3), 1),
@@ -553,11 +560,11 @@ def served_section(gb, device, rates, seconds, pool_size, want_cpu):
     ctx = gb.Context(device)
 
     def alone(i, kind, out=None):
+        # one request on its own: the one-call path from its edges (one block
+        # for a small graph, else a device graph built, run and freed)
         n, s, d = pool[i]
-        g = gb.Graph.from_edges(ctx, n, s, d)
-        lab = ctx.scc(g, labels=out) if kind == 0 else ctx.wcc(g, labels=out)
-        g.close()
-        return lab
+        return ctx.scc_edges(n, s, d, labels=out) if kind == 0 else ctx.wcc_edges(n, s, d,
+                                                                                 labels=out)
 
     for i in range(min(20, pool_size)):
         alone(i, 0)
@@ -577,6 +584,11 @@ def served_section(gb, device, rates, seconds, pool_size, want_cpu):
             ref_svc = np.stack([np.array(per_scc), np.array(per_cc)], axis=1)
             ref_kind = "reference"
     sctx = gb.Context(device)
+    # the merged runs take their size class's options (the committed table);
+    # the one-at-a-time runs likewise
+    from connectivity_gb300 import tune as gbtune
+    gbtune.install(sctx)
+    gbtune.install(ctx)
     # one warm-up stream through a server on the same context, so that
     # one-time costs (the memory pool's first growth, first launches) stay
     # out of the measured streams
@@ -764,8 +776,22 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
         gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
     TE = allmax(time.perf_counter() - t0)
     e2e_ok = bool(np.array_equal(out_p, gpu_labels))
-    h2d = (n + 1) * 4 * 2 + m * 4 * 2
+    # gb_run_scc reads the out-CSR and both offset arrays; the in-lists are
+    # derived on the device (in_array is not read)
+    h2d = (n + 1) * 4 * 2 + m * 4
     d2h = n * 4
+    # the same calls with in_array copied as given (both CSRs over the link)
+    gb.dropin_set_copy_in(True)
+    try:
+        gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)  # warm-up
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(KE):
+            gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
+        TEC = allmax(time.perf_counter() - t0)
+        e2e_copy_ok = bool(np.array_equal(out_p, gpu_labels))
+    finally:
+        gb.dropin_set_copy_in(False)
     # the mirrored 32-bit CSR of cc's reader (per vertex: out- then
     # in-neighbours), for gb_run_cc
     odeg, ideg = np.diff(oo), np.diff(io)
@@ -851,8 +877,15 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(TE / KE * 1e3, 3), "steps": KE,
                 "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers; "
-                       "builds no hints)",
-                "labels_match_device_run": e2e_ok},
+                       "builds no hints; in-lists derived on the device from the out-CSR, "
+                       "in_array not read)",
+                "labels_match_device_run": e2e_ok,
+                "copy_in_lists": {"value": round(job_gteps(m, ws, TEC, KE), 3),
+                                  "ms_per_step": round(TEC / KE * 1e3, 3),
+                                  "h2d_bytes_per_step": (n + 1) * 4 * 2 + m * 4 * 2,
+                                  "api": "gb_run_scc after gb_dropin_set_copy_in(1): both CSRs "
+                                         "read as given",
+                                  "labels_match_device_run": e2e_copy_ok}},
         "wcc": {"value": round(job_gteps(2 * m, ws, T_w, K), 3), "unit": "GTEPS (mirrored arcs)",
                 "arcs": 2 * m, "ms_per_step": round(T_w / K * 1e3, 4), "steps": K,
                 "api": "gb_wcc on the resident graph (out- and in-CSR walked as the mirrored "
@@ -943,7 +976,7 @@ def run_gbconn(args):
         rates = [r if r == "max" else float(r) for r in args.serve_rates.split(",") if r]
         line["served"] = served_section(gb, local, rates, args.serve_seconds, args.serve_pool,
                                         want_cpu)
-        line["served"]["opts"] = "defaults"
+        line["served"]["opts"] = "size-class table (connectivity_gb300/tables/classes_scc.json)"
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

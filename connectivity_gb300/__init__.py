@@ -160,6 +160,7 @@ for _n in ("gb_scc", "gb_wcc", "gb_cc"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
 for _n in ("gb_scc_async", "gb_wcc_async"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
+_sig("gb_dropin_set_copy_in", C.c_int32, [C.c_int32])
 _sig("gb_run_scc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int])
 _sig("gb_run_cc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, C.c_int, C.c_double])
 _sig("gb_read_edge", C.c_int32, [C.c_char_p, _I32P, _I64P, C.POINTER(_P), C.POINTER(_P)])
@@ -512,6 +513,21 @@ class Graph:
         return cls(h)
 
     @classmethod
+    def from_csr32(cls, ctx: Context, n: int, out_array, out_degree_list, in_array=None,
+                   in_degree_list=None) -> "Graph":
+        """gb_graph_from_csr32: the reference's 32-bit CSR layout.  With
+        in_degree_list given and in_array None, the in-lists are derived on
+        the device from the out-CSR.  Arrays are used as given (pinned
+        arrays are read by the device directly), so they must already be
+        contiguous uint32 offsets and int32 ids."""
+        h = C.c_void_p()
+        m = int(out_degree_list[n])
+        _check(_lib.gb_graph_from_csr32(ctx._h, n, m, _ptr(out_array), _ptr(out_degree_list),
+                                        _ptr(in_array), _ptr(in_degree_list), C.byref(h)),
+               "gb_graph_from_csr32")
+        return cls(h)
+
+    @classmethod
     def rmat(cls, ctx: Context, scale: int, edge_factor: int = 16, seed: int = 1,
              abc: tuple[float, float, float] = RMAT_ABC) -> "Graph":
         h = C.c_void_p()
@@ -706,6 +722,12 @@ def run_scc_ref(n: int, out_array, in_array, out_degree_list, in_degree_list,
     return scc_maps
 
 
+def dropin_set_copy_in(copy: bool) -> None:
+    """gb_dropin_set_copy_in: whether gb_run_scc copies in_array (True) or
+    derives the in-lists on the device from the out-CSR (False, default)."""
+    _check(_lib.gb_dropin_set_copy_in(1 if copy else 0), "gb_dropin_set_copy_in")
+
+
 def run_cc_ref(n: int, out_array, out_degree_list, max_deg_vert: int = -1,
                avg_degree: float = 0.0, cc_maps: np.ndarray | None = None) -> np.ndarray:
     """gb_run_cc: the reference's run_cc signature on the mirrored host CSR."""
@@ -726,4 +748,5 @@ __all__ = [
     "Context", "Graph", "GBError", "Opts", "Stats", "opts", "read_edge", "output_labels",
     "scc_verify", "cc_verify", "canonicalize", "rmat_edges", "grid_edges", "batch_sizes",
     "csr_from_edges", "run_scc_ref", "run_cc_ref", "LIB_PATH", "Batch", "rmat_edges_n",
+    "dropin_set_copy_in",
 ]

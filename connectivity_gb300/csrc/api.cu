@@ -1,6 +1,7 @@
 // C ABI of libgbconn (include/gbconn.h): contexts, device graphs, runs and
 // the reference-shaped drop-ins.  Host code only; the kernels live in
 // kernels.cu and csr_build.cu.
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -436,6 +437,7 @@ using gb::validate_csr;
 std::mutex g_default_mu;
 gb_ctx* g_default_ctx = nullptr;
 gb_graph* g_stage = nullptr;     // reused device buffers of the drop-ins
+std::atomic<int> g_dropin_copy_in{0};  // gb_run_scc: 1 = copy in_array, 0 = derive
 int64_t g_stage_m = -1;
 int32_t g_stage_n = -1;
 
@@ -739,60 +741,88 @@ static const void* pinned_view(const void* p) {
 
 // Fills g (whose buffers hold at least n / m) from the reference's CSR layout.
 // Pinned host arrays are read by the ingest kernels directly (one crossing
-// of the host link, checked on the way); other memory is copied, widened
-// and then checked on the device.
+// of the host link, checked on the way); other memory is copied first.
+// derive_in (directed graphs, m < 2^31): in_array is not read; the in-lists
+// are written on the device from the out-CSR and checked against idl.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
-                            const uint32_t* odl, const int32_t* in_array, const uint32_t* idl) {
-  {
-    const void* vo = pinned_view(odl);
-    const void* va = m > 0 ? pinned_view(out_array) : odl;
-    const void* vi = g->symmetric ? odl : pinned_view(idl);
-    const void* vb = g->symmetric || m == 0 ? odl : pinned_view(in_array);
-    if (vo && va && vi && vb) {
-      int* d_bad = nullptr;
-      CK(cudaMallocAsync(&d_bad, sizeof(int), c->stream), "ingest");
-      gb_status s = GB_OK;
-      cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
-      if (e == cudaSuccess)
-        e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
-                             d_bad, c->stream);
-      if (e == cudaSuccess && !g->symmetric)
-        e = gb::ingest_csr32(n, m, (const uint32_t*)vi, (const int32_t*)vb, g->in_off, g->in_adj,
-                             d_bad, c->stream);
-      int bad = 0;
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-      cudaFreeAsync(d_bad, c->stream);
-      if (e != cudaSuccess) return cuda_fail(e, "ingest");
-      if (bad) {
-        gb_set_error("CSR check: %s", "offsets not monotone from 0 to m, or an id outside [0, n)");
-        s = GB_ERR_INVALID;
+                            const uint32_t* odl, const int32_t* in_array, const uint32_t* idl,
+                            bool derive_in) {
+  derive_in = derive_in && !g->symmetric;
+  const void* vo = pinned_view(odl);
+  const void* va = m > 0 ? pinned_view(out_array) : odl;
+  const void* vi = g->symmetric ? odl : pinned_view(idl);
+  const void* vb = g->symmetric || m == 0 || derive_in ? odl : pinned_view(in_array);
+  uint32_t* tmp = nullptr;
+  if (!(vo && va && vi && vb)) {
+    if (!derive_in) {
+      CK(cudaMallocAsync(&tmp, (size_t)(n + 1) * 4, c->stream), "offset staging");
+      gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);
+      if (s == GB_OK) CK(gb::widen_offsets(tmp, g->out_off, (int64_t)n + 1, c->stream), "widen");
+      if (s == GB_OK) s = upload(c, g->out_adj, out_array, (size_t)m * 4);
+      if (s == GB_OK && !g->symmetric) {
+        s = upload(c, tmp, idl, (size_t)(n + 1) * 4);
+        if (s == GB_OK) CK(gb::widen_offsets(tmp, g->in_off, (int64_t)n + 1, c->stream), "widen");
+        if (s == GB_OK) s = upload(c, g->in_adj, in_array, (size_t)m * 4);
       }
+      cudaFreeAsync(tmp, c->stream);
+      if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
+      if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
       return s;
     }
+    // staged on the device, then ingested from there (the out-lists in place)
+    CK(cudaMallocAsync(&tmp, (size_t)(n + 1) * 8, c->stream), "offset staging");
+    gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);
+    if (s == GB_OK) s = upload(c, tmp + n + 1, idl, (size_t)(n + 1) * 4);
+    if (s == GB_OK) s = upload(c, g->out_adj, out_array, (size_t)m * 4);
+    if (s != GB_OK) {
+      cudaFreeAsync(tmp, c->stream);
+      return s;
+    }
+    vo = tmp;
+    vi = tmp + n + 1;
+    va = g->out_adj;
   }
-  uint32_t* tmp = nullptr;
-  CK(cudaMallocAsync(&tmp, (size_t)(n + 1) * 4, c->stream), "offset staging");
-  gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);
-  if (s == GB_OK) CK(gb::widen_offsets(tmp, g->out_off, (int64_t)n + 1, c->stream), "widen");
-  if (s == GB_OK) s = upload(c, g->out_adj, out_array, (size_t)m * 4);
-  if (s == GB_OK && !g->symmetric) {
-    s = upload(c, tmp, idl, (size_t)(n + 1) * 4);
-    if (s == GB_OK) CK(gb::widen_offsets(tmp, g->in_off, (int64_t)n + 1, c->stream), "widen");
-    if (s == GB_OK) s = upload(c, g->in_adj, in_array, (size_t)m * 4);
+  int* d_bad = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_bad, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+  if (e == cudaSuccess && derive_in)
+    e = gb::ingest_csr32_derive_in(n, m, (const uint32_t*)vo, (const int32_t*)va,
+                                   (const uint32_t*)vi, g->out_off, g->out_adj, g->in_off,
+                                   g->in_adj, d_bad, c->stream);
+  if (e == cudaSuccess && !derive_in)
+    e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
+                         d_bad, c->stream);
+  if (e == cudaSuccess && !derive_in && !g->symmetric)
+    e = gb::ingest_csr32(n, m, (const uint32_t*)vi, (const int32_t*)vb, g->in_off, g->in_adj,
+                         d_bad, c->stream);
+  int bad = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (d_bad) cudaFreeAsync(d_bad, c->stream);
+  if (tmp) cudaFreeAsync(tmp, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ingest");
+  if (bad) {
+    gb_set_error("CSR check: %s",
+                 derive_in ? "offsets not monotone from 0 to m, an id outside [0, n), or in-degrees "
+                             "that do not match the out-CSR"
+                           : "offsets not monotone from 0 to m, or an id outside [0, n)");
+    return GB_ERR_INVALID;
   }
-  cudaFreeAsync(tmp, c->stream);
-  if (s == GB_OK) s = validate_csr(c, n, m, g->out_off, g->out_adj);
-  if (s == GB_OK && !g->symmetric) s = validate_csr(c, n, m, g->in_off, g->in_adj);
-  return s;
+  return GB_OK;
 }
 
 gb_status gb_graph_from_csr32(gb_ctx* c, int32_t n, uint32_t m, const int32_t* out_array,
                               const uint32_t* odl, const int32_t* in_array, const uint32_t* idl,
                               gb_graph** out) {
-  if (!c || !out || n < 0 || !odl || (m > 0 && !out_array) || ((idl == nullptr) != (in_array == nullptr)))
+  if (!c || !out || n < 0 || !odl || (m > 0 && !out_array) || (in_array && !idl))
     return GB_ERR_INVALID;
+  // in-offsets without in-lists: the in-lists come from the out-CSR
+  const bool derive = idl && !in_array;
+  if (derive && m >= (1u << 31)) {
+    gb_set_error("gb_graph_from_csr32: %s", "deriving the in-lists needs m < 2^31");
+    return GB_ERR_INVALID;
+  }
   *out = nullptr;
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   gb_graph* g = new (std::nothrow) gb_graph();
@@ -802,7 +832,7 @@ gb_status gb_graph_from_csr32(gb_ctx* c, int32_t n, uint32_t m, const int32_t* o
   g->m = m;
   g->symmetric = idl == nullptr;
   gb_status s = graph_alloc(g, !g->symmetric);
-  if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl);
+  if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl, derive);
   if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
@@ -1095,11 +1125,18 @@ static gb_status stage_graph(gb_ctx* c, int32_t n, int64_t m, bool symmetric, gb
   return GB_OK;
 }
 
+gb_status gb_dropin_set_copy_in(int32_t copy) {
+  if (copy != 0 && copy != 1) return GB_ERR_INVALID;
+  g_dropin_copy_in.store(copy);
+  return GB_OK;
+}
+
 gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_array,
                      const unsigned* out_degree_list, const unsigned* in_degree_list, int* scc_maps,
                      int max_deg_vert, double avg_degree, int vert_cutoff) {
   (void)avg_degree;
-  if (n < 0 || !out_degree_list || !in_degree_list || (m > 0 && (!out_array || !in_array)) ||
+  const bool derive = g_dropin_copy_in.load() == 0 && m < (1u << 31);
+  if (n < 0 || !out_degree_list || !in_degree_list || (m > 0 && (!out_array || (!derive && !in_array))) ||
       (n > 0 && !scc_maps))
     return GB_ERR_INVALID;
   std::lock_guard<std::mutex> lk(g_default_mu);
@@ -1108,7 +1145,7 @@ gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_arra
   if (s != GB_OK) return s;
   gb_graph* g;
   if ((s = stage_graph(c, n, m, false, &g)) != GB_OK) return s;
-  s = fill_csr32(c, g, n, m, out_array, out_degree_list, in_array, in_degree_list);
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, in_array, in_degree_list, derive);
   if (s != GB_OK) return s;
   gb_opts o;
   gb_opts_default(&o);
@@ -1127,7 +1164,7 @@ gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out
   if (s != GB_OK) return s;
   gb_graph* g;
   if ((s = stage_graph(c, n, m, true, &g)) != GB_OK) return s;
-  s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr);
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr, false);
   if (s != GB_OK) return s;
   gb_opts o;
   gb_opts_default(&o);

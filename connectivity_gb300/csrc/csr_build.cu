@@ -201,6 +201,254 @@ __global__ void k_ingest_adj(const int32_t* __restrict__ h, int32_t* __restrict_
   if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
 }
 
+// ---------------------------------------------------------------------------
+// In-lists derived from the out-CSR.
+//
+// The reference's run_scc takes both CSRs of the graph (graph struct,
+// multistep/scc_main.cpp:75-86, both built by create_csr, :127-191).  The
+// in-CSR is the out-CSR transposed, so a caller that hands over both moves
+// every edge across the host link twice.  Here only the out-CSR and the
+// in-offsets cross it: k_place_in reads the out-adjacency in tiles of kTile
+// edges (from host memory the device maps, or from device memory), stores
+// it, finds each edge's source by a max-scan of the tile's list heads, and
+// writes the source into the target's in-list at the next free slot (an
+// atomic on a per-vertex cursor that starts at the list's first slot).
+// Targets with at least kHubDeg in-edges (a bitmap made with the offsets)
+// take their slots once per tile: the tile's edges to them are counted in a
+// shared hash table, one atomic per (tile, target) reserves a run of slots
+// and the edges take consecutive slots of it, so a hub with hundreds of
+// thousands of in-edges sees one atomic per tile instead of one per edge.
+// Each block loads its next tile before it works on the current one, so the
+// host link stays busy while the block places edges.
+//
+// The order within an in-list is the order of the atomics, not the caller's
+// (no label depends on it).  Slots stay below m, so no write leaves the
+// array; in-offsets that are not those of the out-CSR's transpose leave some
+// cursor off its list's end, which k_check_cursors reports (*bad).  With
+// every cursor at its list's end, every vertex received exactly its
+// in-degree of placements, all inside its own list.
+// ---------------------------------------------------------------------------
+constexpr int kPT = 256;                 // threads per block
+constexpr int kPE = 8;                   // edges per thread
+constexpr int kTile = kPT * kPE;         // edges per tile
+constexpr uint32_t kHubDeg = 2048;       // in-degree from which slots are reserved per tile
+constexpr int kHashBits = 9;
+constexpr int kHash = 1 << kHashBits;    // shared hash entries
+constexpr int kProbe = 8;                // linear probes before the per-edge atomic
+constexpr uint32_t kNoSlot = 0xffffffffu;
+
+// Tile position of a thread's edge k: two runs of four consecutive edges, so
+// the tile is read as 16-byte words with consecutive threads on consecutive
+// words.
+__device__ __forceinline__ int tile_pos(int k) {
+  return (k >> 2) * 4 * kPT + 4 * (int)threadIdx.x + (k & 3);
+}
+
+// In-offsets: widened into off (int64), cursor[v] = off[v] (each list's
+// first free slot), hub bit of v = in-degree >= kHubDeg; checked as
+// k_ingest_off checks.
+__global__ void k_ingest_in_off(const uint32_t* __restrict__ h, int32_t n, int64_t m,
+                                int64_t* __restrict__ off, uint32_t* __restrict__ cursor,
+                                uint32_t* __restrict__ hub_bits, int* bad) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~(int64_t)31; base <= n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + lane;
+    const uint32_t x = i <= n ? h[i] : 0u;
+    uint32_t nx = __shfl_down_sync(0xffffffffu, x, 1);
+    if (lane == 31 && i + 1 <= n) nx = h[i + 1];
+    const unsigned hub = __ballot_sync(0xffffffffu, i < n && nx >= x && nx - x >= kHubDeg);
+    if (lane == 0 && base < n) hub_bits[base >> 5] = hub;
+    if (i <= n) {
+      off[i] = (int64_t)x;
+      if (i < n) cursor[i] = x;
+      if ((i == 0 && x != 0u) || (i == n && (int64_t)x != m) || (i < n && nx < x)) atomicOr(bad, 1);
+    }
+  }
+}
+
+// tile_src[t] = the vertex whose out-list holds edge t * kTile.  Skipped once
+// the offsets were found bad; indexes stay below `tiles` whatever they hold.
+__global__ void k_tile_heads(int32_t n, int64_t tiles, const int64_t* __restrict__ off,
+                             int32_t* __restrict__ tile_src, const int* bad) {
+  if (*(volatile const int*)bad) return;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = off[u], b = off[u + 1];
+    if (a < 0) continue;
+    for (int64_t t = (a + kTile - 1) / kTile; t < tiles && t * kTile < b; ++t)
+      tile_src[t] = (int32_t)u;
+  }
+}
+
+// Every cursor must have reached its list's end.
+__global__ void k_check_cursors(int32_t n, const int64_t* __restrict__ off,
+                                const uint32_t* __restrict__ cursor, int* bad) {
+  bool ok = true;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    ok = ok && (int64_t)cursor[v] == off[v + 1];
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+__global__ void __launch_bounds__(kPT) k_place_in(
+    const int32_t* __restrict__ src_adj, int32_t* __restrict__ out_adj, int64_t m, int32_t n,
+    const int64_t* __restrict__ out_off, const uint32_t* __restrict__ hub_bits,
+    uint32_t* __restrict__ cursor, const int32_t* __restrict__ tile_src,
+    int32_t* __restrict__ in_adj, int* bad) {
+  __shared__ int32_t head[kTile];
+  __shared__ int32_t hkey[kHash];
+  __shared__ uint32_t hval[kHash];  // a target's edge count in the tile, then its first slot
+  __shared__ int32_t wmax[kPT / 32];
+  __shared__ int s_skip;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  // bad offsets (either CSR): nothing is placed, nothing is indexed by them
+  if (tid == 0) s_skip = *(volatile const int*)bad;
+  __syncthreads();
+  if (s_skip) return;
+  const int64_t tiles = (m + kTile - 1) / kTile;
+  const int64_t full_tiles = m / kTile;
+  const bool vec =
+      ((reinterpret_cast<uintptr_t>(src_adj) | reinterpret_cast<uintptr_t>(out_adj)) & 15u) == 0;
+  const bool store = src_adj != out_adj;
+  const uint32_t slot_cap = (uint32_t)m;
+  bool ok = true;
+  int64_t t = blockIdx.x;
+  // the next full tile's words, loaded one tile ahead
+  int4 n0 = make_int4(0, 0, 0, 0), n1 = n0;
+  if (vec && t < full_tiles) {
+    const int4* s4 = reinterpret_cast<const int4*>(src_adj + t * kTile);
+    n0 = s4[tid];
+    n1 = s4[kPT + tid];
+  }
+  for (; t < tiles; t += gridDim.x) {
+    const int64_t e0 = t * kTile;
+    const int len = (int)(m - e0 < kTile ? m - e0 : kTile);
+    // 1. the tile's targets
+    int32_t w[kPE];
+    if (vec && t < full_tiles) {
+      const int4 q0 = n0, q1 = n1;
+      const int64_t tn = t + gridDim.x;
+      if (tn < full_tiles) {
+        const int4* s4 = reinterpret_cast<const int4*>(src_adj + tn * kTile);
+        n0 = s4[tid];
+        n1 = s4[kPT + tid];
+      }
+      if (store) {
+        int4* d4 = reinterpret_cast<int4*>(out_adj + e0);
+        d4[tid] = q0;
+        d4[kPT + tid] = q1;
+      }
+      w[0] = q0.x; w[1] = q0.y; w[2] = q0.z; w[3] = q0.w;
+      w[4] = q1.x; w[5] = q1.y; w[6] = q1.z; w[7] = q1.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kPE; ++k) {
+        const int p = tile_pos(k);
+        w[k] = p < len ? src_adj[e0 + p] : 0;
+        if (p < len && store) out_adj[e0 + p] = w[k];
+      }
+    }
+    // 2. sources: every out-list starting inside the tile marks its first
+    // position, the list holding edge e0 marks position 0; a max-scan then
+    // gives every position its list's vertex
+    for (int i = tid; i < kTile; i += kPT) head[i] = -1;
+    for (int i = tid; i < kHash; i += kPT) {
+      hkey[i] = -1;
+      hval[i] = 0u;
+    }
+    __syncthreads();
+    const int32_t u0 = tile_src[t];
+    if (u0 < 0 || u0 >= n) {
+      ok = false;  // not reached with checked offsets
+    } else {
+      const int64_t e1 = e0 + len;
+      for (int64_t u = (int64_t)u0 + tid; u < n; u += kPT) {
+        const int64_t a = out_off[u];
+        if (a >= e1) break;
+        if (out_off[u + 1] > a) atomicMax(&head[a > e0 ? (int)(a - e0) : 0], (int32_t)u);
+      }
+    }
+    __syncthreads();
+    {
+      int32_t x[kPE];
+      int32_t run = -1;
+#pragma unroll
+      for (int k = 0; k < kPE; ++k) {
+        run = max(run, head[tid * kPE + k]);
+        x[k] = run;
+      }
+      int32_t inc = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc = max(inc, y);
+      }
+      int32_t pre = __shfl_up_sync(0xffffffffu, inc, 1);
+      if (lane == 0) pre = -1;
+      if (lane == 31) wmax[wid] = inc;
+      __syncthreads();
+      for (int i = 0; i < wid; ++i) pre = max(pre, wmax[i]);
+#pragma unroll
+      for (int k = 0; k < kPE; ++k) head[tid * kPE + k] = max(pre, x[k]);
+    }
+    __syncthreads();
+    // 3. slots.  A thread's loads come first (sources, hub bits), then its
+    // hub edges are counted in the shared table, then the other edges'
+    // atomics are issued together and only then their stores, so its eight
+    // atomics are in flight at once.
+    int32_t us[kPE];
+    uint32_t info[kPE];  // hub edge: (table entry << 16) | rank in the tile
+#pragma unroll
+    for (int k = 0; k < kPE; ++k) {
+      const int p = tile_pos(k);
+      const bool in = p < len && (uint32_t)w[k] < (uint32_t)n;
+      if (p < len && !in) ok = false;
+      us[k] = in ? head[p] : -1;
+      if (in && us[k] < 0) ok = false;
+      info[k] = in ? __ldg(hub_bits + (w[k] >> 5)) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kPE; ++k) {
+      const int32_t v = w[k];
+      const bool hub = us[k] >= 0 && ((info[k] >> (v & 31)) & 1u);
+      info[k] = kNoSlot;
+      if (!hub) continue;
+      uint32_t h = ((uint32_t)v * 2654435761u) >> (32 - kHashBits);
+      int probe = 0;
+      for (; probe < kProbe; ++probe) {
+        const int32_t k0 = atomicCAS(&hkey[h], -1, v);
+        if (k0 == -1 || k0 == v) break;
+        h = (h + 1) & (kHash - 1);
+      }
+      if (probe < kProbe) info[k] = (h << 16) | atomicAdd(&hval[h], 1u);
+    }
+    uint32_t slot[kPE];
+#pragma unroll
+    for (int k = 0; k < kPE; ++k)
+      slot[k] = (us[k] >= 0 && info[k] == kNoSlot) ? atomicAdd(&cursor[w[k]], 1u) : kNoSlot;
+#pragma unroll
+    for (int k = 0; k < kPE; ++k)
+      if (slot[k] < slot_cap) in_adj[slot[k]] = us[k];
+    __syncthreads();
+    for (int h = tid; h < kHash; h += kPT) {
+      const uint32_t c = hval[h];
+      if (c == 0u) continue;
+      const uint32_t base = atomicAdd(&cursor[hkey[h]], c);
+      hval[h] = (uint64_t)base + c <= (uint64_t)slot_cap ? base : kNoSlot;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPE; ++k) {
+      if (info[k] == kNoSlot) continue;
+      const uint32_t b = hval[info[k] >> 16];
+      if (b != kNoSlot) in_adj[b + (info[k] & 0xffffu)] = us[k];
+    }
+    __syncthreads();
+  }
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicOr(bad, 1);
+}
+
 // Pivot keys: out*in (kind 0) or degree (kind 1).
 __device__ __forceinline__ unsigned long long pivot_key(const int64_t* out_off, const int64_t* in_off,
                                                         int kind, int64_t v) {
@@ -464,6 +712,55 @@ cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int3
   if (e != cudaSuccess || m == 0) return e;
   k_ingest_adj<<<grid_for(m / 4 + 1), 256, 0, s>>>(h_adj, adj, m, n, d_bad);
   return cudaGetLastError();
+}
+
+cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_off,
+                                   const int32_t* h_out_adj, const uint32_t* h_in_off,
+                                   int64_t* out_off, int32_t* out_adj, int64_t* in_off,
+                                   int32_t* in_adj, int* d_bad, cudaStream_t s) {
+  if (m >= (1ll << 31)) return cudaErrorInvalidValue;
+  k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_out_off, out_off, n, m, d_bad);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int64_t tiles = (m + kTile - 1) / kTile;
+  const int64_t words = ((int64_t)n + 31) / 32;
+  // cursors (n), hub bits (words), tile heads (tiles)
+  uint32_t* tmp = nullptr;
+  e = cudaMallocAsync(&tmp, ((size_t)n + (size_t)words + (size_t)tiles + 1) * 4, s);
+  if (e != cudaSuccess) return e;
+  uint32_t* cursor = tmp;
+  uint32_t* hub_bits = cursor + n;
+  int32_t* tile_src = reinterpret_cast<int32_t*>(hub_bits + words);
+  k_ingest_in_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_in_off, n, m, in_off, cursor,
+                                                           hub_bits, d_bad);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && m > 0) {
+    cudaMemsetAsync(tile_src, 0xff, (size_t)tiles * 4, s);
+    k_tile_heads<<<grid_for(n), 256, 0, s>>>(n, tiles, out_off, tile_src, d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && m > 0) {
+    static int blocks[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (blocks[dev] == 0) {
+      int per_sm = 0, sms = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_in, kPT, 0);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      blocks[dev] = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    }
+    const int g = (int)(tiles < blocks[dev] ? tiles : blocks[dev]);
+    k_place_in<<<g, kPT, 0, s>>>(h_out_adj, out_adj, m, n, out_off, hub_bits, cursor, tile_src,
+                                 in_adj, d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && n > 0) {
+    k_check_cursors<<<grid_for(n), 256, 0, s>>>(n, in_off, cursor, d_bad);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(tmp, s);
+  return e;
 }
 
 cudaError_t pivot_device(int32_t n, const int64_t* out_off, const int64_t* in_off, int kind,

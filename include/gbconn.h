@@ -206,7 +206,12 @@ gb_status gb_graph_from_csr(gb_ctx* ctx, int32_t n, int64_t m, const int64_t* ou
                             const int32_t* in_adj, gb_graph** g);
 /* From the reference's own CSR layout (graph struct, scc_main.cpp:75-86):
  * 32-bit unsigned offsets out_degree_list[n+1] / in_degree_list[n+1].
- * in_* may be NULL (symmetric graph of cc_main.cpp:72-79). */
+ * in_* may be NULL (symmetric graph of cc_main.cpp:72-79).  in_array NULL
+ * with in_degree_list given (m < 2^31): the in-lists are written on the
+ * device from the out-CSR while it is read (only the out-CSR and the
+ * in-offsets cross the host link); their order within a vertex is then not
+ * the caller's, and in-offsets that are not those of the out-CSR's
+ * transpose give GB_ERR_INVALID. */
 gb_status gb_graph_from_csr32(gb_ctx* ctx, int32_t n, uint32_t m, const int32_t* out_array,
                               const uint32_t* out_degree_list, const int32_t* in_array,
                               const uint32_t* in_degree_list, gb_graph** g);
@@ -424,6 +429,14 @@ gb_status gb_server_stats_get(gb_server* server, gb_server_stats* stats);
 gb_status gb_server_destroy(gb_server* server);
 
 /* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
+/* How gb_run_scc gets the in-lists.  copy = 0 (default): in_array is not
+ * read; the in-lists are derived on the device from the out-CSR and checked
+ * against in_degree_list, as gb_graph_from_csr32 does with in_array NULL, so
+ * half of the graph's bytes stay off the host link (in_array may be NULL).
+ * copy = 1: in_array is copied as given.  Labels are the same either way
+ * for an in-CSR that is the out-CSR's transpose, which is what create_csr
+ * (scc_main.cpp:127-191) builds.  Graphs of m >= 2^31 always copy. */
+gb_status gb_dropin_set_copy_in(int32_t copy);
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
  * fields passed one by one and scc_maps owned by the caller (n ints).  Uses
