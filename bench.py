@@ -15,9 +15,11 @@ value : the CSR and its pull hints already resident in HBM, labels written
         its hints freed (what gb_run_scc, which builds no hints, runs).
 e2e   : the reference-shaped C-ABI call gb_run_scc (the run_scc signature
         with the reference's 32-bit CSR layout) on pinned host buffers: every
-        step reads the out-CSR and both offset arrays from host memory
-        (the in-lists are derived on the device) and writes the labels
-        device->host; e2e.copy_in_lists: the same with both CSRs read.
+        step reads the out-CSR, both offset arrays and the in-lists of the
+        last fifth of the in-edges from host memory (the others are derived
+        on the device from the out-CSR) and writes the labels
+        device->host; e2e.by_share: the same with the in-lists all copied
+        (0.0) or all derived (1.0).
 wcc   : WCC (run_cc on the mirrored graph) of the same graph: gb_wcc device
         resident, and gb_run_cc end to end on the mirrored 32-bit CSR.
 Parity: the canonical labels' SHA-256 and the verify lines are compared with
@@ -59,6 +61,7 @@ sys.path.insert(0, ROOT)
 METRIC = "SCC GTEPS on R-MAT-24 (1 GB300) vs host OpenMP; batched graphs/s and p99 ms"
 SCALE, EF, SEED = 24, 16, 1
 BATCH_COUNT = 20000
+E2E_SHARE = 0.8  # gb_run_scc's default share of in-lists derived on the device
 BATCH_DIST = dict(seed=4, median=2000.0, sigma=1.5, n_min=64, n_max=500000, ef_min=4, ef_max=32)
 ABC = (0.57, 0.19, 0.19)
 PINS = os.path.join(ROOT, "tests", "golden", "pins.json")
@@ -768,6 +771,7 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
     oa_p, ia_p = pin(oa), pin(ia)
     out_p = pin(np.empty(n, np.int32))
     piv, avg = ctx.pivot(g, 0)
+    gb.dropin_set_derive_share(E2E_SHARE)
     gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)  # warm-up
     KE = max(1, min(args.e2e_steps, K))
     barrier()
@@ -776,22 +780,26 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
         gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
     TE = allmax(time.perf_counter() - t0)
     e2e_ok = bool(np.array_equal(out_p, gpu_labels))
-    # gb_run_scc reads the out-CSR and both offset arrays; the in-lists are
-    # derived on the device (in_array is not read)
-    h2d = (n + 1) * 4 * 2 + m * 4
+    # gb_run_scc reads the out-CSR, both offset arrays and the part of
+    # in_array it does not derive on the device
+    e_split = int(idl[np.searchsorted(idl, E2E_SHARE * m, side="left")]) if m else 0
+    h2d = (n + 1) * 4 * 2 + m * 4 + (m - e_split) * 4
     d2h = n * 4
-    # the same calls with in_array copied as given (both CSRs over the link)
-    gb.dropin_set_copy_in(True)
-    try:
-        gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)  # warm-up
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(KE):
-            gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
-        TEC = allmax(time.perf_counter() - t0)
-        e2e_copy_ok = bool(np.array_equal(out_p, gpu_labels))
-    finally:
-        gb.dropin_set_copy_in(False)
+    # the same calls at the two ends of the split: in-lists all copied, and
+    # all derived on the device
+    shares = {}
+    for share in (0.0, 1.0):
+        gb.dropin_set_derive_share(share)
+        try:
+            gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)  # warm-up
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(KE):
+                gb.run_scc_ref(n, oa_p, ia_p, odl, idl, piv, avg, 10000, out_p)
+            ts = allmax(time.perf_counter() - t0)
+            shares[share] = (ts, bool(np.array_equal(out_p, gpu_labels)))
+        finally:
+            gb.dropin_set_derive_share(E2E_SHARE)
     # the mirrored 32-bit CSR of cc's reader (per vertex: out- then
     # in-neighbours), for gb_run_cc
     odeg, ideg = np.diff(oo), np.diff(io)
@@ -877,15 +885,15 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(TE / KE * 1e3, 3), "steps": KE,
                 "api": "gb_run_scc (run_scc signature, reference CSR layout, pinned host buffers; "
-                       "builds no hints; in-lists derived on the device from the out-CSR, "
-                       "in_array not read)",
+                       "builds no hints; the in-lists of the first derive_share of the in-edges "
+                       "derived on the device from the out-CSR, the rest of in_array copied "
+                       "beside them)",
                 "labels_match_device_run": e2e_ok,
-                "copy_in_lists": {"value": round(job_gteps(m, ws, TEC, KE), 3),
-                                  "ms_per_step": round(TEC / KE * 1e3, 3),
-                                  "h2d_bytes_per_step": (n + 1) * 4 * 2 + m * 4 * 2,
-                                  "api": "gb_run_scc after gb_dropin_set_copy_in(1): both CSRs "
-                                         "read as given",
-                                  "labels_match_device_run": e2e_copy_ok}},
+                "derive_share": E2E_SHARE,
+                "by_share": {str(k): {"value": round(job_gteps(m, ws, v[0], KE), 3),
+                                      "ms_per_step": round(v[0] / KE * 1e3, 3),
+                                      "labels_match_device_run": v[1]}
+                             for k, v in shares.items()}},
         "wcc": {"value": round(job_gteps(2 * m, ws, T_w, K), 3), "unit": "GTEPS (mirrored arcs)",
                 "arcs": 2 * m, "ms_per_step": round(T_w / K * 1e3, 4), "steps": K,
                 "api": "gb_wcc on the resident graph (out- and in-CSR walked as the mirrored "

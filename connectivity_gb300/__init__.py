@@ -160,7 +160,7 @@ for _n in ("gb_scc", "gb_wcc", "gb_cc"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts), C.POINTER(Stats)])
 for _n in ("gb_scc_async", "gb_wcc_async"):
     _sig(_n, C.c_int32, [_P, _P, _P, C.POINTER(Opts)])
-_sig("gb_dropin_set_copy_in", C.c_int32, [C.c_int32])
+_sig("gb_dropin_set_derive_share", C.c_int32, [C.c_double])
 _sig("gb_run_scc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, _P, _P, C.c_int, C.c_double, C.c_int])
 _sig("gb_run_cc", C.c_int32, [C.c_int, C.c_uint, _P, _P, _P, C.c_int, C.c_double])
 _sig("gb_read_edge", C.c_int32, [C.c_char_p, _I32P, _I64P, C.POINTER(_P), C.POINTER(_P)])
@@ -722,10 +722,11 @@ def run_scc_ref(n: int, out_array, in_array, out_degree_list, in_degree_list,
     return scc_maps
 
 
-def dropin_set_copy_in(copy: bool) -> None:
-    """gb_dropin_set_copy_in: whether gb_run_scc copies in_array (True) or
-    derives the in-lists on the device from the out-CSR (False, default)."""
-    _check(_lib.gb_dropin_set_copy_in(1 if copy else 0), "gb_dropin_set_copy_in")
+def dropin_set_derive_share(share: float) -> None:
+    """gb_dropin_set_derive_share: the share of in-edges whose lists
+    gb_run_scc derives on the device from the out-CSR (1: in_array is not
+    read; 0: it is copied whole)."""
+    _check(_lib.gb_dropin_set_derive_share(float(share)), "gb_dropin_set_derive_share")
 
 
 def run_cc_ref(n: int, out_array, out_degree_list, max_deg_vert: int = -1,
@@ -748,5 +749,5 @@ __all__ = [
     "Context", "Graph", "GBError", "Opts", "Stats", "opts", "read_edge", "output_labels",
     "scc_verify", "cc_verify", "canonicalize", "rmat_edges", "grid_edges", "batch_sizes",
     "csr_from_edges", "run_scc_ref", "run_cc_ref", "LIB_PATH", "Batch", "rmat_edges_n",
-    "dropin_set_copy_in",
+    "dropin_set_derive_share",
 ]

@@ -437,7 +437,9 @@ using gb::validate_csr;
 std::mutex g_default_mu;
 gb_ctx* g_default_ctx = nullptr;
 gb_graph* g_stage = nullptr;     // reused device buffers of the drop-ins
-std::atomic<int> g_dropin_copy_in{0};  // gb_run_scc: 1 = copy in_array, 0 = derive
+// gb_run_scc: share of the in-edges whose lists are derived on the device
+// (the rest of in_array is copied beside the derivation)
+std::atomic<double> g_dropin_share{0.8};
 int64_t g_stage_m = -1;
 int32_t g_stage_n = -1;
 
@@ -541,6 +543,12 @@ gb_status gb_ctx_destroy(gb_ctx* c) {
   for (auto& set : c->ev)
     for (auto& e : set)
       if (e) cudaEventDestroy(e);
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  for (auto& e : c->side_ev)
+    if (e) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return GB_OK;
@@ -739,19 +747,62 @@ static const void* pinned_view(const void* p) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// Whether the host can read p (pageable, pinned or managed memory).
+static bool host_readable(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;  // not known to the runtime: ordinary host memory
+  }
+  return a.type != cudaMemoryTypeDevice;
+}
+
+// The side stream and its events, created at first use.
+static gb_status side_stream(gb_ctx* c) {
+  if (c->side) return GB_OK;
+  CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "side stream");
+  CK(cudaEventCreateWithFlags(&c->side_ev[0], cudaEventDisableTiming), "side event");
+  CK(cudaEventCreateWithFlags(&c->side_ev[1], cudaEventDisableTiming), "side event");
+  return GB_OK;
+}
+
 // Fills g (whose buffers hold at least n / m) from the reference's CSR layout.
 // Pinned host arrays are read by the ingest kernels directly (one crossing
 // of the host link, checked on the way); other memory is copied first.
-// derive_in (directed graphs, m < 2^31): in_array is not read; the in-lists
-// are written on the device from the out-CSR and checked against idl.
+// derive_share (directed graphs, m < 2^31): the in-lists holding the first
+// derive_share of the in-edges (targets below the split vertex) are written
+// on the device from the out-CSR while it is read, and the rest of in_array
+// is copied beside it (a DMA on the side stream for pinned memory), so the
+// device's placement and the host link share the work; 0 copies in_array
+// whole, 1 (or in_array NULL) does not read it.  The derived lists are
+// checked against idl.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
                             const uint32_t* odl, const int32_t* in_array, const uint32_t* idl,
-                            bool derive_in) {
-  derive_in = derive_in && !g->symmetric;
+                            double derive_share) {
+  bool derive_in = !g->symmetric && m < (1u << 31) && (derive_share > 0.0 || !in_array);
+  // the split is chosen on the host from idl: arrays in device memory are
+  // derived whole
+  if (!in_array || !host_readable(idl)) derive_share = 1.0;
+  // split vertex: the first whose in-offset reaches the derived share
+  int32_t t_split = n;
+  int64_t e_split = m;
+  if (derive_in && derive_share < 1.0 && n > 0 && m > 0) {
+    const double goal = derive_share * (double)m;
+    int32_t lo = 0, hi = n;
+    while (lo < hi) {
+      const int32_t mid = lo + (hi - lo) / 2;
+      if ((double)idl[mid] >= goal) hi = mid;
+      else lo = mid + 1;
+    }
+    t_split = lo;
+    e_split = (int64_t)idl[lo] <= (int64_t)m ? (int64_t)idl[lo] : (int64_t)m;
+  }
   const void* vo = pinned_view(odl);
   const void* va = m > 0 ? pinned_view(out_array) : odl;
   const void* vi = g->symmetric ? odl : pinned_view(idl);
-  const void* vb = g->symmetric || m == 0 || derive_in ? odl : pinned_view(in_array);
+  const void* vb = g->symmetric || m == 0 || (derive_in && e_split >= (int64_t)m) ? odl
+                                                                                  : pinned_view(in_array);
   uint32_t* tmp = nullptr;
   if (!(vo && va && vi && vb)) {
     if (!derive_in) {
@@ -774,6 +825,8 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
     gb_status s = upload(c, tmp, odl, (size_t)(n + 1) * 4);
     if (s == GB_OK) s = upload(c, tmp + n + 1, idl, (size_t)(n + 1) * 4);
     if (s == GB_OK) s = upload(c, g->out_adj, out_array, (size_t)m * 4);
+    if (s == GB_OK && e_split < (int64_t)m)
+      s = upload(c, g->in_adj + e_split, in_array + e_split, (size_t)((int64_t)m - e_split) * 4);
     if (s != GB_OK) {
       cudaFreeAsync(tmp, c->stream);
       return s;
@@ -782,13 +835,30 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
     vi = tmp + n + 1;
     va = g->out_adj;
   }
+  const bool side_copy = tmp == nullptr && derive_in && e_split < (int64_t)m;
+  if (side_copy) {
+    // the copied in-lists go over the link beside the derivation
+    gb_status s = side_stream(c);
+    if (s != GB_OK) return s;
+    CK(cudaEventRecord(c->side_ev[0], c->stream), "side event");
+    CK(cudaStreamWaitEvent(c->side, c->side_ev[0], 0), "side wait");
+    CK(cudaMemcpyAsync(g->in_adj + e_split, in_array + e_split,
+                       (size_t)((int64_t)m - e_split) * 4, cudaMemcpyDefault, c->side),
+       "in-list copy");
+    CK(cudaEventRecord(c->side_ev[1], c->side), "side event");
+  }
   int* d_bad = nullptr;
   cudaError_t e = cudaMallocAsync(&d_bad, sizeof(int), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
   if (e == cudaSuccess && derive_in)
     e = gb::ingest_csr32_derive_in(n, m, (const uint32_t*)vo, (const int32_t*)va,
                                    (const uint32_t*)vi, g->out_off, g->out_adj, g->in_off,
-                                   g->in_adj, d_bad, c->stream);
+                                   g->in_adj, t_split, d_bad, c->stream);
+  if (e == cudaSuccess && derive_in && e_split < (int64_t)m) {
+    if (side_copy) e = cudaStreamWaitEvent(c->stream, c->side_ev[1], 0);
+    if (e == cudaSuccess)
+      e = gb::check_ids_flag(n, g->in_adj + e_split, (int64_t)m - e_split, d_bad, c->stream);
+  }
   if (e == cudaSuccess && !derive_in)
     e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
                          d_bad, c->stream);
@@ -799,6 +869,8 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  // (on a failure above, the side copy may still be writing the graph)
+  if (side_copy) cudaStreamSynchronize(c->side);
   if (d_bad) cudaFreeAsync(d_bad, c->stream);
   if (tmp) cudaFreeAsync(tmp, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "ingest");
@@ -832,7 +904,7 @@ gb_status gb_graph_from_csr32(gb_ctx* c, int32_t n, uint32_t m, const int32_t* o
   g->m = m;
   g->symmetric = idl == nullptr;
   gb_status s = graph_alloc(g, !g->symmetric);
-  if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl, derive);
+  if (s == GB_OK) s = fill_csr32(c, g, n, m, out_array, odl, in_array, idl, derive ? 1.0 : 0.0);
   if (s == GB_OK) s = graph_hints(c, g);
   if (s != GB_OK) {
     graph_free(g);
@@ -1125,9 +1197,9 @@ static gb_status stage_graph(gb_ctx* c, int32_t n, int64_t m, bool symmetric, gb
   return GB_OK;
 }
 
-gb_status gb_dropin_set_copy_in(int32_t copy) {
-  if (copy != 0 && copy != 1) return GB_ERR_INVALID;
-  g_dropin_copy_in.store(copy);
+gb_status gb_dropin_set_derive_share(double share) {
+  if (!(share >= 0.0 && share <= 1.0)) return GB_ERR_INVALID;
+  g_dropin_share.store(share);
   return GB_OK;
 }
 
@@ -1135,7 +1207,8 @@ gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_arra
                      const unsigned* out_degree_list, const unsigned* in_degree_list, int* scc_maps,
                      int max_deg_vert, double avg_degree, int vert_cutoff) {
   (void)avg_degree;
-  const bool derive = g_dropin_copy_in.load() == 0 && m < (1u << 31);
+  const double share = g_dropin_share.load();
+  const bool derive = (share > 0.0 || !in_array) && m < (1u << 31);
   if (n < 0 || !out_degree_list || !in_degree_list || (m > 0 && (!out_array || (!derive && !in_array))) ||
       (n > 0 && !scc_maps))
     return GB_ERR_INVALID;
@@ -1145,7 +1218,8 @@ gb_status gb_run_scc(int n, unsigned m, const int* out_array, const int* in_arra
   if (s != GB_OK) return s;
   gb_graph* g;
   if ((s = stage_graph(c, n, m, false, &g)) != GB_OK) return s;
-  s = fill_csr32(c, g, n, m, out_array, out_degree_list, in_array, in_degree_list, derive);
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, in_array, in_degree_list,
+                 derive ? share : 0.0);
   if (s != GB_OK) return s;
   gb_opts o;
   gb_opts_default(&o);
@@ -1164,7 +1238,7 @@ gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out
   if (s != GB_OK) return s;
   gb_graph* g;
   if ((s = stage_graph(c, n, m, true, &g)) != GB_OK) return s;
-  s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr, false);
+  s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr, 0.0);
   if (s != GB_OK) return s;
   gb_opts o;
   gb_opts_default(&o);

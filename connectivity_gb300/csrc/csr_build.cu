@@ -151,6 +151,16 @@ __global__ void k_check_csr(int32_t n, int64_t m, const int64_t* off, const int3
   }
 }
 
+// Every id of adj[0, count) in [0, n).
+__global__ void k_check_adj_ids(const int32_t* __restrict__ adj, int64_t count, int32_t n,
+                                int* bad) {
+  bool ok = true;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    ok = ok && (uint32_t)adj[e] < (uint32_t)n;
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
 // Ingest of the reference's 32-bit CSR from host memory the device reads
 // directly (pinned): offsets are widened to int64 and checked (off[0] == 0,
 // off[n] == m, non-decreasing), ids are checked against [0, n), in the same
@@ -295,7 +305,7 @@ __global__ void __launch_bounds__(kPT) k_place_in(
     const int32_t* __restrict__ src_adj, int32_t* __restrict__ out_adj, int64_t m, int32_t n,
     const int64_t* __restrict__ out_off, const uint32_t* __restrict__ hub_bits,
     uint32_t* __restrict__ cursor, const int32_t* __restrict__ tile_src,
-    int32_t* __restrict__ in_adj, int* bad) {
+    int32_t* __restrict__ in_adj, int32_t t_split, int* bad) {
   __shared__ int32_t head[kTile];
   __shared__ int32_t hkey[kHash];
   __shared__ uint32_t hval[kHash];  // a target's edge count in the tile, then its first slot
@@ -336,8 +346,8 @@ __global__ void __launch_bounds__(kPT) k_place_in(
       }
       if (store) {
         int4* d4 = reinterpret_cast<int4*>(out_adj + e0);
-        d4[tid] = q0;
-        d4[kPT + tid] = q1;
+        __stcs(d4 + tid, q0);
+        __stcs(d4 + kPT + tid, q1);
       }
       w[0] = q0.x; w[1] = q0.y; w[2] = q0.z; w[3] = q0.w;
       w[4] = q1.x; w[5] = q1.y; w[6] = q1.z; w[7] = q1.w;
@@ -402,8 +412,9 @@ __global__ void __launch_bounds__(kPT) k_place_in(
 #pragma unroll
     for (int k = 0; k < kPE; ++k) {
       const int p = tile_pos(k);
-      const bool in = p < len && (uint32_t)w[k] < (uint32_t)n;
-      if (p < len && !in) ok = false;
+      const bool id_ok = p < len && (uint32_t)w[k] < (uint32_t)n;
+      if (p < len && !id_ok) ok = false;
+      const bool in = id_ok && w[k] < t_split;  // targets from t_split on are copied
       us[k] = in ? head[p] : -1;
       if (in && us[k] < 0) ok = false;
       info[k] = in ? __ldg(hub_bits + (w[k] >> 5)) : 0u;
@@ -429,7 +440,7 @@ __global__ void __launch_bounds__(kPT) k_place_in(
       slot[k] = (us[k] >= 0 && info[k] == kNoSlot) ? atomicAdd(&cursor[w[k]], 1u) : kNoSlot;
 #pragma unroll
     for (int k = 0; k < kPE; ++k)
-      if (slot[k] < slot_cap) in_adj[slot[k]] = us[k];
+      if (slot[k] < slot_cap) __stcs(in_adj + slot[k], us[k]);
     __syncthreads();
     for (int h = tid; h < kHash; h += kPT) {
       const uint32_t c = hval[h];
@@ -442,7 +453,7 @@ __global__ void __launch_bounds__(kPT) k_place_in(
     for (int k = 0; k < kPE; ++k) {
       if (info[k] == kNoSlot) continue;
       const uint32_t b = hval[info[k] >> 16];
-      if (b != kNoSlot) in_adj[b + (info[k] & 0xffffu)] = us[k];
+      if (b != kNoSlot) __stcs(in_adj + b + (info[k] & 0xffffu), us[k]);
     }
     __syncthreads();
   }
@@ -699,6 +710,13 @@ cudaError_t check_csr(int32_t n, int64_t m, const int64_t* off, const int32_t* a
   return cudaStreamSynchronize(s);
 }
 
+cudaError_t check_ids_flag(int32_t n, const int32_t* adj, int64_t count, int* d_bad,
+                           cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_check_adj_ids<<<grid_for(count), 256, 0, s>>>(adj, count, n, d_bad);
+  return cudaGetLastError();
+}
+
 cudaError_t check_csr_flag(int32_t n, int64_t m, const int64_t* off, const int32_t* adj,
                            int* d_bad, cudaStream_t s) {
   k_check_csr<<<grid_for((m > n ? m : n) + 1), 256, 0, s>>>(n, m, off, adj, d_bad);
@@ -717,8 +735,9 @@ cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int3
 cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_off,
                                    const int32_t* h_out_adj, const uint32_t* h_in_off,
                                    int64_t* out_off, int32_t* out_adj, int64_t* in_off,
-                                   int32_t* in_adj, int* d_bad, cudaStream_t s) {
-  if (m >= (1ll << 31)) return cudaErrorInvalidValue;
+                                   int32_t* in_adj, int32_t t_split, int* d_bad,
+                                   cudaStream_t s) {
+  if (m >= (1ll << 31) || t_split < 0 || t_split > n) return cudaErrorInvalidValue;
   k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_out_off, out_off, n, m, d_bad);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -752,11 +771,11 @@ cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_o
     }
     const int g = (int)(tiles < blocks[dev] ? tiles : blocks[dev]);
     k_place_in<<<g, kPT, 0, s>>>(h_out_adj, out_adj, m, n, out_off, hub_bits, cursor, tile_src,
-                                 in_adj, d_bad);
+                                 in_adj, t_split, d_bad);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess && n > 0) {
-    k_check_cursors<<<grid_for(n), 256, 0, s>>>(n, in_off, cursor, d_bad);
+  if (e == cudaSuccess && t_split > 0) {
+    k_check_cursors<<<grid_for(t_split), 256, 0, s>>>(t_split, in_off, cursor, d_bad);
     e = cudaGetLastError();
   }
   cudaFreeAsync(tmp, s);

@@ -265,15 +265,20 @@ cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaS
 // an int64-offset device CSR, checked on the way (*d_bad |= 1 on a bad CSR).
 cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
                          int64_t* off, int32_t* adj, int* d_bad, cudaStream_t s);
-// The same for a directed graph given its out-CSR and its in-offsets only:
-// the in-lists are written on the device while the out-lists are read (the
-// order within an in-list is then not the input's).  *d_bad |= 1 on a bad
-// CSR or in-offsets that are not the out-CSR's transpose's.  The adjacency
-// may be read from out_adj itself (already on the device).  m < 2^31.
+// The same for a directed graph given its out-CSR and its in-offsets: the
+// in-lists of the targets below t_split are written on the device while the
+// out-lists are read (their order within a list is then not the input's);
+// the in-lists from t_split on are left to the caller (copied).  *d_bad |= 1
+// on a bad CSR or in-offsets that are not those of the out-CSR's transpose
+// (below t_split).  The adjacency may be read from out_adj itself (already
+// on the device).  m < 2^31, 0 <= t_split <= n.
 cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_off,
                                    const int32_t* h_out_adj, const uint32_t* h_in_off,
                                    int64_t* out_off, int32_t* out_adj, int64_t* in_off,
-                                   int32_t* in_adj, int* d_bad, cudaStream_t s);
+                                   int32_t* in_adj, int32_t t_split, int* d_bad, cudaStream_t s);
+// *d_bad |= 1 when an id of adj[0, count) is outside [0, n).  Does not wait.
+cudaError_t check_ids_flag(int32_t n, const int32_t* adj, int64_t count, int* d_bad,
+                           cudaStream_t s);
 // Batch labels: global ids -> ids local to each graph.
 cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
                             cudaStream_t s);

@@ -429,14 +429,17 @@ gb_status gb_server_stats_get(gb_server* server, gb_server_stats* stats);
 gb_status gb_server_destroy(gb_server* server);
 
 /* ---- reference-shaped drop-ins (host buffers, reference layout) ------- */
-/* How gb_run_scc gets the in-lists.  copy = 0 (default): in_array is not
- * read; the in-lists are derived on the device from the out-CSR and checked
- * against in_degree_list, as gb_graph_from_csr32 does with in_array NULL, so
- * half of the graph's bytes stay off the host link (in_array may be NULL).
- * copy = 1: in_array is copied as given.  Labels are the same either way
- * for an in-CSR that is the out-CSR's transpose, which is what create_csr
- * (scc_main.cpp:127-191) builds.  Graphs of m >= 2^31 always copy. */
-gb_status gb_dropin_set_copy_in(int32_t copy);
+/* How gb_run_scc gets the in-lists.  The in-CSR is the out-CSR transposed
+ * (create_csr, scc_main.cpp:127-191, builds both), so half of its lists can
+ * be written on the device from the out-lists while they are read, instead
+ * of crossing the host link.  share = the fraction of the in-edges (those of
+ * the lowest target ids) whose lists are derived so; the rest of in_array
+ * is copied beside the derivation.  1: in_array is not read (it may be
+ * NULL); 0: in_array is copied whole.  Default 0.8.  Derived lists are
+ * checked against in_degree_list (GB_ERR_INVALID when it is not the
+ * transpose's), and their order within a vertex is free; the labels are the
+ * same for every share.  Graphs of m >= 2^31 copy. */
+gb_status gb_dropin_set_derive_share(double share);
 /* run_scc(graph& g, int*& scc_maps, int max_deg_vert, double avg_degree,
  * int vert_cutoff), multistep/scc_main.cpp:210-211, with the graph struct's
  * fields passed one by one and scc_maps owned by the caller (n ints).  Uses

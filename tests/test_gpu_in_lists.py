@@ -1,6 +1,6 @@
 """In-lists derived on the device from the out-CSR (gb_graph_from_csr32 with
-in_array NULL, and gb_run_scc by default): only the out-CSR and the
-in-offsets are read, the in-lists are written while the out-lists are read.
+in_array NULL, and gb_run_scc for a share of the in-edges): the in-lists are
+written while the out-lists are read, and the rest of in_array is copied.
 
 Checked: every derived in-list holds the same sources as the transpose
 (as a multiset, the order within a list is free), the labels equal the
@@ -121,26 +121,53 @@ def test_derived_in_lists_are_the_transpose(ctx, name, kind):
 
 
 @pytest.mark.parametrize("kind", ["pinned", "pageable"])
-def test_run_scc_reads_no_in_lists_by_default(kind):
-    """gb_run_scc derives the in-lists: garbage (or no array) in in_array
-    gives the oracle's labels; with copying on, in_array is used as given."""
+@pytest.mark.parametrize("share", [1.0, 0.75, 0.3, 0.0])
+def test_run_scc_split_between_derived_and_copied(kind, share):
+    """gb_run_scc derives the in-lists of the first `share` of the in-edges
+    and copies the rest of in_array: the oracle's labels at every share; at
+    share 1 in_array is not read (garbage or NULL), and NULL in_array always
+    means derive everything."""
     pin = _pinner(kind)
-    for n, s, d in (graphs.rmat(13, 16, 31), _star_in(5000), _many_hubs(600, 2200)):
-        cg = oracle.CpuGraph(n, s, d)
-        odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
-        oa = pin(cg.out_adj)
-        want = oracle.scc(cg)
-        junk = pin(np.full(max(cg.m, 1), 7, np.int32))
-        assert np.array_equal(gb.run_scc_ref(n, oa, junk, odl, idl), want)
-        assert np.array_equal(gb.run_scc_ref(n, oa, None, odl, idl), want)
-        gb.dropin_set_copy_in(True)
-        try:
+    gb.dropin_set_derive_share(share)
+    try:
+        for n, s, d in (graphs.rmat(13, 16, 31), _star_in(5000), _many_hubs(600, 2200),
+                        _sparse_runs()):
+            cg = oracle.CpuGraph(n, s, d)
+            odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
+            oa = pin(cg.out_adj)
+            want = oracle.scc(cg)
             assert np.array_equal(gb.run_scc_ref(n, oa, pin(cg.in_adj), odl, idl), want)
-            with pytest.raises(gb.GBError) as e:
-                gb.run_scc_ref(n, oa, None, odl, idl)
-            assert e.value.status == gb.GB_ERR_INVALID
-        finally:
-            gb.dropin_set_copy_in(False)
+            assert np.array_equal(gb.run_scc_ref(n, oa, None, odl, idl), want)
+            if share == 1.0:
+                junk = pin(np.full(max(cg.m, 1), 7, np.int32))
+                assert np.array_equal(gb.run_scc_ref(n, oa, junk, odl, idl), want)
+    finally:
+        gb.dropin_set_derive_share(0.8)
+    with pytest.raises(gb.GBError) as e:
+        gb.dropin_set_derive_share(1.5)
+    assert e.value.status == gb.GB_ERR_INVALID
+
+
+@pytest.mark.parametrize("kind", ["pinned", "pageable"])
+def test_bad_id_in_the_copied_in_lists_is_refused(kind):
+    """With a split, the copied part of in_array is checked for ids outside
+    [0, n)."""
+    pin = _pinner(kind)
+    n, s, d = graphs.rmat(12, 16, 8)
+    cg = oracle.CpuGraph(n, s, d)
+    odl, idl = pin(cg.out_off.astype(np.uint32)), pin(cg.in_off.astype(np.uint32))
+    oa = pin(cg.out_adj)
+    ia = pin(cg.in_adj.copy())
+    ia[-3] = n + 9  # in the copied tail at any share below 1
+    gb.dropin_set_derive_share(0.5)
+    try:
+        with pytest.raises(gb.GBError) as e:
+            gb.run_scc_ref(n, oa, ia, odl, idl)
+        assert e.value.status == gb.GB_ERR_INVALID
+        ia[-3] = cg.in_adj[-3]
+        assert np.array_equal(gb.run_scc_ref(n, oa, ia, odl, idl), oracle.scc(cg))
+    finally:
+        gb.dropin_set_derive_share(0.8)
 
 
 @pytest.mark.parametrize("kind", ["pinned", "pageable"])
