@@ -497,22 +497,35 @@ __global__ void k_latch(const Ctl* c, int* sticky) {
   }
 }
 
-__global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t* in_off,
-                               int32_t* deg) {
+// Degree key of the hint rule: the total degree itself below 32, above it
+// eight steps per power of two (the exponent and the next three bits), so
+// that every key fits a byte and the key array (n bytes) stays in the L2
+// while the adjacency streams past it.  Non-decreasing in the degree.
+__device__ __forceinline__ uint8_t degree_key(long long d) {
+  if (d < 32) return (uint8_t)(d < 0 ? 0 : d);
+  int e = 63 - __clzll((unsigned long long)d);
+  if (e > 30) e = 30;
+  const long long dd = d < (1ll << 31) ? d : (1ll << 31) - 1;
+  return (uint8_t)(32 + 8 * (e - 5) + (int)((dd >> (e - 3)) & 7));
+}
+
+__global__ void k_degree_key(int32_t n, const int64_t* out_off, const int64_t* in_off,
+                             uint8_t* key) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     long long d = out_off[v + 1] - out_off[v];
     if (in_off) d += in_off[v + 1] - in_off[v];
-    deg[v] = (int32_t)(d < 0x7fffffffll ? d : 0x7fffffffll);
+    key[v] = degree_key(d);
   }
 }
 
-// The pull hint of a vertex: its neighbour of largest total degree, the
-// first one in adjacency order on ties (-1 without neighbours).  Vertices
+// The pull hint of a vertex: its neighbour of largest degree key, the first
+// one in adjacency order on ties (-1 without neighbours).  Vertices
 // are taken in three tiers by degree, each spread evenly over the grid:
 //   <= kHintThread neighbours: one thread, four loads in flight at a time
 //      (most vertices of a power-law graph);
-//   <= kHintWarp: appended to `mid`, then a warp per vertex in k_hint_mid,
+//   <= kHintWarp: appended to `mid`, then a warp per vertex in k_hint_mid
+//      (four loads in flight per lane),
 //      warps taking the list's vertices in turn;
 //   more: appended to `heavy`, then a block per vertex in k_hint_heavy.
 // Walking the middle tier inside the pass that finds it (a warp over the
@@ -522,6 +535,7 @@ __global__ void k_total_degree(int32_t n, const int64_t* out_off, const int64_t*
 constexpr int kHintThread = 32;
 constexpr int kHintWarp = 2048;
 constexpr int kHintBlock = 256;
+constexpr int kHintWU = 4;  // loads in flight per lane, warp and block tiers
 
 __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& best_d,
                                             int64_t& best_e) {
@@ -532,7 +546,7 @@ __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& bes
 }
 
 __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* off,
-                                                     const int32_t* adj, const int32_t* deg,
+                                                     const int32_t* adj, const uint8_t* deg,
                                                      int32_t* hint, int32_t* mid,
                                                      int32_t* nmid, int32_t* heavy,
                                                      int32_t* nheavy) {
@@ -552,9 +566,9 @@ __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* o
         const int32_t a2 = e + 2 < d ? adj[s + e + 2] : -1;
         const int32_t a3 = e + 3 < d ? adj[s + e + 3] : -1;
         const int32_t d0 = deg[a0];
-        const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
-        const int32_t d2 = a2 >= 0 ? deg[a2] : -1;
-        const int32_t d3 = a3 >= 0 ? deg[a3] : -1;
+        const int32_t d1 = a1 >= 0 ? (int32_t)deg[a1] : -1;
+        const int32_t d2 = a2 >= 0 ? (int32_t)deg[a2] : -1;
+        const int32_t d3 = a3 >= 0 ? (int32_t)deg[a3] : -1;
         if (d0 > best_d) { best_d = d0; best_e = e; }
         if (d1 > best_d) { best_d = d1; best_e = e + 1; }
         if (d2 > best_d) { best_d = d2; best_e = e + 2; }
@@ -567,7 +581,7 @@ __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* o
 
 // A warp per middle-tier vertex, the list spread over every warp.
 __global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, const int32_t* adj,
-                                                         const int32_t* deg, int32_t* hint,
+                                                         const uint8_t* deg, int32_t* hint,
                                                          const int32_t* mid,
                                                          const int32_t* nmid) {
   const int lane = threadIdx.x & 31;
@@ -578,13 +592,15 @@ __global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, con
     const int64_t s = off[v], d = off[v + 1] - s;
     int32_t best_d = -1;
     int64_t best_e = -1;
-    for (int64_t e = lane; e < d; e += 64) {
-      const int32_t a0 = adj[s + e];
-      const int32_t a1 = e + 32 < d ? adj[s + e + 32] : -1;
-      const int32_t d0 = deg[a0];
-      const int32_t d1 = a1 >= 0 ? deg[a1] : -1;
-      if (d0 > best_d) { best_d = d0; best_e = e; }
-      if (d1 > best_d) { best_d = d1; best_e = e + 32; }
+    for (int64_t e = lane; e < d; e += 32 * kHintWU) {
+      int32_t a[kHintWU], k[kHintWU];
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q) a[q] = e + 32 * q < d ? adj[s + e + 32 * q] : -1;
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q)
+        if (k[q] > best_d) { best_d = k[q]; best_e = e + 32 * q; }
     }
     for (int o = 16; o; o >>= 1) {
       const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
@@ -596,7 +612,7 @@ __global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, con
 }
 
 // A block per heavy vertex (more than kHintWarp neighbours).
-__global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const int32_t* deg,
+__global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const uint8_t* deg,
                              int32_t* hint, const int32_t* heavy, const int32_t* nheavy) {
   __shared__ int32_t sd[32];
   __shared__ int64_t se[32];
@@ -607,9 +623,16 @@ __global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const int32
     const int64_t s = off[v], d = off[v + 1] - s;
     int32_t best_d = -1;
     int64_t best_e = -1;
-    for (int64_t e = threadIdx.x; e < d; e += blockDim.x) {
-      const int32_t dd = deg[adj[s + e]];
-      if (dd > best_d) { best_d = dd; best_e = e; }
+    const int64_t T = blockDim.x;
+    for (int64_t e = threadIdx.x; e < d; e += T * kHintWU) {
+      int32_t a[kHintWU], k[kHintWU];
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q) a[q] = e + T * q < d ? adj[s + e + T * q] : -1;
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
+#pragma unroll
+      for (int q = 0; q < kHintWU; ++q)
+        if (k[q] > best_d) { best_d = k[q]; best_e = e + T * q; }
     }
     for (int o = 16; o; o >>= 1) {
       const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
@@ -923,16 +946,16 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  // scratch: total degrees (n), the middle and heavy lists (n each) and
-  // their counts, one pair per side
-  int32_t* deg = nullptr;
-  cudaError_t e = cudaMallocAsync(&deg, ((size_t)n * 3 + 4) * 4, s);
+  // scratch: the middle and heavy lists (n each) and their counts, one pair
+  // per side, then the degree keys (n bytes)
+  int32_t* mid = nullptr;
+  cudaError_t e = cudaMallocAsync(&mid, ((size_t)n * 2 + 4) * 4 + (size_t)n, s);
   if (e != cudaSuccess) return e;
-  int32_t* mid = deg + n;
   int32_t* heavy = mid + n;
   int32_t* cnt = heavy + n;  // [0] mid out, [1] heavy out, [2] mid in, [3] heavy in
+  uint8_t* deg = reinterpret_cast<uint8_t*>(cnt + 4);
   cudaMemsetAsync(cnt, 0, 16, s);
-  k_total_degree<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
+  k_degree_key<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
   const int g = grid_for(n);
   const int gw = 152 * 8;  // 8 blocks of 8 warps per SM for the list passes
   for (int side = 0; side < 2; ++side) {
@@ -947,7 +970,7 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
     k_hint_mid<<<gw, kHintBlock, 0, s>>>(off, adj, deg, hint, mid, cnt + 2 * side);
     k_hint_heavy<<<152 * 2, 1024, 0, s>>>(off, adj, deg, hint, heavy, cnt + 2 * side + 1);
   }
-  cudaFreeAsync(deg, s);
+  cudaFreeAsync(mid, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return cudaStreamSynchronize(s);

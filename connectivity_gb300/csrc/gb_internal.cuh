@@ -26,7 +26,7 @@ enum : int {
 struct Csr {
   const int64_t* off;   // n + 1 offsets
   const int32_t* adj;   // neighbour ids
-  const int32_t* hint;  // per vertex, the neighbour of largest total degree
+  const int32_t* hint;  // per vertex, the neighbour of largest degree key
                         // (-1: none), or null
 };
 
@@ -282,7 +282,8 @@ cudaError_t check_ids_flag(int32_t n, const int32_t* adj, int64_t count, int* d_
 // Batch labels: global ids -> ids local to each graph.
 cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, const int64_t* vbase,
                             cudaStream_t s);
-// Pull hints: for every vertex, its neighbour of largest total degree in
+// Pull hints: for every vertex, its neighbour of largest degree key (the
+// total degree, above 32 rounded down to eight steps per power of two) in
 // each CSR (hint_in may be null when in_off is).  Synchronises the stream.
 cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,

@@ -258,7 +258,8 @@ gb_status gb_graph_pivot(gb_ctx* ctx, const gb_graph* g, int32_t kind, int32_t* 
                          double* avg_degree);
 gb_status gb_graph_destroy(gb_graph* g);
 /* Pull hints: per vertex and direction, the neighbour of largest total
- * degree (first in adjacency order on ties), an index derived from the CSR
+ * degree, counted exactly below 32 and above it in eight steps per power of
+ * two (first in adjacency order on ties), an index derived from the CSR
  * that lets a pull step settle most candidates with one lookup.  Every
  * gb_graph_from_* / gb_graph_rmat* call builds them (n int32 per direction);
  * on = 0 frees them and runs then scan in-edges only, on = 1 (re)builds

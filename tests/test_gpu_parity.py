@@ -423,9 +423,22 @@ def test_balanced_push_same_work(ctx, kind):
     assert st_b.pull_steps == 0 and st_t.pull_steps == 0
 
 
+def _degree_key(deg):
+    """The hint rule's degree key: the total degree below 32, above it eight
+    steps per power of two (exponent and the next three bits)."""
+    deg = np.asarray(deg, np.int64)
+    key = deg.copy()
+    big = deg >= 32
+    e = np.frexp(deg[big].astype(np.float64))[1].astype(np.int64) - 1
+    e = np.minimum(e, 30)
+    key[big] = 32 + 8 * (e - 5) + ((np.minimum(deg[big], (1 << 31) - 1) >> (e - 3)) & 7)
+    return key
+
+
 def _hints_want(n, off, adj, deg):
-    """The hint rule restated: the neighbour of largest total degree, the
-    first in adjacency order on ties, -1 without neighbours."""
+    """The hint rule restated: the neighbour of largest degree key (see
+    _degree_key), the first in adjacency order on ties, -1 without
+    neighbours."""
     want = np.full(n, -1, np.int64)
     d = np.diff(off)
     nz = np.flatnonzero(d > 0)
@@ -456,7 +469,7 @@ def test_pull_hints_follow_the_rule(ctx, case):
         n, s, d = [c for c in graphs.edge_cases() if c[0] == "star"][0][1:]
     g = gb.Graph.from_edges(ctx, n, s, d)
     oo, oa, io, ia = g.to_host()
-    deg = np.minimum(np.diff(oo) + np.diff(io), 0x7fffffff)
+    deg = _degree_key(np.diff(oo) + np.diff(io))
     ho, hi = g.hints()
     assert np.array_equal(ho, _hints_want(n, oo, oa, deg))
     assert np.array_equal(hi, _hints_want(n, io, ia, deg))
