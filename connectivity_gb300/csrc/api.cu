@@ -112,6 +112,7 @@ void fill_params(const gb_opts* o, gb::RunParams& p) {
   p.tune.beta = o->beta > 0 ? o->beta : 25.0f;
   p.tune.max_steps = o->max_steps > 0 ? o->max_steps : (1 << 30);
   p.tune.expand_mode = o->expand_mode == 1 ? 1 : 0;
+  p.colour_mode = o->colour_mode == 1 || o->colour_mode == 2 ? o->colour_mode : 0;
 }
 
 }  // namespace
@@ -471,6 +472,7 @@ void gb_opts_default(gb_opts* o) {
   o->fwbw_rounds = 1;
   o->expand_mode = 0;
   o->small_path = 1;
+  o->colour_mode = 2;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {

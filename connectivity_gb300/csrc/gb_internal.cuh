@@ -191,6 +191,8 @@ struct RunParams {
   int32_t canonical;      // 1: relabel with the minimum member id
   int32_t pivot_hint;     // >= 0: use as FW-BW source if still valid
   int32_t count_unassigned;  // 1: a final pass counts labels outside [0, n)
+  int32_t colour_mode;    // SCC: 0 colour rounds, 1 signature rounds, 2 the
+                          // signature rounds from kSigMin residual vertices
   Tune tune;
 };
 

@@ -1027,6 +1027,42 @@ struct MarkVisit {
   __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
 };
 
+// Signature propagation (colour_mode 1): the visited vertex's value (the
+// smallest id reaching it, or reached from it) is lowered along an edge that
+// stays inside its class (both ends carried the same value pair in the
+// previous round).  The source value is the vertex itself: its value and
+// class are read here.
+struct SigVisit {
+  static constexpr bool kWeighted = false;
+  static constexpr bool kLocal = true;
+  const uint32_t* valid;
+  int32_t* val;
+  const int32_t* cls;
+  __device__ __forceinline__ bool local() const { return true; }
+  __device__ __forceinline__ int32_t source(int32_t v) const { return v; }
+  __device__ __forceinline__ void edges(const int32_t (&sv)[kEU], const int32_t (&w)[kEU],
+                                        const int (&)[kEU], const bool (&act)[kEU],
+                                        bool (&out)[kEU]) const {
+    bool p[kEU];
+    int32_t cv[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) {
+      p[q] = act[q] && bit_get(valid, w[q]);
+      cv[q] = 0;
+      if (p[q]) {
+        cv[q] = __ldcg(val + sv[q]);
+        p[q] = __ldcg(cls + sv[q]) == __ldcg(cls + w[q]) && __ldcg(val + w[q]) > cv[q];
+      }
+    }
+    int32_t m[kEU];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) m[q] = p[q] ? atomicMin(val + w[q], cv[q]) : cv[q];
+#pragma unroll
+    for (int q = 0; q < kEU; ++q) out[q] = p[q] && m[q] > cv[q];
+  }
+  __device__ __forceinline__ unsigned long long weight(int32_t) const { return 0ull; }
+};
+
 // Fixed-point trim: removing r takes one edge from each neighbour's live
 // count (out-edge r->w: w loses an in-edge; in-edge u->r: u loses an
 // out-edge).  A valid vertex whose count reaches zero is removed and labelled
@@ -2536,6 +2572,126 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   steps_close(c, st);
 }
 
+// ------------------------------------------------------------------------
+// Signature rounds (colour_mode 1, or 2 on a large residual; SCC): each round,
+// every valid vertex v gets fw[v], the smallest id that reaches it, and
+// bw[v], the smallest id it reaches, both through edges inside its class
+// (the vertices that carried the same (fw, bw) pair in the previous round;
+// one class in the first round).  Members of one SCC share a class and a
+// pair; a vertex whose two values agree reaches and is reached by that id,
+// so it is in that vertex's SCC, whose smallest member it is: the label.
+// The other vertices take their pair as their class (a 32-bit mix of it;
+// a collision only merges classes), and no edge between classes is
+// followed again.  Every class loses its smallest vertex's SCC each round,
+// as a colour round does, but the classes split the residual into pieces
+// whose propagations are short, and no backward marking search is needed.
+// The labels are the colour rounds' (the minimum member of each SCC).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int32_t sig_class(int32_t f, int32_t b) {
+  uint32_t x = (uint32_t)f * 0x9E3779B1u;
+  x ^= (uint32_t)b * 0x85EBCA77u + 0x7F4A7C15u + (x << 6) + (x >> 2);
+  return (int32_t)x;
+}
+
+// Residual (valid vertices after FW-BW) from which colour_mode 2 takes the
+// signature rounds.
+constexpr int32_t kSigMin = 65536;
+
+// (not inlined: its registers are allocated apart from the default run's
+// hot loops)
+__device__ __noinline__ void signature_rounds(const Args& A, Smem& sm) {
+  Work w = A.w;
+  Ctl* c = w.ctl;
+  const GraphView& g = A.g;
+  const int G = gridDim.x, b = blockIdx.x, T = blockDim.x, t = threadIdx.x;
+  const long long gt = (long long)b * T + t, gstride = (long long)G * T;
+  Tally ty;
+  if (ld_vol(&c->err)) return;
+  int32_t nl = __ldcg(&c->nvalid);
+  if (nl == 0) return;
+  Steps st = steps_open(c);
+  int32_t* fw = w.colour;
+  int32_t* bw = w.live_in;
+  int32_t* cls = w.live_out;
+  const Adj outs = adj1(g.out), ins = adj1(g.in);
+  int32_t* L = w.listA;
+  int32_t* L2 = w.listB;
+  int rounds = 0;
+  long long labelled = 0;
+  int32_t* bufs[2] = {w.x0, w.x1};
+  int32_t* hl[2] = {w.h0, w.h1};
+  const Tune& tn = A.p.tune;
+  for (long long i = gt; i < nl; i += gstride) cls[__ldcg(L + i)] = 0;
+  while (nl > 0) {
+    if (rounds > g.n || st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 40); return; }
+    trace_rec(c, nl, 8);
+    for (long long i = gt; i < nl; i += gstride) {
+      const int32_t v = __ldcg(L + i);
+      fw[v] = v;
+      bw[v] = v;
+      ty.list++;
+    }
+    if (!step_sync(c, st, 41)) return;
+    // forward values along out-edges, then backward values along in-edges;
+    // the first step of each pushes from every vertex of L
+    for (int dir = 0; dir < 2; ++dir) {
+      const SigVisit sv{w.vbits, dir == 0 ? fw : bw, cls};
+      const Adj& a = dir == 0 ? outs : ins;
+      const int32_t* front = L;
+      int32_t nfront = nl, nheavy = 0;
+      int cur = 0, hs = 0;
+      for (;;) {
+        if (st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 42); return; }
+        trace_rec(c, nfront, 9);
+        const Sink sk = sink_make(bufs[cur], 0, w.n, step_out(c, st.s), false, nullptr,
+                                  hl[hs ^ 1], w.n, 305);
+        expand<1>(front, nfront, hl[hs], nheavy, a, sv, sk, tn, sm, c, ty);
+        stat_inc(c, kStColourSteps);
+        if (!step_sync(c, st, 43)) return;
+        const StepIn in = step_read(c, st.s);
+        if (in.count == 0 && in.huge == 0) break;
+        front = bufs[cur];
+        nfront = in.count;
+        nheavy = in.huge;
+        cur ^= 1;
+        hs ^= 1;
+      }
+    }
+    // a vertex whose two values agree is labelled; the others are reclassed
+    trace_rec(c, nl, 10);
+    for (long long i = gt; i < nl; i += gstride) {
+      const int32_t v = __ldcg(L + i);
+      const int32_t f = __ldcg(fw + v), bk = __ldcg(bw + v);
+      if (f == bk) {
+        w.label[v] = f;
+        bit_claim(w.done, v);
+      } else {
+        cls[v] = sig_class(f, bk);
+      }
+    }
+    if (!step_sync(c, st, 44)) return;
+    trace_rec(c, nl, 12);
+    auto release = [&](int32_t v) { bit_release(w.vbits, v); };
+    if (!compact_ordered(L, nl, L2, w.done, w, sm, st, 45, &c->nvalid, ty, release)) return;
+    if (!step_sync(c, st, 46)) return;
+    const int32_t nn = __ldcg(&c->nvalid);
+    labelled += nl - nn;
+    nl = nn;
+    int32_t* tmp = L;
+    L = L2;
+    L2 = tmp;
+    ++rounds;
+    stat_inc(c, kStColourRounds);
+  }
+  if (b == 0 && t == 0) {
+    c->ncolour_rounds = rounds;
+    c->ncolour = (int32_t)labelled;
+  }
+  trace_rec(c, 0, 15);
+  tally_flush(ty, c, kKColour, A.p.count_unassigned != 0, sm.red_u);
+  steps_close(c, st);
+}
+
 // Device time at a phase boundary (block 0, thread 0), into the run's slot
 // of the context's phase-time ring.
 __device__ __forceinline__ void phase_mark(const Args& A, int i) {
@@ -2575,7 +2731,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_run(Args A) {
   }
   if (!grid_barrier(c, 901)) return;
   phase_mark(A, 2);
-  if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
+  // (every block reads the same count after the barrier, so all take the
+  // same branch)
+  const bool sig = A.kind == kSCC &&
+                   (A.p.colour_mode == 1 || (A.p.colour_mode == 2 && __ldcg(&c->nvalid) >= kSigMin));
+  if (sig) signature_rounds(A, sm);
+  else if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
   else colour_rounds<2>(A, sm);
   if (!grid_barrier(c, 902)) return;
   phase_mark(A, 3);

@@ -111,6 +111,15 @@ typedef struct gb_opts {
                           the graph fits; 0: never.  Needs canonical = 1;
                           the statistics then hold the times only.  No
                           reference counterpart. */
+  int32_t colour_mode; /* SCC after FW-BW: 0 the reference's colour rounds
+                          (scc_color.cpp:340-373); 1 signature rounds: every
+                          round propagates the smallest reaching id and the
+                          smallest reached id inside classes of vertices
+                          whose pair matched the round before, labels the
+                          vertices whose two ids agree, and never follows an
+                          edge between classes again; 2 (default) signature
+                          rounds when at least 65536 vertices are left after
+                          FW-BW, else colour rounds.  Same labels. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);

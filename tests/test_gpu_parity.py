@@ -36,6 +36,8 @@ VARIANTS = {
     "pull_early": {"alpha": 1e9, "beta": 1e-3, "k_pull": 1},
     "push_only": {"alpha": 1e-9},
     "small_grid": {"grid_blocks": 3},
+    "signature": {"colour_mode": 1},
+    "signature_trim2": {"colour_mode": 1, "trim_level": 2, "fwbw_rounds": 2},
 }
 
 
