@@ -33,7 +33,7 @@ namespace {
 
 struct Param {
   int which;  // 0 t_block, 1 t_grid, 2 k_pull, 3 alpha, 4 beta, 5 grid_blocks (fraction),
-              // 6 expand_mode, 7 small_path
+              // 6 expand_mode, 7 small_path, 8 colour_mode
   std::vector<double> values;
 };
 
@@ -47,6 +47,7 @@ void set_param(gb_opts& o, int which, double v, int grid) {
     case 5: o.grid_blocks = v >= 1.0 ? 0 : std::max(1, (int)(grid * v)); break;
     case 6: o.expand_mode = (int32_t)v; break;
     case 7: o.small_path = (int32_t)v; break;
+    case 8: o.colour_mode = (int32_t)v; break;
   }
 }
 
@@ -59,6 +60,7 @@ double get_param(const gb_opts& o, int which, int grid) {
     case 4: return o.beta;
     case 6: return o.expand_mode;
     case 7: return o.small_path;
+    case 8: return o.colour_mode;
     default: return o.grid_blocks <= 0 ? 1.0 : (double)o.grid_blocks / grid;
   }
 }
@@ -101,6 +103,7 @@ gb_status tune(gb_ctx* c, int reps, Run run, gb_opts* best, double* ms_out) {
       {4, {10, 25, 100}},
       {5, {0.5, 1.0}},
       {6, {0, 1}},
+      {8, {0, 1, 2}},  // colour rounds, signature rounds, by residual size
   };
   gb_opts cur;
   gb_opts_default(&cur);

@@ -26,7 +26,8 @@ from . import Batch, Context, Graph, Opts, opts
 CLASSES = [(1 << 10, 8), (1 << 12, 16), (1 << 14, 16), (1 << 16, 16), (1 << 18, 16),
            (1 << 20, 16), (1 << 22, 16), (1 << 24, 16)]
 
-TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode", "small_path")
+TUNED = ("t_block", "t_grid", "k_pull", "alpha", "beta", "grid_blocks", "expand_mode", "small_path",
+         "colour_mode")
 
 
 def opts_to_dict(o: Opts) -> dict:
