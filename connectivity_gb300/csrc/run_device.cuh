@@ -2438,8 +2438,10 @@ __device__ __forceinline__ void reach_phase(Args& A, Smem& sm) {
 // cc_color.cpp:47-175).  Colours are minima (see ColourVisit), so a root is
 // the smallest id of its SCC and every label is canonical.
 // ------------------------------------------------------------------------
+// Stops (before a round) after max_rounds rounds; *cur = the valid list
+// then (listA or listB).
 template <int NC>
-__device__ void colour_rounds(const Args& A, Smem& sm) {
+__device__ void colour_rounds(const Args& A, Smem& sm, int max_rounds, int32_t** cur) {
   Work w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -2461,7 +2463,9 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
   int32_t* bufs[2] = {w.x0, w.x1};
   int32_t* hl[2] = {w.h0, w.h1};
   const Tune& tn = A.p.tune;
+  *cur = L;
   while (nl > 0) {
+    if (rounds >= max_rounds) break;
     if (rounds > g.n || st.s - st.s0 >= tn.max_steps) { set_err(c, kErrIterLimit, 30); return; }
     trace_rec(c, nl, 8);
     for (long long i = gt; i < nl; i += gstride) {
@@ -2560,6 +2564,7 @@ __device__ void colour_rounds(const Args& A, Smem& sm) {
     int32_t* tmp = L;
     L = L2;
     L2 = tmp;
+    *cur = L;
     ++rounds;
     stat_inc(c, kStColourRounds);
   }
@@ -2593,13 +2598,15 @@ __device__ __forceinline__ int32_t sig_class(int32_t f, int32_t b) {
   return (int32_t)x;
 }
 
-// Residual (valid vertices after FW-BW) from which colour_mode 2 takes the
-// signature rounds.
+// colour_mode 2: the signature rounds take a residual (valid vertices
+// after FW-BW) of at least kSigMin vertices, and whatever kSigAfter colour
+// rounds leave of a smaller one.
 constexpr int32_t kSigMin = 65536;
+constexpr int kSigAfter = 4;
 
 // (not inlined: its registers are allocated apart from the default run's
 // hot loops)
-__device__ __noinline__ void signature_rounds(const Args& A, Smem& sm) {
+__device__ __noinline__ void signature_rounds(const Args& A, Smem& sm, int32_t* L, int32_t* L2) {
   Work w = A.w;
   Ctl* c = w.ctl;
   const GraphView& g = A.g;
@@ -2614,9 +2621,8 @@ __device__ __noinline__ void signature_rounds(const Args& A, Smem& sm) {
   int32_t* bw = w.live_in;
   int32_t* cls = w.live_out;
   const Adj outs = adj1(g.out), ins = adj1(g.in);
-  int32_t* L = w.listA;
-  int32_t* L2 = w.listB;
-  int rounds = 0;
+  int rounds = __ldcg(&c->ncolour_rounds);  // after colour rounds: continues their count
+  int32_t labelled_before = __ldcg(&c->ncolour);
   long long labelled = 0;
   int32_t* bufs[2] = {w.x0, w.x1};
   int32_t* hl[2] = {w.h0, w.h1};
@@ -2685,7 +2691,7 @@ __device__ __noinline__ void signature_rounds(const Args& A, Smem& sm) {
   }
   if (b == 0 && t == 0) {
     c->ncolour_rounds = rounds;
-    c->ncolour = (int32_t)labelled;
+    c->ncolour = labelled_before + (int32_t)labelled;
   }
   trace_rec(c, 0, 15);
   tally_flush(ty, c, kKColour, A.p.count_unassigned != 0, sm.red_u);
@@ -2731,13 +2737,24 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_run(Args A) {
   }
   if (!grid_barrier(c, 901)) return;
   phase_mark(A, 2);
-  // (every block reads the same count after the barrier, so all take the
-  // same branch)
-  const bool sig = A.kind == kSCC &&
-                   (A.p.colour_mode == 1 || (A.p.colour_mode == 2 && __ldcg(&c->nvalid) >= kSigMin));
-  if (sig) signature_rounds(A, sm);
-  else if (A.kind == kSCC || A.g.in.off == nullptr) colour_rounds<1>(A, sm);
-  else colour_rounds<2>(A, sm);
+  // (every block reads the same counts after a barrier, so all take the
+  // same branches)
+  const bool scc = A.kind == kSCC;
+  if (scc && (A.p.colour_mode == 1 || (A.p.colour_mode == 2 && __ldcg(&c->nvalid) >= kSigMin))) {
+    signature_rounds(A, sm, A.w.listA, A.w.listB);
+  } else {
+    // colour_mode 2: a residual still left after kSigAfter colour rounds
+    // goes on in signature rounds (a deep condensation: chains)
+    const int cap = scc && A.p.colour_mode == 2 ? kSigAfter : 0x7fffffff;
+    int32_t* cur = A.w.listA;
+    if (scc || A.g.in.off == nullptr) colour_rounds<1>(A, sm, cap, &cur);
+    else colour_rounds<2>(A, sm, cap, &cur);
+    if (cap != 0x7fffffff) {
+      if (!grid_barrier(c, 903)) return;
+      if (__ldcg(&c->nvalid) > 0 && !ld_vol(&c->err))
+        signature_rounds(A, sm, cur, cur == A.w.listA ? A.w.listB : A.w.listA);
+    }
+  }
   if (!grid_barrier(c, 902)) return;
   phase_mark(A, 3);
 }

@@ -476,3 +476,19 @@ def test_pull_hints_follow_the_rule(ctx, case):
     assert np.array_equal(ho, _hints_want(n, oo, oa, deg))
     assert np.array_equal(hi, _hints_want(n, io, ia, deg))
     g.close()
+
+
+@pytest.mark.parametrize("mode", [2, 1])
+def test_long_chain_residual(ctx, mode):
+    """A residual that is one long chain of single-vertex components (every
+    vertex also points at a sink hub): colour rounds would label one vertex
+    per round; the default switches to signature rounds after a few colour
+    rounds, which need two.  Labels equal the oracle's."""
+    n = 20001
+    s = np.concatenate([np.arange(1, n, dtype=np.int32), np.arange(1, n - 1, dtype=np.int32)])
+    d = np.concatenate([np.zeros(n - 1, np.int32), np.arange(2, n, dtype=np.int32)])
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab, st = ctx.scc(g, o=opts(colour_mode=mode), stats=True)
+    assert np.array_equal(lab, _scc_want(n, s, d))
+    assert st.colour_rounds <= 8
+    g.close()
