@@ -16,11 +16,13 @@
 //   2. FW-BW (scc_fwbw.cpp:47-466) from the valid vertex of largest
 //      out x in live degree (lowest id on ties): forward reach, backward
 //      reach inside it; their intersection is one component;
-//   3. colour rounds (scc_color.cpp:47-373) until no vertex is left: every
-//      vertex takes the smallest id that reaches it (min-colour push to the
-//      fixed point), every vertex whose colour is its own id is a root, and
-//      the vertices of its colour that reach it (backward search) are its
-//      component.
+//   3. colour rounds (scc_color.cpp:47-373): every vertex takes the
+//      smallest id that reaches it (min-colour push to the fixed point),
+//      every vertex whose colour is its own id is a root, and the vertices
+//      of its colour that reach it (backward search) are its component;
+//      after four of them, signature rounds until no vertex is left (the
+//      smallest reaching and reached ids inside classes of equal pairs;
+//      equal ids label the vertex).
 // WCC (cc_main.cpp:184-245): union-find over the edges with hooking of the
 // larger root under the smaller, so each root is its component's smallest
 // id; no fixed-point loop.
@@ -44,6 +46,7 @@ constexpr int kST = 1024;
 constexpr int kSW = kST / 32;
 constexpr uint32_t kValid = 1u, kFw = 2u, kBw = 4u, kInq = 8u;
 constexpr int kCtlInts = 160;
+constexpr int32_t kSmallColourRounds = 4;  // colour rounds before the signature rounds
 // control words (int32 slots of the shared control area)
 constexpr int cQn = 0;       // queue lengths [2]
 constexpr int cBad = 2;      // an edge id outside [0, n)
@@ -452,9 +455,11 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
     }
   }
 
-  // 3. colour rounds
+  // 3. colour rounds (at most kSmallColourRounds), then signature rounds for
+  // what is left
   int32_t* col = cnt_o;  // live degrees are not needed any more
-  for (int32_t round = 0; nvalid > 0 && !ctl[cStop]; ++round) {
+  int32_t round = 0;
+  for (; nvalid > 0 && !ctl[cStop] && round < kSmallColourRounds; ++round) {
     if (round >= cap) {
       ctl[cStop] = 1;
       break;
@@ -528,6 +533,77 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
       }
     }
     nvalid -= block_sum(cnt3, ctl);
+  }
+  // Signature rounds (a deep condensation, such as a long chain between
+  // cycles, would take one colour round per component): each round, fw = the
+  // smallest id reaching a vertex and bw = the smallest id it reaches, both
+  // inside its class (kept in lab[] while the vertex is valid; one class at
+  // first); fw == bw labels the vertex with that id, its SCC's smallest
+  // member; the others take the pair as their class.
+  if (nvalid > 0 && !ctl[cStop]) {
+    int32_t* fw = cnt_o;
+    int32_t* bw = cnt_i;
+    for (int v = tid; v < n; v += kST)
+      if (flg[v] & kValid) lab[v] = 0;
+    __syncthreads();
+    auto propagate = [&](int32_t* val, const int32_t* off, const int32_t* adj) {
+      if (tid == 0) qn[0] = 0;
+      __syncthreads();
+      for (int v = tid; v < n; v += kST) {
+        if (flg[v] & kValid) {
+          val[v] = v;
+          flg[v] = kValid | kInq;
+          push(q[0], &qn[0], v);
+        }
+      }
+      __syncthreads();
+      cur = 0;
+      for (int32_t it = 0;; ++it) {
+        const int nf = qn[cur];
+        if (nf == 0) break;
+        if (it >= cap) {
+          ctl[cStop] = 1;
+          break;
+        }
+        const int nx = cur ^ 1;
+        if (tid == 0) qn[nx] = 0;
+        for (int i = tid; i < nf; i += kST) atomicAnd(&flg[q[cur][i]], ~kInq);
+        __syncthreads();
+        expand_front(q[cur], nf, off, adj, g.base, pre, ctl, [&](int32_t v, int32_t w) {
+          if (!(flg[w] & kValid) || lab[w] != lab[v]) return;
+          const int32_t cv = val[v];
+          if (val[w] > cv && atomicMin(&val[w], cv) > cv && !(atomicOr(&flg[w], kInq) & kInq))
+            push(q[nx], &qn[nx], w);
+        });
+        cur = nx;
+      }
+    };
+    for (; nvalid > 0 && !ctl[cStop]; ++round) {
+      if (round >= cap) {
+        ctl[cStop] = 1;
+        break;
+      }
+      propagate(fw, ooff, g.oadj);
+      if (ctl[cStop]) break;
+      propagate(bw, ioff, g.iadj);
+      if (ctl[cStop]) break;
+      int32_t cnt4 = 0;
+      for (int v = tid; v < n; v += kST) {
+        if (flg[v] & kValid) {
+          const int32_t f = fw[v], b = bw[v];
+          if (f == b) {
+            lab[v] = f;
+            flg[v] = 0;
+            ++cnt4;
+          } else {
+            uint32_t x = (uint32_t)f * 0x9E3779B1u;
+            x ^= (uint32_t)b * 0x85EBCA77u + 0x7F4A7C15u + (x << 6) + (x >> 2);
+            lab[v] = (int32_t)x;
+          }
+        }
+      }
+      nvalid -= block_sum(cnt4, ctl);
+    }
   }
   __syncthreads();
   if (ctl[cStop]) {
