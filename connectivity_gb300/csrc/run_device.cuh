@@ -2601,7 +2601,7 @@ __device__ __forceinline__ int32_t sig_class(int32_t f, int32_t b) {
 // colour_mode 2: the signature rounds take a residual (valid vertices
 // after FW-BW) of at least kSigMin vertices, and whatever kSigAfter colour
 // rounds leave of a smaller one.
-constexpr int32_t kSigMin = 65536;
+constexpr int32_t kSigMin = 1 << 20;
 constexpr int kSigAfter = 4;
 
 // (not inlined: its registers are allocated apart from the default run's

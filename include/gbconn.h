@@ -118,7 +118,7 @@ typedef struct gb_opts {
                           whose pair matched the round before, labels the
                           vertices whose two ids agree, and never follows an
                           edge between classes again; 2 (default) signature
-                          rounds when at least 65536 vertices are left after
+                          rounds when at least 1048576 vertices are left after
                           FW-BW, else colour rounds.  Same labels. */
 } gb_opts;
 
