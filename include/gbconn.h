@@ -119,7 +119,8 @@ typedef struct gb_opts {
                           vertices whose two ids agree, and never follows an
                           edge between classes again; 2 (default) signature
                           rounds when at least 1048576 vertices are left after
-                          FW-BW, else colour rounds.  Same labels. */
+                          FW-BW, else up to four colour rounds and signature
+                          rounds for what they leave.  Same labels. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);
