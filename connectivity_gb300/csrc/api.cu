@@ -315,7 +315,7 @@ gb_status run_small(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* lab
   d.labels = dl;
   const int32_t max_steps = o && o->max_steps > 0 ? o->max_steps : (1 << 30);
   CK(gb::launch_small(kind == gb::kSCC ? 0 : 1, d, nullptr, 1, g->n, max_steps, &c->d_ctl->err,
-                      sm),
+                      sm, o ? o->colour_mode : 2),
      "kernel launch");
   cudaEventRecord(ev[1], sm);
   cudaEventRecord(ev[4], sm);
@@ -1115,7 +1115,7 @@ gb_status run_edges(gb_ctx* c, gb::RunKind kind, int32_t n, int64_t m, const int
   if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), sm);
   if (e == cudaSuccess)
     e = gb::launch_small(kind == gb::kSCC ? 0 : 1, sd, nullptr, 1, n, max_steps, &c->d_ctl->err,
-                         sm);
+                         sm, o->colour_mode);
   if (e == cudaSuccess && !dev_labels)
     e = cudaMemcpyAsync(labels, sd.labels, (size_t)n * 4, cudaMemcpyDeviceToHost, sm);
   if (e == cudaSuccess)

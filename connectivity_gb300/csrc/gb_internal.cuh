@@ -259,9 +259,12 @@ size_t small_smem_bytes(int32_t max_n);
 // kind 0 = SCC, 1 = WCC.  One block per graph: `count` descriptors from
 // `many` (device memory), or `one` when many is null (count 1).  A failure
 // (an id outside [0, n) in edge form: kErrInvalid; a loop past max_steps:
-// kErrIterLimit) is written to *err with atomicCAS from 0.
+// kErrIterLimit) is written to *err with atomicCAS from 0.  colour_mode as
+// in gb_opts: 0 colour rounds to the end, 1 signature rounds, 2 four colour
+// rounds and signature rounds for the rest.
 cudaError_t launch_small(int kind, const SmallDesc& one, const SmallDesc* many, int count,
-                         int32_t max_n, int32_t max_steps, int* err, cudaStream_t s);
+                         int32_t max_n, int32_t max_steps, int* err, cudaStream_t s,
+                         int32_t colour_mode = 2);
 cudaError_t widen_offsets(const uint32_t* in, int64_t* out, int64_t count, cudaStream_t s);
 // Reference-layout CSR (32-bit offsets) from device-readable host memory into
 // an int64-offset device CSR, checked on the way (*d_bad |= 1 on a bad CSR).

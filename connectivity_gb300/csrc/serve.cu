@@ -326,7 +326,8 @@ gb_status part_launch(gb_server* sv, Part& p, int kind) {
         cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), s) != cudaSuccess)
       return GB_ERR_CUDA;
     const int32_t max_steps = sv->opts.max_steps > 0 ? sv->opts.max_steps : (1 << 30);
-    if (gb::launch_small(kind, h[0], p.d_descs, ns, max_n, max_steps, &c->d_ctl->err, s) !=
+    if (gb::launch_small(kind, h[0], p.d_descs, ns, max_n, max_steps, &c->d_ctl->err, s,
+                         sv->opts.colour_mode) !=
             cudaSuccess ||
         gb::launch_latch(c->d_ctl, c->d_sticky, s) != cudaSuccess)
       return GB_ERR_CUDA;

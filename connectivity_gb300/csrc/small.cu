@@ -46,7 +46,7 @@ constexpr int kST = 1024;
 constexpr int kSW = kST / 32;
 constexpr uint32_t kValid = 1u, kFw = 2u, kBw = 4u, kInq = 8u;
 constexpr int kCtlInts = 160;
-constexpr int32_t kSmallColourRounds = 4;  // colour rounds before the signature rounds
+
 // control words (int32 slots of the shared control area)
 constexpr int cQn = 0;       // queue lengths [2]
 constexpr int cBad = 2;      // an edge id outside [0, n)
@@ -218,7 +218,8 @@ __device__ __forceinline__ void uf_unite(int32_t* p, int32_t a, int32_t b) {
 
 template <int KIND>
 __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc* many,
-                                                  int32_t max_steps, int* err) {
+                                                  int32_t max_steps, int32_t colour_rounds,
+                                                  int* err) {
   extern __shared__ int32_t smem[];
   const SmallDesc D = many ? many[blockIdx.x] : one;
   const int n = D.n;
@@ -455,11 +456,11 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
     }
   }
 
-  // 3. colour rounds (at most kSmallColourRounds), then signature rounds for
-  // what is left
+  // 3. colour rounds (at most colour_rounds), then signature rounds for what
+  // is left
   int32_t* col = cnt_o;  // live degrees are not needed any more
   int32_t round = 0;
-  for (; nvalid > 0 && !ctl[cStop] && round < kSmallColourRounds; ++round) {
+  for (; nvalid > 0 && !ctl[cStop] && round < colour_rounds; ++round) {
     if (round >= cap) {
       ctl[cStop] = 1;
       break;
@@ -615,7 +616,7 @@ __global__ void __launch_bounds__(kST, 1) k_small(SmallDesc one, const SmallDesc
 
 template <int KIND>
 cudaError_t launch_k(const SmallDesc& one, const SmallDesc* many, int count, int32_t max_n,
-                     int32_t max_steps, int* err, cudaStream_t s) {
+                     int32_t max_steps, int32_t colour_rounds, int* err, cudaStream_t s) {
   // the shared-memory attribute, once per device
   static bool attr_set[64][2] = {};
   int dev = 0;
@@ -628,7 +629,7 @@ cudaError_t launch_k(const SmallDesc& one, const SmallDesc* many, int count, int
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64) attr_set[dev][KIND] = true;
   }
-  k_small<KIND><<<count, kST, smem, s>>>(one, many, max_steps, err);
+  k_small<KIND><<<count, kST, smem, s>>>(one, many, max_steps, colour_rounds, err);
   return cudaGetLastError();
 }
 
@@ -640,11 +641,14 @@ size_t small_smem_bytes(int32_t max_n) {
 }
 
 cudaError_t launch_small(int kind, const SmallDesc& one, const SmallDesc* many, int count,
-                         int32_t max_n, int32_t max_steps, int* err, cudaStream_t s) {
+                         int32_t max_n, int32_t max_steps, int* err, cudaStream_t s,
+                         int32_t colour_mode) {
   if (count <= 0) return cudaSuccess;
   if (max_n > kSmallMaxN) return cudaErrorInvalidValue;
-  return kind == 0 ? launch_k<0>(one, many, count, max_n, max_steps, err, s)
-                   : launch_k<1>(one, many, count, max_n, max_steps, err, s);
+  // colour rounds before the signature rounds: all (0), none (1), four (2)
+  const int32_t cr = colour_mode == 0 ? 0x7fffffff : (colour_mode == 1 ? 0 : 4);
+  return kind == 0 ? launch_k<0>(one, many, count, max_n, max_steps, cr, err, s)
+                   : launch_k<1>(one, many, count, max_n, max_steps, cr, err, s);
 }
 
 }  // namespace gb

@@ -162,19 +162,34 @@ def test_automatic_choice_by_edges(ctx):
         g.close()
 
 
+def _chain_between_cycles(L):
+    n = L + 6
+    s = [0, 1, 2, n - 3, n - 2, n - 1, 2]
+    d = [1, 2, 0, n - 2, n - 1, n - 3, 3]
+    s += list(range(3, 3 + L - 1)) + [3 + L - 1]
+    d += list(range(4, 3 + L)) + [n - 3]
+    return n, np.array(s, np.int32), np.array(d, np.int32)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_one_block_colour_modes_agree(ctx, mode):
+    """The one-block path takes gb_opts.colour_mode: colour rounds to the
+    end (0), signature rounds from the start (1), or four colour rounds and
+    then signature rounds (2); the labels are the oracle's in each."""
+    for n, s, d in (_chain_between_cycles(300), graphs.rmat(11, 8, 6), graphs.grid(40)):
+        g = gb.Graph.from_edges(ctx, n, s, d)
+        lab = ctx.scc(g, o=gb.opts(small_path=2, colour_mode=mode))
+        assert np.array_equal(lab, oracle.scc(oracle.CpuGraph(n, s, d)))
+        g.close()
+
+
 @pytest.mark.parametrize("path", [0, 2])
 def test_chain_between_cycles(ctx, path):
     """Two 3-cycles joined by a 4,000-vertex chain: nothing is trimmed, and
     every chain vertex is a component of its own, so colour rounds would
     take one round per chain vertex; the signature rounds that follow the
     first colour rounds finish it.  One-block path and cooperative kernel."""
-    L = 4000
-    n = L + 6
-    s = [0, 1, 2, n - 3, n - 2, n - 1, 2]
-    d = [1, 2, 0, n - 2, n - 1, n - 3, 3]
-    s += list(range(3, 3 + L - 1)) + [3 + L - 1]
-    d += list(range(4, 3 + L)) + [n - 3]
-    s, d = np.array(s, np.int32), np.array(d, np.int32)
+    n, s, d = _chain_between_cycles(4000)
     g = gb.Graph.from_edges(ctx, n, s, d)
     lab = ctx.scc(g, o=gb.opts(small_path=path))
     assert np.array_equal(lab, oracle.scc(oracle.CpuGraph(n, s, d)))
