@@ -187,8 +187,14 @@ def _check(status: int, where: str) -> None:
         raise GBError(status, where)
 
 
-def _ptr(a: np.ndarray | None):
-    return None if a is None else a.ctypes.data_as(C.c_void_p)
+def _ptr(a):
+    """Address of a numpy array, or of anything with data_ptr() (a torch
+    tensor, host or device)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
 
 
 def _take(p: C.c_void_p, count: int, dtype) -> np.ndarray:

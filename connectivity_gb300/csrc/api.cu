@@ -545,12 +545,6 @@ gb_status gb_ctx_destroy(gb_ctx* c) {
   for (auto& set : c->ev)
     for (auto& e : set)
       if (e) cudaEventDestroy(e);
-  if (c->side) {
-    cudaStreamSynchronize(c->side);
-    cudaStreamDestroy(c->side);
-  }
-  for (auto& e : c->side_ev)
-    if (e) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return GB_OK;
@@ -737,16 +731,36 @@ gb_status gb_graph_from_csr(gb_ctx* c, int32_t n, int64_t m, const int64_t* out_
   return GB_OK;
 }
 
-// The device address of pinned host memory (the same address under unified
-// addressing), or null when p is not pinned host memory.
-static const void* pinned_view(const void* p) {
+// Whether the current device reads pageable host memory through the host's
+// page tables (Grace-class hosts), at the host link's rate; cached per
+// device.
+static bool pageable_readable() {
+  static int cache[64] = {0};  // 0 unknown, 1 no, 2 yes
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  if (cache[dev] == 0) {
+    int a = 0, b = 0;
+    cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    cache[dev] = a && b ? 2 : 1;
+  }
+  return cache[dev] == 2;
+}
+
+// An address the device's kernels can read host memory at: pinned memory's
+// device address (the same under unified addressing), pageable memory itself
+// where the device reads it through the host's page tables; null otherwise
+// (and for device memory).
+static const void* host_view(const void* p) {
   if (!p) return nullptr;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  if (a.type == cudaMemoryTypeUnregistered && pageable_readable()) return p;
+  return nullptr;
 }
 
 // Whether the host can read p (pageable, pinned or managed memory).
@@ -760,25 +774,18 @@ static bool host_readable(const void* p) {
   return a.type != cudaMemoryTypeDevice;
 }
 
-// The side stream and its events, created at first use.
-static gb_status side_stream(gb_ctx* c) {
-  if (c->side) return GB_OK;
-  CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "side stream");
-  CK(cudaEventCreateWithFlags(&c->side_ev[0], cudaEventDisableTiming), "side event");
-  CK(cudaEventCreateWithFlags(&c->side_ev[1], cudaEventDisableTiming), "side event");
-  return GB_OK;
-}
-
 // Fills g (whose buffers hold at least n / m) from the reference's CSR layout.
-// Pinned host arrays are read by the ingest kernels directly (one crossing
-// of the host link, checked on the way); other memory is copied first.
+// Host arrays the device can read (pinned, or pageable where the device
+// reads it through the host's page tables) are read by the ingest kernels
+// directly (one crossing of the host link, checked on the way); other
+// memory is copied first.
 // derive_share (directed graphs, m < 2^31): the in-lists holding the first
 // derive_share of the in-edges (targets below the split vertex) are written
 // on the device from the out-CSR while it is read, and the rest of in_array
-// is copied beside it (a DMA on the side stream for pinned memory), so the
-// device's placement and the host link share the work; 0 copies in_array
-// whole, 1 (or in_array NULL) does not read it.  The derived lists are
-// checked against idl.
+// is copied by the same kernel (tiles of both interleaved), so the device's
+// placement and the host link share the work; 0 copies in_array whole, 1
+// (or in_array NULL) does not read it.  The derived lists are checked
+// against idl.
 static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const int32_t* out_array,
                             const uint32_t* odl, const int32_t* in_array, const uint32_t* idl,
                             double derive_share) {
@@ -800,11 +807,11 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
     t_split = lo;
     e_split = (int64_t)idl[lo] <= (int64_t)m ? (int64_t)idl[lo] : (int64_t)m;
   }
-  const void* vo = pinned_view(odl);
-  const void* va = m > 0 ? pinned_view(out_array) : odl;
-  const void* vi = g->symmetric ? odl : pinned_view(idl);
+  const void* vo = host_view(odl);
+  const void* va = m > 0 ? host_view(out_array) : odl;
+  const void* vi = g->symmetric ? odl : host_view(idl);
   const void* vb = g->symmetric || m == 0 || (derive_in && e_split >= (int64_t)m) ? odl
-                                                                                  : pinned_view(in_array);
+                                                                                  : host_view(in_array);
   uint32_t* tmp = nullptr;
   if (!(vo && va && vi && vb)) {
     if (!derive_in) {
@@ -837,30 +844,20 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
     vi = tmp + n + 1;
     va = g->out_adj;
   }
-  const bool side_copy = tmp == nullptr && derive_in && e_split < (int64_t)m;
-  if (side_copy) {
-    // the copied in-lists go over the link beside the derivation
-    gb_status s = side_stream(c);
-    if (s != GB_OK) return s;
-    CK(cudaEventRecord(c->side_ev[0], c->stream), "side event");
-    CK(cudaStreamWaitEvent(c->side, c->side_ev[0], 0), "side wait");
-    CK(cudaMemcpyAsync(g->in_adj + e_split, in_array + e_split,
-                       (size_t)((int64_t)m - e_split) * 4, cudaMemcpyDefault, c->side),
-       "in-list copy");
-    CK(cudaEventRecord(c->side_ev[1], c->side), "side event");
-  }
   int* d_bad = nullptr;
   cudaError_t e = cudaMallocAsync(&d_bad, sizeof(int), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+  // the in-lists from e_split on: copied inside the derivation kernel from
+  // host memory it reads, or already staged (then checked here)
+  const bool tail_in_kernel = tmp == nullptr && e_split < (int64_t)m;
   if (e == cudaSuccess && derive_in)
     e = gb::ingest_csr32_derive_in(n, m, (const uint32_t*)vo, (const int32_t*)va,
                                    (const uint32_t*)vi, g->out_off, g->out_adj, g->in_off,
-                                   g->in_adj, t_split, d_bad, c->stream);
-  if (e == cudaSuccess && derive_in && e_split < (int64_t)m) {
-    if (side_copy) e = cudaStreamWaitEvent(c->stream, c->side_ev[1], 0);
-    if (e == cudaSuccess)
-      e = gb::check_ids_flag(n, g->in_adj + e_split, (int64_t)m - e_split, d_bad, c->stream);
-  }
+                                   g->in_adj, t_split,
+                                   tail_in_kernel ? (const int32_t*)vb : nullptr,
+                                   tail_in_kernel ? e_split : (int64_t)m, d_bad, c->stream);
+  if (e == cudaSuccess && derive_in && !tail_in_kernel && e_split < (int64_t)m)
+    e = gb::check_ids_flag(n, g->in_adj + e_split, (int64_t)m - e_split, d_bad, c->stream);
   if (e == cudaSuccess && !derive_in)
     e = gb::ingest_csr32(n, m, (const uint32_t*)vo, (const int32_t*)va, g->out_off, g->out_adj,
                          d_bad, c->stream);
@@ -871,8 +868,6 @@ static gb_status fill_csr32(gb_ctx* c, gb_graph* g, int32_t n, uint32_t m, const
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  // (on a failure above, the side copy may still be writing the graph)
-  if (side_copy) cudaStreamSynchronize(c->side);
   if (d_bad) cudaFreeAsync(d_bad, c->stream);
   if (tmp) cudaFreeAsync(tmp, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "ingest");

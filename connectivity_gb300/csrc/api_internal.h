@@ -29,10 +29,6 @@ struct gb_ctx {
   unsigned long long* d_tphase = nullptr;  // kRing x 4 device phase-boundary times
   unsigned long long* h_tphase = nullptr;  // pinned copy
   long long runs = 0;             // runs issued on this context
-  // copies that run beside the context stream's kernels (created at first
-  // use): the in-lists a split derivation copies while the rest is derived
-  cudaStream_t side = nullptr;
-  cudaEvent_t side_ev[2] = {};    // [0] context stream ready, [1] side copy done
 };
 
 struct gb_graph {

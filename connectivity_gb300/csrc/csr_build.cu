@@ -305,7 +305,8 @@ __global__ void __launch_bounds__(kPT) k_place_in(
     const int32_t* __restrict__ src_adj, int32_t* __restrict__ out_adj, int64_t m, int32_t n,
     const int64_t* __restrict__ out_off, const uint32_t* __restrict__ hub_bits,
     uint32_t* __restrict__ cursor, const int32_t* __restrict__ tile_src,
-    int32_t* __restrict__ in_adj, int32_t t_split, int* bad) {
+    int32_t* __restrict__ in_adj, int32_t t_split, const int32_t* __restrict__ src_in,
+    int64_t tail0, int* bad) {
   __shared__ int32_t head[kTile];
   __shared__ int32_t hkey[kHash];
   __shared__ uint32_t hval[kHash];  // a target's edge count in the tile, then its first slot
@@ -316,48 +317,96 @@ __global__ void __launch_bounds__(kPT) k_place_in(
   if (tid == 0) s_skip = *(volatile const int*)bad;
   __syncthreads();
   if (s_skip) return;
-  const int64_t tiles = (m + kTile - 1) / kTile;
-  const int64_t full_tiles = m / kTile;
+  // Placement tiles (the out-adjacency) and copy tiles (the in-lists from
+  // tail0 on, copied as given) are interleaved evenly in one tile order, so
+  // the blocks mix device-bound placement with link-bound copies.  Copy
+  // tiles start at the first multiple of four from tail0; the elements
+  // before it go with copy tile 0.
+  const int64_t P = (m + kTile - 1) / kTile;
+  const int64_t ca = tail0 < m ? ((tail0 + 3) & ~(int64_t)3) : m;
+  const int64_t Q = ca < m ? (m - ca + kTile - 1) / kTile : 0;
+  const int64_t U = P + Q;
   const bool vec =
       ((reinterpret_cast<uintptr_t>(src_adj) | reinterpret_cast<uintptr_t>(out_adj)) & 15u) == 0;
+  const bool tvec = Q > 0 && ((reinterpret_cast<uintptr_t>(src_in + ca) |
+                               reinterpret_cast<uintptr_t>(in_adj + ca)) & 15u) == 0;
   const bool store = src_adj != out_adj;
   const uint32_t slot_cap = (uint32_t)m;
   bool ok = true;
-  int64_t t = blockIdx.x;
+  // tile u: a copy tile when the even interleave puts one there
+  auto kind_of = [&](int64_t u, bool& copy, int64_t& t, int64_t& e0, int& len, bool& full,
+                     const int32_t*& src) {
+    const int64_t cq = Q ? u * Q / U : 0;
+    copy = Q && (u + 1) * Q / U > cq;
+    t = copy ? cq : u - cq;
+    e0 = copy ? ca + t * kTile : t * kTile;
+    len = (int)(m - e0 < kTile ? m - e0 : kTile);
+    full = len == kTile && (copy ? tvec : vec);
+    src = (copy ? src_in : src_adj) + e0;
+  };
+  int64_t u = blockIdx.x;
   // the next full tile's words, loaded one tile ahead
   int4 n0 = make_int4(0, 0, 0, 0), n1 = n0;
-  if (vec && t < full_tiles) {
-    const int4* s4 = reinterpret_cast<const int4*>(src_adj + t * kTile);
-    n0 = s4[tid];
-    n1 = s4[kPT + tid];
+  if (u < U) {
+    bool cp, fl;
+    int64_t tt, ee;
+    int ll;
+    const int32_t* sp;
+    kind_of(u, cp, tt, ee, ll, fl, sp);
+    if (fl) {
+      n0 = reinterpret_cast<const int4*>(sp)[tid];
+      n1 = reinterpret_cast<const int4*>(sp)[kPT + tid];
+    }
   }
-  for (; t < tiles; t += gridDim.x) {
-    const int64_t e0 = t * kTile;
-    const int len = (int)(m - e0 < kTile ? m - e0 : kTile);
-    // 1. the tile's targets
+  for (; u < U; u += gridDim.x) {
+    bool copy, full;
+    int64_t t, e0;
+    int len;
+    const int32_t* src;
+    kind_of(u, copy, t, e0, len, full, src);
+    // 1. the tile's words
     int32_t w[kPE];
-    if (vec && t < full_tiles) {
+    if (full) {
       const int4 q0 = n0, q1 = n1;
-      const int64_t tn = t + gridDim.x;
-      if (tn < full_tiles) {
-        const int4* s4 = reinterpret_cast<const int4*>(src_adj + tn * kTile);
-        n0 = s4[tid];
-        n1 = s4[kPT + tid];
+      if (u + gridDim.x < U) {
+        bool cp, fl;
+        int64_t tt, ee;
+        int ll;
+        const int32_t* sp;
+        kind_of(u + gridDim.x, cp, tt, ee, ll, fl, sp);
+        if (fl) {
+          n0 = reinterpret_cast<const int4*>(sp)[tid];
+          n1 = reinterpret_cast<const int4*>(sp)[kPT + tid];
+        }
       }
-      if (store) {
-        int4* d4 = reinterpret_cast<int4*>(out_adj + e0);
+      if (copy || store) {
+        int4* d4 = reinterpret_cast<int4*>((copy ? in_adj : out_adj) + e0);
         __stcs(d4 + tid, q0);
         __stcs(d4 + kPT + tid, q1);
       }
       w[0] = q0.x; w[1] = q0.y; w[2] = q0.z; w[3] = q0.w;
       w[4] = q1.x; w[5] = q1.y; w[6] = q1.z; w[7] = q1.w;
     } else {
+      int32_t* dst = (copy ? in_adj : out_adj) + e0;
 #pragma unroll
       for (int k = 0; k < kPE; ++k) {
         const int p = tile_pos(k);
-        w[k] = p < len ? src_adj[e0 + p] : 0;
-        if (p < len && store) out_adj[e0 + p] = w[k];
+        w[k] = p < len ? src[p] : 0;
+        if (p < len && (copy || store)) dst[p] = w[k];
       }
+    }
+    if (copy) {
+      // ids of copied in-lists are checked here; copy tile 0 also takes the
+      // elements from tail0 up to the first copy tile
+#pragma unroll
+      for (int k = 0; k < kPE; ++k)
+        if (tile_pos(k) < len && (uint32_t)w[k] >= (uint32_t)n) ok = false;
+      if (t == 0 && tid < ca - tail0) {
+        const int32_t x = src_in[tail0 + tid];
+        in_adj[tail0 + tid] = x;
+        if ((uint32_t)x >= (uint32_t)n) ok = false;
+      }
+      continue;
     }
     // 2. sources: every out-list starting inside the tile marks its first
     // position, the list holding edge e0 marks position 0; a max-scan then
@@ -758,9 +807,11 @@ cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int3
 cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_off,
                                    const int32_t* h_out_adj, const uint32_t* h_in_off,
                                    int64_t* out_off, int32_t* out_adj, int64_t* in_off,
-                                   int32_t* in_adj, int32_t t_split, int* d_bad,
-                                   cudaStream_t s) {
-  if (m >= (1ll << 31) || t_split < 0 || t_split > n) return cudaErrorInvalidValue;
+                                   int32_t* in_adj, int32_t t_split, const int32_t* h_in_adj,
+                                   int64_t tail0, int* d_bad, cudaStream_t s) {
+  if (m >= (1ll << 31) || t_split < 0 || t_split > n || tail0 < 0 || tail0 > m ||
+      (tail0 < m && h_in_adj == nullptr))
+    return cudaErrorInvalidValue;
   k_ingest_off<<<grid_for((int64_t)n + 1), 256, 0, s>>>(h_out_off, out_off, n, m, d_bad);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -792,9 +843,12 @@ cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_o
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       blocks[dev] = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     }
-    const int g = (int)(tiles < blocks[dev] ? tiles : blocks[dev]);
+    // placement tiles and the copy tiles of the in-lists from tail0 on
+    const int64_t ca = tail0 < m ? ((tail0 + 3) & ~(int64_t)3) : m;
+    const int64_t units = tiles + (ca < m ? (m - ca + kTile - 1) / kTile : 0);
+    const int g = (int)(units < blocks[dev] ? units : blocks[dev]);
     k_place_in<<<g, kPT, 0, s>>>(h_out_adj, out_adj, m, n, out_off, hub_bits, cursor, tile_src,
-                                 in_adj, t_split, d_bad);
+                                 in_adj, t_split, h_in_adj, tail0, d_bad);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && t_split > 0) {

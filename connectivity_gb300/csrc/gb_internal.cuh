@@ -273,14 +273,17 @@ cudaError_t ingest_csr32(int32_t n, int64_t m, const uint32_t* h_off, const int3
 // The same for a directed graph given its out-CSR and its in-offsets: the
 // in-lists of the targets below t_split are written on the device while the
 // out-lists are read (their order within a list is then not the input's);
-// the in-lists from t_split on are left to the caller (copied).  *d_bad |= 1
-// on a bad CSR or in-offsets that are not those of the out-CSR's transpose
-// (below t_split).  The adjacency may be read from out_adj itself (already
-// on the device).  m < 2^31, 0 <= t_split <= n.
+// the in-list entries from tail0 on (those of the targets from t_split on)
+// are copied from h_in_adj in the same kernel, checked against [0, n), when
+// tail0 < m (tail0 == m: the caller fills them).  *d_bad |= 1 on a bad CSR
+// or in-offsets that are not those of the out-CSR's transpose (below
+// t_split).  The adjacency may be read from out_adj itself (already on the
+// device).  m < 2^31, 0 <= t_split <= n.
 cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_off,
                                    const int32_t* h_out_adj, const uint32_t* h_in_off,
                                    int64_t* out_off, int32_t* out_adj, int64_t* in_off,
-                                   int32_t* in_adj, int32_t t_split, int* d_bad, cudaStream_t s);
+                                   int32_t* in_adj, int32_t t_split, const int32_t* h_in_adj,
+                                   int64_t tail0, int* d_bad, cudaStream_t s);
 // *d_bad |= 1 when an id of adj[0, count) is outside [0, n).  Does not wait.
 cudaError_t check_ids_flag(int32_t n, const int32_t* adj, int64_t count, int* d_bad,
                            cudaStream_t s);

@@ -212,3 +212,22 @@ def test_in_offsets_that_do_not_match_are_refused(kind):
         gb.run_scc_ref(n, oa, None, odl, idl2)
     assert e.value.status == gb.GB_ERR_INVALID
     assert np.array_equal(gb.run_scc_ref(n, oa, None, odl, idl), oracle.scc(cg))
+
+
+def test_device_arrays_take_the_staged_derivation(ctx):
+    """A CSR already in device memory is staged on the device (no host view)
+    and the in-lists are derived from the staged out-lists: the transpose's
+    lists, and the oracle's labels."""
+    torch = pytest.importorskip("torch")
+    for n, s, d in (graphs.rmat(13, 16, 31), _star_in(5000), _sparse_runs()):
+        cg = oracle.CpuGraph(n, s, d)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+        oa = dev(cg.out_adj)
+        odl = dev(cg.out_off.astype(np.int64)).to(torch.int32)
+        idl = dev(cg.in_off.astype(np.int64)).to(torch.int32)
+        g = gb.Graph.from_csr32(ctx, n, oa, odl, None, idl)
+        oo, oa2, io, ia = g.to_host()
+        assert np.array_equal(oa2, cg.out_adj) and np.array_equal(io, cg.in_off)
+        assert np.array_equal(_sorted_lists(io, ia), _sorted_lists(cg.in_off, cg.in_adj))
+        assert np.array_equal(ctx.scc(g, o=gb.opts(small_path=0)), oracle.scc(cg))
+        g.close()
