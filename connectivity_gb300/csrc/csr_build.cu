@@ -594,26 +594,39 @@ __device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& bes
   }
 }
 
-__global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* off,
-                                                     const int32_t* adj, const uint8_t* deg,
-                                                     int32_t* hint, int32_t* mid,
-                                                     int32_t* nmid, int32_t* heavy,
+// One side of the hint build: a CSR and the hints it gets.  Both sides go
+// through each tier in one launch; a listed vertex of the in-side is stored
+// as ~v.
+struct HintSide {
+  const int64_t* off;
+  const int32_t* adj;
+  int32_t* hint;
+};
+
+__global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, int sides, HintSide s0,
+                                                     HintSide s1, const uint8_t* deg,
+                                                     int32_t* mid, int32_t* nmid, int32_t* heavy,
                                                      int32_t* nheavy) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-    const int64_t s = off[v], d = off[v + 1] - s;
+  for (int64_t v2 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v2 < (int64_t)sides * n;
+       v2 += stride) {
+    const bool in = v2 >= n;
+    const int64_t v = in ? v2 - n : v2;
+    const HintSide S = in ? s1 : s0;
+    const int64_t s = S.off[v], d = S.off[v + 1] - s;
+    const int32_t tag = in ? ~(int32_t)v : (int32_t)v;
     if (d > kHintWarp) {
-      heavy[atomicAdd(nheavy, 1)] = (int32_t)v;
+      heavy[atomicAdd(nheavy, 1)] = tag;
     } else if (d > kHintThread) {
-      mid[atomicAdd(nmid, 1)] = (int32_t)v;
+      mid[atomicAdd(nmid, 1)] = tag;
     } else {
       int32_t best_d = -1;
       int64_t best_e = -1;
       for (int64_t e = 0; e < d; e += 4) {
-        const int32_t a0 = adj[s + e];
-        const int32_t a1 = e + 1 < d ? adj[s + e + 1] : -1;
-        const int32_t a2 = e + 2 < d ? adj[s + e + 2] : -1;
-        const int32_t a3 = e + 3 < d ? adj[s + e + 3] : -1;
+        const int32_t a0 = S.adj[s + e];
+        const int32_t a1 = e + 1 < d ? S.adj[s + e + 1] : -1;
+        const int32_t a2 = e + 2 < d ? S.adj[s + e + 2] : -1;
+        const int32_t a3 = e + 3 < d ? S.adj[s + e + 3] : -1;
         const int32_t d0 = deg[a0];
         const int32_t d1 = a1 >= 0 ? (int32_t)deg[a1] : -1;
         const int32_t d2 = a2 >= 0 ? (int32_t)deg[a2] : -1;
@@ -623,28 +636,30 @@ __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, const int64_t* o
         if (d2 > best_d) { best_d = d2; best_e = e + 2; }
         if (d3 > best_d) { best_d = d3; best_e = e + 3; }
       }
-      hint[v] = best_e >= 0 ? adj[s + best_e] : -1;
+      S.hint[v] = best_e >= 0 ? S.adj[s + best_e] : -1;
     }
   }
 }
 
 // A warp per middle-tier vertex, the list spread over every warp.
-__global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, const int32_t* adj,
-                                                         const uint8_t* deg, int32_t* hint,
-                                                         const int32_t* mid,
+__global__ void __launch_bounds__(kHintBlock) k_hint_mid(HintSide s0, HintSide s1,
+                                                         const uint8_t* deg, const int32_t* mid,
                                                          const int32_t* nmid) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const int32_t nm = *nmid;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nm; i += warps) {
-    const int32_t v = mid[i];
-    const int64_t s = off[v], d = off[v + 1] - s;
+    const int32_t x = mid[i];
+    const bool in = x < 0;
+    const int32_t v = in ? ~x : x;
+    const HintSide S = in ? s1 : s0;
+    const int64_t s = S.off[v], d = S.off[v + 1] - s;
     int32_t best_d = -1;
     int64_t best_e = -1;
     for (int64_t e = lane; e < d; e += 32 * kHintWU) {
       int32_t a[kHintWU], k[kHintWU];
 #pragma unroll
-      for (int q = 0; q < kHintWU; ++q) a[q] = e + 32 * q < d ? adj[s + e + 32 * q] : -1;
+      for (int q = 0; q < kHintWU; ++q) a[q] = e + 32 * q < d ? S.adj[s + e + 32 * q] : -1;
 #pragma unroll
       for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
 #pragma unroll
@@ -656,27 +671,30 @@ __global__ void __launch_bounds__(kHintBlock) k_hint_mid(const int64_t* off, con
       const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
       hint_better(d2, e2, best_d, best_e);
     }
-    if (lane == 0) hint[v] = adj[s + best_e];
+    if (lane == 0) S.hint[v] = S.adj[s + best_e];
   }
 }
 
 // A block per heavy vertex (more than kHintWarp neighbours).
-__global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const uint8_t* deg,
-                             int32_t* hint, const int32_t* heavy, const int32_t* nheavy) {
+__global__ void k_hint_heavy(HintSide s0, HintSide s1, const uint8_t* deg, const int32_t* heavy,
+                             const int32_t* nheavy) {
   __shared__ int32_t sd[32];
   __shared__ int64_t se[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nh = *nheavy;
   for (int i = blockIdx.x; i < nh; i += gridDim.x) {
-    const int32_t v = heavy[i];
-    const int64_t s = off[v], d = off[v + 1] - s;
+    const int32_t x = heavy[i];
+    const bool in = x < 0;
+    const int32_t v = in ? ~x : x;
+    const HintSide S = in ? s1 : s0;
+    const int64_t s = S.off[v], d = S.off[v + 1] - s;
     int32_t best_d = -1;
     int64_t best_e = -1;
     const int64_t T = blockDim.x;
     for (int64_t e = threadIdx.x; e < d; e += T * kHintWU) {
       int32_t a[kHintWU], k[kHintWU];
 #pragma unroll
-      for (int q = 0; q < kHintWU; ++q) a[q] = e + T * q < d ? adj[s + e + T * q] : -1;
+      for (int q = 0; q < kHintWU; ++q) a[q] = e + T * q < d ? S.adj[s + e + T * q] : -1;
 #pragma unroll
       for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
 #pragma unroll
@@ -701,7 +719,7 @@ __global__ void k_hint_heavy(const int64_t* off, const int32_t* adj, const uint8
         const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
         hint_better(d2, e2, best_d, best_e);
       }
-      if (lane == 0) hint[v] = adj[s + best_e];
+      if (lane == 0) S.hint[v] = S.adj[s + best_e];
     }
     __syncthreads();
   }
@@ -1000,30 +1018,30 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  // scratch: the middle and heavy lists (n each) and their counts, one pair
-  // per side, then the degree keys (n bytes)
+  // the sides to build, the out-side first
+  HintSide sd[2];
+  int sides = 0;
+  if (out_off && hint_out) sd[sides++] = HintSide{out_off, out_adj, hint_out};
+  if (in_off && hint_in) sd[sides++] = HintSide{in_off, in_adj, hint_in};
+  if (sides == 0) return cudaSuccess;
+  if (sides == 1) sd[1] = sd[0];
+  // scratch: the middle and heavy lists of both sides (2n each), their two
+  // counts, then the degree keys (n bytes)
   int32_t* mid = nullptr;
-  cudaError_t e = cudaMallocAsync(&mid, ((size_t)n * 2 + 4) * 4 + (size_t)n, s);
+  cudaError_t e = cudaMallocAsync(&mid, ((size_t)n * 4 + 2) * 4 + (size_t)n, s);
   if (e != cudaSuccess) return e;
-  int32_t* heavy = mid + n;
-  int32_t* cnt = heavy + n;  // [0] mid out, [1] heavy out, [2] mid in, [3] heavy in
-  uint8_t* deg = reinterpret_cast<uint8_t*>(cnt + 4);
-  cudaMemsetAsync(cnt, 0, 16, s);
+  int32_t* heavy = mid + 2 * (size_t)n;
+  int32_t* cnt = heavy + 2 * (size_t)n;  // [0] mid, [1] heavy
+  uint8_t* deg = reinterpret_cast<uint8_t*>(cnt + 2);
+  cudaMemsetAsync(cnt, 0, 8, s);
   k_degree_key<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
-  const int g = grid_for(n);
   const int gw = 152 * 8;  // 8 blocks of 8 warps per SM for the list passes
-  for (int side = 0; side < 2; ++side) {
-    const int64_t* off = side == 0 ? out_off : in_off;
-    const int32_t* adj = side == 0 ? out_adj : in_adj;
-    int32_t* hint = side == 0 ? hint_out : hint_in;
-    if (off == nullptr || hint == nullptr) continue;
-    // (the in side reuses the lists after the out side's passes, in stream
-    // order)
-    k_hint<<<g, kHintBlock, 0, s>>>(n, off, adj, deg, hint, mid, cnt + 2 * side, heavy,
-                                    cnt + 2 * side + 1);
-    k_hint_mid<<<gw, kHintBlock, 0, s>>>(off, adj, deg, hint, mid, cnt + 2 * side);
-    k_hint_heavy<<<152 * 2, 1024, 0, s>>>(off, adj, deg, hint, heavy, cnt + 2 * side + 1);
-  }
+  k_hint<<<grid_for((int64_t)sides * n), kHintBlock, 0, s>>>(n, sides, sd[0], sd[1], deg, mid,
+                                                               cnt, heavy, cnt + 1);
+  // (a side's entries carry its tag; with one side the in-side copy is the
+  // out-side's, never tagged)
+  k_hint_mid<<<gw, kHintBlock, 0, s>>>(sd[0], sd[1], deg, mid, cnt);
+  k_hint_heavy<<<152 * 2, 1024, 0, s>>>(sd[0], sd[1], deg, heavy, cnt + 1);
   cudaFreeAsync(mid, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
