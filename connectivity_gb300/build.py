@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-ffp-contract=off"]
 
 CU_SOURCES = ["kernels.cu", "kernels_options.cu", "csr_build.cu", "api.cu", "batch.cu", "noalloc.cu", "serve.cu",
-              "ingest.cu", "tune.cu", "small.cu"]
+              "ingest.cu", "tune.cu", "small.cu", "afforest.cu"]
 CPP_SOURCES = ["host_util.cpp"]
 HEADERS = ["gb_internal.cuh", "run_device.cuh", "gen_common.h", "host_internal.h", "api_internal.h"]
 

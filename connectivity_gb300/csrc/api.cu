@@ -1233,6 +1233,40 @@ gb_status gb_run_cc(int n, unsigned m, const int* out_array, const unsigned* out
   gb_ctx* c;
   gb_status s = default_ctx(&c);
   if (s != GB_OK) return s;
+  // A CSR the device reads in place: sampled union-find straight from it,
+  // which leaves most of the largest component's lists unread.
+  const void* vo = host_view(out_degree_list);
+  const void* va = m > 0 ? host_view(out_array) : out_degree_list;
+  if (vo && va && n > 0 && m < 0xfffffff0u) {
+    CK(cudaSetDevice(c->device), "cudaSetDevice");
+    const bool dev_labels = is_device_ptr(cc_maps);
+    char* buf = nullptr;
+    const size_t lab_b = dev_labels ? 0 : (size_t)n * 4;
+    CK(cudaMallocAsync((void**)&buf, lab_b + 16, c->stream), "labels");
+    int* d_flags = reinterpret_cast<int*>(buf + lab_b);  // [0] bad CSR, [1] error
+    int32_t* dl = dev_labels ? cc_maps : reinterpret_cast<int32_t*>(buf);
+    int h_flags[2] = {0, 0};
+    cudaError_t e = cudaMemsetAsync(d_flags, 0, 8, c->stream);
+    if (e == cudaSuccess)
+      e = gb::cc_sampled(n, m, (const uint32_t*)vo, (const int32_t*)va, dl, d_flags, d_flags + 1,
+                         c->stream);
+    if (e == cudaSuccess && !dev_labels)
+      e = cudaMemcpyAsync(cc_maps, dl, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h_flags, d_flags, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFreeAsync(buf, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "gb_run_cc");
+    if (h_flags[0]) {
+      gb_set_error("CSR check: %s", "offsets not monotone from 0 to m, or an id outside [0, n)");
+      return GB_ERR_INVALID;
+    }
+    if (h_flags[1]) {
+      gb_set_error("gb_run_cc: %s", "a union-find link ran out of retries");
+      return (gb_status)h_flags[1];
+    }
+    return GB_OK;
+  }
   gb_graph* g;
   if ((s = stage_graph(c, n, m, true, &g)) != GB_OK) return s;
   s = fill_csr32(c, g, n, m, out_array, out_degree_list, nullptr, nullptr, 0.0);
