@@ -57,7 +57,7 @@ class Opts(C.Structure):
         ("k_pull", C.c_int32), ("alpha", C.c_float), ("beta", C.c_float),
         ("max_steps", C.c_int32), ("grid_blocks", C.c_int32), ("trim_pairs", C.c_int32),
         ("fwbw_rounds", C.c_int32), ("expand_mode", C.c_int32), ("small_path", C.c_int32),
-        ("colour_mode", C.c_int32),
+        ("colour_mode", C.c_int32), ("wcc_mode", C.c_int32),
     ]
 
 

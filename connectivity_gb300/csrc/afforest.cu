@@ -71,26 +71,38 @@ __device__ __forceinline__ bool af_link(int32_t u, int32_t v, int32_t* p) {
   return true;
 }
 
-// Every vertex to its first kSample neighbours (the adjacency read in place).
-__global__ void k_af_sample(int32_t n, const uint32_t* __restrict__ off,
-                            const int32_t* __restrict__ adj, int32_t* parent, int* bad,
-                            int* err) {
+// One or two adjacency lists per vertex (a symmetric CSR; or the out- and
+// in-CSR of a directed graph, whose union is symmetric).
+template <typename OffT, int NC>
+struct UfCsr {
+  const OffT* off[NC];
+  const int32_t* adj[NC];
+};
+
+// Every vertex to the first kSample neighbours of each of its lists, in one
+// pass (sampling rounds with a compression between them were measured
+// slower: each round reads every vertex's list head again).
+template <typename OffT, int NC>
+__global__ void k_af_sample(int32_t n, UfCsr<OffT, NC> g, int32_t* parent, int* bad, int* err) {
   if (*(volatile const int*)bad) return;
   bool ok = true, fine = true;
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = off[v], b = off[v + 1];
-    int32_t w[kSample];
 #pragma unroll
-    for (int j = 0; j < kSample; ++j) w[j] = a + j < b ? adj[a + j] : -1;
+    for (int c = 0; c < NC; ++c) {
+      const OffT a = g.off[c][v], b = g.off[c][v + 1];
+      int32_t w[kSample];
 #pragma unroll
-    for (int j = 0; j < kSample; ++j) {
-      if (a + j >= b) continue;
-      if ((uint32_t)w[j] >= (uint32_t)n) {
-        ok = false;
-        continue;
+      for (int j = 0; j < kSample; ++j) w[j] = a + j < b ? g.adj[c][a + j] : -1;
+#pragma unroll
+      for (int j = 0; j < kSample; ++j) {
+        if (a + j >= b) continue;
+        if ((uint32_t)w[j] >= (uint32_t)n) {
+          ok = false;
+          continue;
+        }
+        fine = af_link((int32_t)v, w[j], parent) && fine;
       }
-      fine = af_link((int32_t)v, w[j], parent) && fine;
     }
   }
   if (!ok) atomicOr(bad, 1);
@@ -148,28 +160,104 @@ __global__ void __launch_bounds__(kModeSamples) k_af_mode(int32_t n, const int32
 }
 
 // Vertices outside the sampled largest component link their remaining
-// neighbours.
-__global__ void k_af_rest(int32_t n, const uint32_t* __restrict__ off,
-                          const int32_t* __restrict__ adj, int32_t* parent, const int32_t* giant,
-                          int* bad, int* err) {
+// neighbours.  A warp takes 32 vertices, finds those that have edges left
+// (outside the component), and walks their lists together, a lane per edge;
+// a vertex with more than kAfHeavy edges left goes to `heavy`, walked by
+// whole blocks in k_af_rest_heavy (a hub that the sample left outside the
+// component would otherwise hold one warp for its whole list).
+constexpr long long kAfHeavy = 4096;
+
+template <typename OffT, int NC>
+__global__ void k_af_rest(int32_t n, UfCsr<OffT, NC> g, int32_t* parent, const int32_t* giant,
+                          int32_t* heavy, int32_t* nheavy, int* bad, int* err) {
   if (*(volatile const int*)bad) return;
-  const int32_t c = *giant;
+  const int32_t cg = *giant;
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   bool ok = true, fine = true;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = off[v], b = off[v + 1];
-    if (b - a <= (uint32_t)kSample || ((volatile int32_t*)parent)[v] == c) continue;
-    for (uint32_t e = a + kSample; e < b; ++e) {
-      const int32_t w = adj[e];
-      if ((uint32_t)w >= (uint32_t)n) {
-        ok = false;
-        continue;
+  for (int64_t base = wid * 32; base < n; base += nw * 32) {
+    const int64_t v = base + lane;
+    long long left = 0;
+    if (v < n && ((volatile int32_t*)parent)[v] != cg) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const long long d = (long long)(g.off[c][v + 1] - g.off[c][v]) - kSample;
+        left += d > 0 ? d : 0;
       }
-      fine = af_link((int32_t)v, w, parent) && fine;
+    }
+    const bool big = left > kAfHeavy;
+    if (big) heavy[atomicAdd(nheavy, 1)] = (int32_t)v;
+    unsigned mask = __ballot_sync(0xffffffffu, left > 0 && !big);
+    while (mask) {
+      const int i = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int32_t u = (int32_t)(base + i);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const OffT a = g.off[c][u], b = g.off[c][u + 1];
+        for (OffT e = a + kSample + lane; e < b; e += 32) {
+          const int32_t w = g.adj[c][e];
+          if ((uint32_t)w >= (uint32_t)n) {
+            ok = false;
+            continue;
+          }
+          fine = af_link(u, w, parent) && fine;
+        }
+      }
     }
   }
   if (!ok) atomicOr(bad, 1);
   if (!fine) atomicCAS(err, 0, (int)kErrIterLimit);
+}
+
+template <typename OffT, int NC>
+__global__ void k_af_rest_heavy(int32_t n, UfCsr<OffT, NC> g, int32_t* parent,
+                                const int32_t* heavy, const int32_t* nheavy, int* bad, int* err) {
+  if (*(volatile const int*)bad) return;
+  const int nh = *nheavy;
+  bool ok = true, fine = true;
+  for (int i = blockIdx.x; i < nh; i += gridDim.x) {
+    const int32_t u = heavy[i];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const OffT a = g.off[c][u], b = g.off[c][u + 1];
+      for (OffT e = a + kSample + threadIdx.x; e < b; e += blockDim.x) {
+        const int32_t w = g.adj[c][e];
+        if ((uint32_t)w >= (uint32_t)n) {
+          ok = false;
+          continue;
+        }
+        fine = af_link(u, w, parent) && fine;
+      }
+    }
+  }
+  if (!ok) atomicOr(bad, 1);
+  if (!fine) atomicCAS(err, 0, (int)kErrIterLimit);
+}
+
+__global__ void k_af_self(int32_t n, int32_t* parent) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    parent[v] = (int32_t)v;
+}
+
+// The passes after the parents are set: sample, compress, the largest
+// component, the rest, compress.
+// scratch: [0] the largest component's root, [1] the heavy count, then n
+// heavy entries.
+template <typename OffT, int NC>
+void af_passes(int32_t n, const UfCsr<OffT, NC>& g, int32_t* parent, int32_t* scratch, int* bad,
+               int* err, cudaStream_t s) {
+  const int gr = af_grid(n);
+  cudaMemsetAsync(scratch + 1, 0, 4, s);
+  k_af_sample<OffT, NC><<<gr, 256, 0, s>>>(n, g, parent, bad, err);
+  k_af_compress<<<gr, 256, 0, s>>>(n, parent, err);
+  k_af_mode<<<1, kModeSamples, 0, s>>>(n, parent, scratch);
+  k_af_rest<OffT, NC><<<gr, 256, 0, s>>>(n, g, parent, scratch, scratch + 2, scratch + 1, bad, err);
+  k_af_rest_heavy<OffT, NC><<<152 * 2, 1024, 0, s>>>(n, g, parent, scratch + 2, scratch + 1, bad,
+                                                     err);
+  k_af_compress<<<gr, 256, 0, s>>>(n, parent, err);
 }
 
 }  // namespace
@@ -179,21 +267,45 @@ cudaError_t cc_sampled(int32_t n, int64_t m, const uint32_t* h_off, const int32_
   if (n <= 0) return cudaSuccess;
   if (m >= (1ll << 32) - 16) return cudaErrorInvalidValue;
   uint32_t* off = nullptr;
-  cudaError_t e = cudaMallocAsync(&off, ((size_t)n + 2) * 4, s);
+  cudaError_t e = cudaMallocAsync(&off, ((size_t)2 * n + 3) * 4, s);
   if (e != cudaSuccess) return e;
-  int32_t* giant = reinterpret_cast<int32_t*>(off + n + 1);
+  int32_t* giant = reinterpret_cast<int32_t*>(off + n + 1);  // and the heavy list
   int32_t* parent = labels;  // the roots become the labels
-  const int g = af_grid(n);
   k_af_init<<<af_grid((int64_t)n + 1), 256, 0, s>>>(h_off, n, m, off, parent, d_bad);
   if (m > 0) {
-    k_af_sample<<<g, 256, 0, s>>>(n, off, h_adj, parent, d_bad, d_err);
-    k_af_compress<<<g, 256, 0, s>>>(n, parent, d_err);
-    k_af_mode<<<1, kModeSamples, 0, s>>>(n, parent, giant);
-    k_af_rest<<<g, 256, 0, s>>>(n, off, h_adj, parent, giant, d_bad, d_err);
-    k_af_compress<<<g, 256, 0, s>>>(n, parent, d_err);
+    UfCsr<uint32_t, 1> g;
+    g.off[0] = off;
+    g.adj[0] = h_adj;
+    af_passes(n, g, parent, giant, d_bad, d_err, s);
   }
   e = cudaGetLastError();
   cudaFreeAsync(off, s);
+  return e;
+}
+
+cudaError_t cc_sampled_device(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+                              const int64_t* in_off, const int32_t* in_adj, int32_t* labels,
+                              int* d_bad, int* d_err, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int32_t* giant = nullptr;  // and the heavy list
+  cudaError_t e = cudaMallocAsync(&giant, ((size_t)n + 2) * 4, s);
+  if (e != cudaSuccess) return e;
+  k_af_self<<<af_grid(n), 256, 0, s>>>(n, labels);
+  if (in_off == nullptr) {
+    UfCsr<int64_t, 1> g;
+    g.off[0] = out_off;
+    g.adj[0] = out_adj;
+    af_passes(n, g, labels, giant, d_bad, d_err, s);
+  } else {
+    UfCsr<int64_t, 2> g;
+    g.off[0] = out_off;
+    g.adj[0] = out_adj;
+    g.off[1] = in_off;
+    g.adj[1] = in_adj;
+    af_passes(n, g, labels, giant, d_bad, d_err, s);
+  }
+  e = cudaGetLastError();
+  cudaFreeAsync(giant, s);
   return e;
 }
 

@@ -345,6 +345,57 @@ gb_status run_small(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* lab
   return GB_OK;
 }
 
+// WCC of a device graph by sampled union-find (cc_sampled_device): the
+// same bookkeeping as the one-block path (labels, events, status latch).
+gb_status run_sampled_cc(gb_ctx* c, const gb_graph* g, int32_t* labels, gb_stats* st,
+                         bool wait) {
+  const bool dev_labels = is_device_ptr(labels);
+  if (!wait && !dev_labels) {
+    gb_set_error("run: the asynchronous form needs device labels%s", "");
+    return GB_ERR_INVALID;
+  }
+  gb_status s = ensure_ws(c, g->n);
+  if (s != GB_OK) return s;
+  int32_t* dl = dev_labels ? labels : c->w.label;
+  cudaStream_t sm = c->stream;
+  CK(cudaMemsetAsync(&c->d_ctl->err, 0, 2 * sizeof(int), sm), "memset");
+  cudaEvent_t* ev = c->ev[c->runs % gb_ctx::kRing];
+  CK(cudaMemsetAsync(c->d_tphase + 4 * (c->runs % gb_ctx::kRing), 0,
+                     4 * sizeof(unsigned long long), sm),
+     "memset");
+  c->runs++;
+  cudaEventRecord(ev[0], sm);
+  // (a checked device graph: the id flag, err_where, stays clear)
+  CK(gb::cc_sampled_device(g->n, g->out_off, g->out_adj, g->symmetric ? nullptr : g->in_off,
+                           g->symmetric ? nullptr : g->in_adj, dl, &c->d_ctl->err_where,
+                           &c->d_ctl->err, sm),
+     "kernel launch");
+  cudaEventRecord(ev[1], sm);
+  cudaEventRecord(ev[4], sm);
+  CK(gb::launch_latch(c->d_ctl, c->d_sticky, sm), "kernel launch");
+  if (!dev_labels)
+    CK(cudaMemcpyAsync(labels, dl, (size_t)g->n * 4, cudaMemcpyDeviceToHost, sm), "labels copy");
+  CK(cudaMemcpyAsync(&c->h_ctl->err, &c->d_ctl->err, 2 * sizeof(int), cudaMemcpyDeviceToHost, sm),
+     "status copy");
+  if (!wait) return GB_OK;
+  CK(cudaStreamSynchronize(sm), "run");
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    float tot = 0.f;
+    if (cudaEventElapsedTime(&tot, ev[0], ev[4]) == cudaSuccess) st->ms_total = tot;
+    st->pivot = -1;
+    st->err_where = c->h_ctl->err_where;
+  }
+  *c->h_sticky = 0;
+  cudaMemsetAsync(c->d_sticky, 0, 2 * sizeof(int), sm);
+  const int err = c->h_ctl->err;
+  if (err != 0) {
+    gb_set_error("run: %s", "a union-find link ran out of retries");
+    return (gb_status)err;
+  }
+  return GB_OK;
+}
+
 gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t* labels,
                          const gb_opts* o, gb_stats* st, bool wait, const gb::BatchView* bv) {
   if (!c || !g) {
@@ -362,6 +413,8 @@ gb_status run_graph_impl(gb_ctx* c, const gb_graph* g, gb::RunKind kind, int32_t
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   if (g->n == 0) return GB_OK;
   if (bv == nullptr && use_small(g, o)) return run_small(c, g, kind, labels, o, st, wait);
+  if (bv == nullptr && kind == gb::kWCC && o && o->wcc_mode == 1)
+    return run_sampled_cc(c, g, labels, st, wait);
   gb_status s = ensure_ws(c, g->n);
   if (s != GB_OK) return s;
   const bool dev_labels = is_device_ptr(labels);
@@ -473,6 +526,7 @@ void gb_opts_default(gb_opts* o) {
   o->expand_mode = 0;
   o->small_path = 1;
   o->colour_mode = 2;
+  o->wcc_mode = 0;
 }
 
 gb_status gb_ctx_create(int device, gb_ctx** out) {

@@ -292,6 +292,11 @@ cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_o
 // of retries.  m < 2^32 - 16.  Does not wait.
 cudaError_t cc_sampled(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,
                        int32_t* labels, int* d_bad, int* d_err, cudaStream_t s);
+// The same for a device graph: its symmetric CSR (in_off null) or the union
+// of its out- and in-lists.
+cudaError_t cc_sampled_device(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+                              const int64_t* in_off, const int32_t* in_adj, int32_t* labels,
+                              int* d_bad, int* d_err, cudaStream_t s);
 // *d_bad |= 1 when an id of adj[0, count) is outside [0, n).  Does not wait.
 cudaError_t check_ids_flag(int32_t n, const int32_t* adj, int64_t count, int* d_bad,
                            cudaStream_t s);

@@ -121,6 +121,15 @@ typedef struct gb_opts {
                           rounds when at least 1048576 vertices are left after
                           FW-BW, else up to four colour rounds and signature
                           rounds for what they leave.  Same labels. */
+  int32_t wcc_mode;    /* WCC / CC of a device graph: 0 (default) the
+                          reference's phases (trim, BFS from the pivot,
+                          colour propagation, cc_main.cpp:184-245); 1 sampled
+                          union-find (every vertex links its first two
+                          neighbours per list, then only the vertices outside
+                          the sampled largest component link the rest; the
+                          published Afforest scheme), which gb_run_cc uses on
+                          a CSR in host memory.  Same labels.  Batches and
+                          graphs on the one-block path ignore it. */
 } gb_opts;
 
 void gb_opts_default(gb_opts* o);

@@ -1,5 +1,6 @@
-"""gb_run_cc on host arrays the device reads in place: sampled union-find
-over cc's mirrored CSR (every vertex links its first two neighbours, then
+"""Sampled union-find for WCC / CC: gb_run_cc on host arrays the device
+reads in place, and gb_wcc on device graphs (directed: the union of the
+out- and in-lists; symmetric CSRs).  On cc's mirrored CSR (every vertex links its first two neighbours, then
 only the vertices outside the sampled largest component link the rest).
 Labels must equal the oracle's on every graph, whichever component the
 sample picks; bad offsets, and out-of-range ids among the entries it reads,
@@ -72,3 +73,21 @@ def test_run_cc_refuses_a_bad_csr(kind):
         gb.run_cc_ref(n, pin(adj), pin(off2))
     assert e.value.status == gb.GB_ERR_INVALID
     assert np.array_equal(gb.run_cc_ref(n, pin(adj), pin(off)), oracle.cc(mg))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_wcc_sampled_on_device_graphs(ctx, case):
+    """gb_wcc with wcc_mode 1 on a directed device graph and on its
+    mirrored, symmetric CSR: the oracle's labels, the same as the
+    reference's phases (wcc_mode 0, the default)."""
+    name, n, s, d = case
+    want = oracle.cc(oracle.CpuGraph(n, s, d, mirror=True))
+    g = gb.Graph.from_edges(ctx, n, s, d)
+    lab = ctx.wcc(g, o=gb.opts(small_path=0, wcc_mode=1))
+    assert np.array_equal(lab, want), name
+    assert np.array_equal(ctx.wcc(g, o=gb.opts(small_path=0, wcc_mode=0)), want), name
+    g.close()
+    mg = oracle.CpuGraph(n, s, d, mirror=True)
+    sg = gb.Graph.from_csr(ctx, n, mg.out_off, mg.out_adj)
+    assert np.array_equal(ctx.wcc(sg, o=gb.opts(small_path=0, wcc_mode=1)), want), name
+    sg.close()

@@ -27,7 +27,7 @@ def test_step_cap_reports_iter_limit_then_context_recovers(ctx, case, kind):
     fn = ctx.scc if kind == "scc" else ctx.wcc
     for _ in range(2):
         with pytest.raises(gb.GBError) as e:
-            fn(g, o=gb.opts(max_steps=2, small_path=0))
+            fn(g, o=gb.opts(max_steps=2, small_path=0, wcc_mode=0))
         assert e.value.status == 5, str(e.value)  # GB_ERR_ITER_LIMIT
         lab = fn(g)
         want = (oracle.scc(oracle.CpuGraph(n, s, d)) if kind == "scc"

@@ -16,8 +16,11 @@ pytestmark = pytest.mark.gpu
 def opts(**kw):
     """Options of a run of the cooperative kernel: this file tests that
     kernel on small graphs too (the one-block path, which small graphs take
-    by default, has its own tests in test_gpu_small.py)."""
+    by default, has its own tests in test_gpu_small.py), and its WCC too
+    (the sampled union-find, the default for WCC, is tested in
+    test_gpu_cc_dropin.py)."""
     kw.setdefault("small_path", 0)
+    kw.setdefault("wcc_mode", 0)
     return gb.opts(**kw)
 
 CASES = graphs.edge_cases()
