@@ -812,12 +812,12 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
     sadj[np.repeat(soff[:-1] + odeg - io[:-1], ideg) + np.arange(m)] = ia
     sdl, sadj_p = pin(soff.astype(np.uint32)), pin(sadj)
     # what gb_run_cc reads of it in place: the offsets, every vertex's first
-    # two entries, and the rest of the lists of the vertices outside the
-    # largest component (the sampled union-find skips the others)
+    # entry, and the rest of the lists of the vertices outside the largest
+    # component (the sampled union-find skips the others)
     sdeg = np.diff(soff)
     giant = np.bincount(wcc_labels).argmax() if n else 0
-    cc_read = ((n + 1) * 4 + 4 * int(np.minimum(sdeg, 2).sum()) +
-               4 * int(np.maximum(sdeg - 2, 0)[wcc_labels != giant].sum()))
+    cc_read = ((n + 1) * 4 + 4 * int(np.minimum(sdeg, 1).sum()) +
+               4 * int(np.maximum(sdeg - 1, 0)[wcc_labels != giant].sum()))
     del sadj, soff, sdeg
     cout_p = pin(np.empty(n, np.int32))
     cpiv, cavg = ctx.pivot(g, 1)
@@ -911,7 +911,7 @@ def headline(gb, ctx, stream, args, ws, rank, local, barrier, allmax):
                         "unit": "GTEPS (mirrored arcs)",
                         "h2d_bytes_per_step": cc_read, "d2h_bytes_per_step": d2h,
                         "h2d_note": ("bytes of the pinned CSR the kernels read in place: the "
-                                     "offsets, two entries per vertex and the lists of the "
+                                     "offsets, one entry per vertex and the lists of the "
                                      "vertices outside the largest component (the host link "
                                      "moves whole sectors); the CSR is "
                                      f"{(n + 1) * 4 + 2 * m * 4} bytes"),

@@ -9,7 +9,9 @@
 // component its smallest id as root, which is the canonical label of the
 // reference's cc labels (cc_main.cpp:184-245).  The order of the work
 // follows the published Afforest scheme (Sutton, Ben-Nun and Barak, IPDPS
-// 2018): every vertex first links to its first kSample neighbours; the most
+// 2018): every vertex first links to its first kSample neighbours (one:
+// measured faster than the scheme's two on R-MAT, whose first neighbours
+// are hubs); the most
 // frequent root among a sample of vertices is then taken for the largest
 // component, and only the vertices outside it link their remaining
 // neighbours.  A vertex inside it may skip them: a neighbour outside the
@@ -22,7 +24,7 @@
 namespace gb {
 namespace {
 
-constexpr int kSample = 2;          // neighbours every vertex links first
+constexpr int kSample = 1;          // neighbours every vertex links first
 constexpr int kModeSamples = 1024;  // vertices sampled for the largest component
 constexpr int kModeHash = 2048;
 constexpr int kLinkCap = 1 << 20;   // retries of one link before it reports failure

@@ -286,8 +286,8 @@ cudaError_t ingest_csr32_derive_in(int32_t n, int64_t m, const uint32_t* h_out_o
                                    int64_t tail0, int* d_bad, cudaStream_t s);
 // Connected components of a symmetric 32-bit CSR that the device reads in
 // place (host memory it can read, or device memory), by sampled union-find
-// that never reads the largest component's lists past their first two
-// entries (afforest.cu).  labels (device, n) get each component's smallest
+// that never reads the largest component's lists past their first entry
+// (afforest.cu).  labels (device, n) get each component's smallest
 // id.  *d_bad |= 1 on a bad CSR; *d_err = kErrIterLimit when a link ran out
 // of retries.  m < 2^32 - 16.  Does not wait.
 cudaError_t cc_sampled(int32_t n, int64_t m, const uint32_t* h_off, const int32_t* h_adj,

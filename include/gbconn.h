@@ -124,8 +124,8 @@ typedef struct gb_opts {
   int32_t wcc_mode;    /* WCC / CC of a device graph: 0 (default) the
                           reference's phases (trim, BFS from the pivot,
                           colour propagation, cc_main.cpp:184-245); 1 sampled
-                          union-find (every vertex links its first two
-                          neighbours per list, then only the vertices outside
+                          union-find (every vertex links its first
+                          neighbour per list, then only the vertices outside
                           the sampled largest component link the rest; the
                           published Afforest scheme), which gb_run_cc uses on
                           a CSR in host memory.  Same labels.  Batches and

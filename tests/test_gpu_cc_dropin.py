@@ -1,6 +1,6 @@
 """Sampled union-find for WCC / CC: gb_run_cc on host arrays the device
 reads in place, and gb_wcc on device graphs (directed: the union of the
-out- and in-lists; symmetric CSRs).  On cc's mirrored CSR (every vertex links its first two neighbours, then
+out- and in-lists; symmetric CSRs).  On cc's mirrored CSR (every vertex links its first neighbour, then
 only the vertices outside the sampled largest component link the rest).
 Labels must equal the oracle's on every graph, whichever component the
 sample picks; bad offsets, and out-of-range ids among the entries it reads,
