@@ -129,6 +129,20 @@ void dev_free(void* p, bool pooled, cudaStream_t s) {
   else cudaFree(p);
 }
 
+// The hint arrays come from the stream-ordered pool whatever the graph's
+// other arrays do.  On a graph that is not pooled they are freed once the
+// whole device is idle, as cudaFree does for its other arrays.
+void hint_free(gb_graph* g, int32_t*& p) {
+  if (!p) return;
+  if (g->pooled) {
+    cudaFreeAsync(p, g->pool_stream);
+  } else {
+    cudaDeviceSynchronize();
+    cudaFree(p);
+  }
+  p = nullptr;
+}
+
 gb_status graph_alloc(gb_graph* g, bool with_in) {
   const size_t offb = (size_t)(g->n + 1) * 8, adjb = (size_t)(g->m > 0 ? g->m : 1) * 4;
   cudaStream_t s = g->pool_stream;
@@ -148,21 +162,22 @@ void graph_free(gb_graph* g) {
   dev_free(g->out_adj, g->pooled, s);
   dev_free(g->in_off, g->pooled, s);
   dev_free(g->in_adj, g->pooled, s);
-  dev_free(g->hint_out, g->pooled, s);
-  dev_free(g->hint_in, g->pooled, s);
+  hint_free(g, g->hint_out);
+  hint_free(g, g->hint_in);
   g->out_off = g->in_off = nullptr;
   g->out_adj = g->in_adj = nullptr;
   g->hint_out = g->hint_in = nullptr;
 }
 
-// Builds the pull hints of a graph whose CSR is complete on the device.
+// Builds the pull hints of a graph whose CSR is complete on the device
+// (hint arrays from the pool: a rebuild maps no memory).
 gb_status graph_hints(gb_ctx* c, gb_graph* g) {
   const size_t hb = (size_t)(g->n > 0 ? g->n : 1) * 4;
   if (!g->hint_out)
-    CK(dev_alloc((void**)&g->hint_out, hb, g->pooled, g->pool_stream), "hint allocation");
+    CK(dev_alloc((void**)&g->hint_out, hb, true, c->stream), "hint allocation");
   if (!g->symmetric && !g->hint_in)
-    CK(dev_alloc((void**)&g->hint_in, hb, g->pooled, g->pool_stream), "hint allocation");
-  CK(gb::build_hints(g->n, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
+    CK(dev_alloc((void**)&g->hint_in, hb, true, c->stream), "hint allocation");
+  CK(gb::build_hints(g->n, g->m, g->out_off, g->out_adj, g->in_off, g->in_adj, g->hint_out, g->hint_in,
                      c->stream),
      "hints");
   return GB_OK;
@@ -576,6 +591,22 @@ gb_status gb_ctx_create(int device, gb_ctx** out) {
     if (s != GB_OK) break;
     c->grid = gb::max_coop_grid(device);
     if (c->grid <= 0) { gb_set_error("gb_ctx_create: %s", "no cooperative occupancy"); s = GB_ERR_UNSUPPORTED; break; }
+    // Scratch freed through the stream-ordered allocator stays reserved in
+    // the device's pool, up to kPoolKeep, instead of going back to the
+    // driver at every synchronise: per-call scratch (hint lists, union-find
+    // parents, staged labels) is then not mapped afresh on every call.  A
+    // larger threshold already set in the process is left as it is.
+    constexpr uint64_t kPoolKeep = 4ull << 30;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t cur = 0;
+      if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur) == cudaSuccess &&
+          cur < kPoolKeep) {
+        uint64_t keep = kPoolKeep;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    }
+    cudaGetLastError();
   } while (0);
   if (s != GB_OK) {
     gb_ctx_destroy(c);
@@ -1073,9 +1104,8 @@ gb_status gb_graph_set_hints(gb_ctx* c, gb_graph* g, int32_t on) {
   // runs already queued on the context may still read the hints
   CK(cudaStreamSynchronize(c->stream), "gb_graph_set_hints");
   if (on) return graph_hints(c, g);
-  gb::dev_free(g->hint_out, g->pooled, g->pool_stream);
-  gb::dev_free(g->hint_in, g->pooled, g->pool_stream);
-  g->hint_out = g->hint_in = nullptr;
+  gb::hint_free(g, g->hint_out);
+  gb::hint_free(g, g->hint_in);
   return GB_OK;
 }
 

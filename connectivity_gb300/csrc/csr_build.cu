@@ -13,6 +13,7 @@
 #include "gb_internal.cuh"
 #include "gen_common.h"
 
+#include <algorithm>
 #include <cstring>
 
 namespace gb {
@@ -569,29 +570,38 @@ __global__ void k_degree_key(int32_t n, const int64_t* out_off, const int64_t* i
 }
 
 // The pull hint of a vertex: its neighbour of largest degree key, the first
-// one in adjacency order on ties (-1 without neighbours).  Vertices
-// are taken in three tiers by degree, each spread evenly over the grid:
-//   <= kHintThread neighbours: one thread, four loads in flight at a time
+// one in adjacency order on ties (-1 without neighbours).  Vertices are
+// taken in three tiers by degree:
+//   <= kHintThread neighbours: one thread, eight loads in flight at a time
 //      (most vertices of a power-law graph);
-//   <= kHintWarp: appended to `mid`, then a warp per vertex in k_hint_mid
-//      (four loads in flight per lane),
-//      warps taking the list's vertices in turn;
-//   more: appended to `heavy`, then a block per vertex in k_hint_heavy.
-// Walking the middle tier inside the pass that finds it (a warp over the
-// middle vertices among its own 32) or cutting the adjacency into
-// warp-sized pieces of 32 consecutive vertices leaves long tails: R-MAT
-// puts its high-degree vertices at neighbouring ids.
+//   <= kHintWarp: appended to `mid`, then half a warp per vertex in
+//      k_hint_mid (two vertices per warp, eight loads in flight per lane);
+//   more: the vertex gets an ordinal in `heavy` and its list is cut into
+//      chunks of kHintChunk entries, each appended to `chunk`; a warp per
+//      chunk in k_hint_heavy folds the chunk's best (key, position) into the
+//      ordinal's slot with a 64-bit atomicMax, and k_hint_slots turns the
+//      slots into hints.  A hub's list is then spread over many warps.
+// Appends to the middle and heavy lists take one atomic per warp.  Walking
+// the middle tier inside the pass that finds it, or cutting the adjacency
+// into pieces of 32 consecutive vertices, leaves long tails: R-MAT puts its
+// high-degree vertices at neighbouring ids.
 constexpr int kHintThread = 32;
 constexpr int kHintWarp = 2048;
 constexpr int kHintBlock = 256;
-constexpr int kHintWU = 4;  // loads in flight per lane, warp and block tiers
+constexpr int kHintThreadWU = 8;  // loads in flight per thread, thread tier
+constexpr int kHintMidWU = 8;     // per lane, middle tier
+constexpr int kHintHeavyWU = 8;   // and heavy tier
+constexpr int kHintChunk = 32 * kHintHeavyWU * 4;  // 1,024 entries: four rounds of a warp
 
-__device__ __forceinline__ void hint_better(int32_t d2, int64_t e2, int32_t& best_d,
-                                            int64_t& best_e) {
-  if (d2 > best_d || (d2 == best_d && e2 >= 0 && (best_e < 0 || e2 < best_e))) {
-    best_d = d2;
-    best_e = e2;
-  }
+// (key, position) packed so that the larger key wins and, between equal
+// keys, the earlier position: 16 bits of position in the middle tier
+// (lists of at most kHintWarp entries), 48 in the heavy tier.
+__device__ __forceinline__ uint32_t mid_pack(int32_t key, int32_t e) {
+  return ((uint32_t)key << 16) | (0xFFFFu - (uint32_t)e);
+}
+constexpr uint64_t kHintPos48 = (1ull << 48) - 1;
+__device__ __forceinline__ uint64_t heavy_pack(int32_t key, int64_t e) {
+  return ((uint64_t)key << 48) | (kHintPos48 - (uint64_t)e);
 }
 
 // One side of the hint build: a CSR and the hints it gets.  Both sides go
@@ -603,126 +613,196 @@ struct HintSide {
   int32_t* hint;
 };
 
+// The lists the first pass fills.  count: [0] middle vertices, [1] heavy
+// vertices (ordinals), [2] heavy chunks.
+struct HintLists {
+  int32_t* mid;
+  int32_t* heavy;                // tag of each heavy ordinal
+  unsigned long long* slot;      // packed best of each heavy ordinal (zeroed)
+  int64_t* chunk;                // (ordinal << 32) | chunk index
+  unsigned long long* count;
+  int64_t heavy_cap, chunk_cap;  // bounds the sizes guarantee (checked anyway)
+};
+
+__device__ __forceinline__ HintSide side_of(int32_t x, const HintSide s0, const HintSide s1) {
+  return x < 0 ? s1 : s0;
+}
+
 __global__ void __launch_bounds__(kHintBlock) k_hint(int32_t n, int sides, HintSide s0,
                                                      HintSide s1, const uint8_t* deg,
-                                                     int32_t* mid, int32_t* nmid, int32_t* heavy,
-                                                     int32_t* nheavy) {
+                                                     HintLists L) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const int64_t total = (int64_t)sides * n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t v2 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v2 < (int64_t)sides * n;
-       v2 += stride) {
+  // the bound is tested on the warp's first vertex, so that every lane of a
+  // warp takes part in the appends' ballots
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); b < total;
+       b += stride) {
+    const int64_t v2 = b + lane;
+    const bool live = v2 < total;
     const bool in = v2 >= n;
     const int64_t v = in ? v2 - n : v2;
     const HintSide S = in ? s1 : s0;
-    const int64_t s = S.off[v], d = S.off[v + 1] - s;
+    int64_t s = 0, d = 0;
+    if (live) {
+      s = S.off[v];
+      d = S.off[v + 1] - s;
+    }
     const int32_t tag = in ? ~(int32_t)v : (int32_t)v;
-    if (d > kHintWarp) {
-      heavy[atomicAdd(nheavy, 1)] = tag;
-    } else if (d > kHintThread) {
-      mid[atomicAdd(nmid, 1)] = tag;
-    } else {
-      int32_t best_d = -1;
-      int64_t best_e = -1;
-      for (int64_t e = 0; e < d; e += 4) {
-        const int32_t a0 = S.adj[s + e];
-        const int32_t a1 = e + 1 < d ? S.adj[s + e + 1] : -1;
-        const int32_t a2 = e + 2 < d ? S.adj[s + e + 2] : -1;
-        const int32_t a3 = e + 3 < d ? S.adj[s + e + 3] : -1;
-        const int32_t d0 = deg[a0];
-        const int32_t d1 = a1 >= 0 ? (int32_t)deg[a1] : -1;
-        const int32_t d2 = a2 >= 0 ? (int32_t)deg[a2] : -1;
-        const int32_t d3 = a3 >= 0 ? (int32_t)deg[a3] : -1;
-        if (d0 > best_d) { best_d = d0; best_e = e; }
-        if (d1 > best_d) { best_d = d1; best_e = e + 1; }
-        if (d2 > best_d) { best_d = d2; best_e = e + 2; }
-        if (d3 > best_d) { best_d = d3; best_e = e + 3; }
+    const bool heavy = live && d > kHintWarp;
+    const bool middle = live && d > kHintThread && !heavy;
+    const unsigned bm = __ballot_sync(0xffffffffu, middle);
+    if (bm) {
+      const int leader = __ffs(bm) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&L.count[0], (unsigned long long)__popc(bm));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (middle) L.mid[base + __popc(bm & below)] = tag;
+    }
+    const unsigned bh = __ballot_sync(0xffffffffu, heavy);
+    if (bh) {
+      const int leader = __ffs(bh) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&L.count[1], (unsigned long long)__popc(bh));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (heavy) {
+        const int64_t j = (int64_t)base + __popc(bh & below);
+        const int64_t c = (d + kHintChunk - 1) / kHintChunk;
+        const int64_t c0 = (int64_t)atomicAdd(&L.count[2], (unsigned long long)c);
+        if (j < L.heavy_cap) {
+          L.heavy[j] = tag;
+          for (int64_t q = 0; q < c && c0 + q < L.chunk_cap; ++q)
+            L.chunk[c0 + q] = (j << 32) | q;
+        }
       }
-      S.hint[v] = best_e >= 0 ? S.adj[s + best_e] : -1;
+    }
+    if (live && d <= kHintThread) {
+      int32_t best_d = -1, best_a = -1;
+      for (int64_t e = 0; e < d; e += kHintThreadWU) {
+        int32_t a[kHintThreadWU], k[kHintThreadWU];
+#pragma unroll
+        for (int q = 0; q < kHintThreadWU; ++q) a[q] = e + q < d ? S.adj[s + e + q] : -1;
+#pragma unroll
+        for (int q = 0; q < kHintThreadWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
+#pragma unroll
+        for (int q = 0; q < kHintThreadWU; ++q)
+          if (k[q] > best_d) {
+            best_d = k[q];
+            best_a = a[q];
+          }
+      }
+      S.hint[v] = best_a;
     }
   }
 }
 
-// A warp per middle-tier vertex, the list spread over every warp.
+// Half a warp per middle-tier vertex, two vertices per warp, the list
+// spread over every warp.  A half-warp reads the tag and offsets of its next
+// vertex before it walks the current one, so that those loads overlap.
 __global__ void __launch_bounds__(kHintBlock) k_hint_mid(HintSide s0, HintSide s1,
                                                          const uint8_t* deg, const int32_t* mid,
-                                                         const int32_t* nmid) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int32_t nm = *nmid;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nm; i += warps) {
-    const int32_t x = mid[i];
-    const bool in = x < 0;
-    const int32_t v = in ? ~x : x;
-    const HintSide S = in ? s1 : s0;
-    const int64_t s = S.off[v], d = S.off[v + 1] - s;
-    int32_t best_d = -1;
-    int64_t best_e = -1;
-    for (int64_t e = lane; e < d; e += 32 * kHintWU) {
-      int32_t a[kHintWU], k[kHintWU];
-#pragma unroll
-      for (int q = 0; q < kHintWU; ++q) a[q] = e + 32 * q < d ? S.adj[s + e + 32 * q] : -1;
-#pragma unroll
-      for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
-#pragma unroll
-      for (int q = 0; q < kHintWU; ++q)
-        if (k[q] > best_d) { best_d = k[q]; best_e = e + 32 * q; }
+                                                         const unsigned long long* nmid) {
+  const int lane = threadIdx.x & 31, hl = lane & 15;
+  const int64_t halves = (int64_t)gridDim.x * (blockDim.x >> 4);
+  const int64_t nm = (int64_t)*nmid;
+  int64_t b = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;
+  int32_t x = 0, d = 0;
+  int64_t s = 0;
+  if (b + (lane >> 4) < nm) {
+    x = mid[b + (lane >> 4)];
+    const HintSide S = side_of(x, s0, s1);
+    const int32_t v = x < 0 ? ~x : x;
+    s = S.off[v];
+    d = (int32_t)(S.off[v + 1] - s);
+  }
+  for (; b < nm; b += halves) {
+    const int64_t i = b + (lane >> 4);
+    const bool live = i < nm;
+    const int32_t v = x < 0 ? ~x : x;
+    const HintSide S = side_of(x, s0, s1);
+    const int64_t cs = s;
+    const int32_t cd = d;
+    // the next vertex's header
+    x = 0;
+    d = 0;
+    s = 0;
+    if (i + halves < nm) {
+      x = mid[i + halves];
+      const HintSide N = side_of(x, s0, s1);
+      const int32_t vn = x < 0 ? ~x : x;
+      s = N.off[vn];
+      d = (int32_t)(N.off[vn + 1] - s);
     }
-    for (int o = 16; o; o >>= 1) {
-      const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
-      const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
-      hint_better(d2, e2, best_d, best_e);
+    uint32_t best = 0;
+    for (int32_t e = hl; e < cd; e += 16 * kHintMidWU) {
+      int32_t a[kHintMidWU];
+#pragma unroll
+      for (int q = 0; q < kHintMidWU; ++q) a[q] = e + 16 * q < cd ? S.adj[cs + e + 16 * q] : -1;
+#pragma unroll
+      for (int q = 0; q < kHintMidWU; ++q)
+        if (a[q] >= 0) best = max(best, mid_pack(deg[a[q]], e + 16 * q));
     }
-    if (lane == 0) S.hint[v] = S.adj[s + best_e];
+    for (int o = 8; o; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (live && hl == 0) S.hint[v] = S.adj[cs + (int32_t)(0xFFFFu - (best & 0xFFFFu))];
   }
 }
 
-// A block per heavy vertex (more than kHintWarp neighbours).
-__global__ void k_hint_heavy(HintSide s0, HintSide s1, const uint8_t* deg, const int32_t* heavy,
-                             const int32_t* nheavy) {
-  __shared__ int32_t sd[32];
-  __shared__ int64_t se[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nh = *nheavy;
-  for (int i = blockIdx.x; i < nh; i += gridDim.x) {
-    const int32_t x = heavy[i];
-    const bool in = x < 0;
-    const int32_t v = in ? ~x : x;
-    const HintSide S = in ? s1 : s0;
+// A warp per chunk of a heavy vertex's list: the chunk's best folded into
+// the vertex's slot.
+__global__ void __launch_bounds__(kHintBlock, 8) k_hint_heavy(HintSide s0, HintSide s1,
+                                                           const uint8_t* deg, HintLists L) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t nc = min((int64_t)L.count[2], L.chunk_cap);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nc; i += warps) {
+    const int64_t c = L.chunk[i];
+    const int64_t j = c >> 32;
+    const int32_t x = L.heavy[j];
+    const int32_t v = x < 0 ? ~x : x;
+    const HintSide S = side_of(x, s0, s1);
     const int64_t s = S.off[v], d = S.off[v + 1] - s;
-    int32_t best_d = -1;
-    int64_t best_e = -1;
-    const int64_t T = blockDim.x;
-    for (int64_t e = threadIdx.x; e < d; e += T * kHintWU) {
-      int32_t a[kHintWU], k[kHintWU];
+    const int64_t e0 = (c & 0xffffffffll) * kHintChunk;
+    const int64_t e1 = min(d, e0 + kHintChunk);
+    unsigned long long best = 0;
+    for (int64_t e = e0 + lane; e < e1; e += 32 * kHintHeavyWU) {
+      int32_t a[kHintHeavyWU];
 #pragma unroll
-      for (int q = 0; q < kHintWU; ++q) a[q] = e + T * q < d ? S.adj[s + e + T * q] : -1;
+      for (int q = 0; q < kHintHeavyWU; ++q) a[q] = e + 32 * q < e1 ? S.adj[s + e + 32 * q] : -1;
 #pragma unroll
-      for (int q = 0; q < kHintWU; ++q) k[q] = a[q] >= 0 ? (int32_t)deg[a[q]] : -1;
-#pragma unroll
-      for (int q = 0; q < kHintWU; ++q)
-        if (k[q] > best_d) { best_d = k[q]; best_e = e + T * q; }
+      for (int q = 0; q < kHintHeavyWU; ++q)
+        if (a[q] >= 0) best = max(best, (unsigned long long)heavy_pack(deg[a[q]], e + 32 * q));
     }
-    for (int o = 16; o; o >>= 1) {
-      const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
-      const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
-      hint_better(d2, e2, best_d, best_e);
-    }
-    if (lane == 0) {
-      sd[wid] = best_d;
-      se[wid] = best_e;
-    }
-    __syncthreads();
-    if (wid == 0) {
-      best_d = lane < (int)(blockDim.x >> 5) ? sd[lane] : -1;
-      best_e = lane < (int)(blockDim.x >> 5) ? se[lane] : -1;
-      for (int o = 16; o; o >>= 1) {
-        const int32_t d2 = __shfl_xor_sync(0xffffffffu, best_d, o);
-        const int64_t e2 = __shfl_xor_sync(0xffffffffu, best_e, o);
-        hint_better(d2, e2, best_d, best_e);
-      }
-      if (lane == 0) S.hint[v] = S.adj[s + best_e];
-    }
-    __syncthreads();
+    for (int o = 16; o; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (lane == 0) atomicMax(&L.slot[j], best);
   }
+}
+
+// Heavy ordinals' slots -> hints.
+__global__ void k_hint_slots(HintSide s0, HintSide s1, HintLists L) {
+  const int64_t nh = min((int64_t)L.count[1], L.heavy_cap);
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nh;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t x = L.heavy[j];
+    const int32_t v = x < 0 ? ~x : x;
+    const HintSide S = side_of(x, s0, s1);
+    const unsigned long long best = L.slot[j];  // non-zero once a chunk folded in
+    const uint64_t e = kHintPos48 - (best & kHintPos48);
+    S.hint[v] = best ? S.adj[S.off[v] + (int64_t)e] : -1;
+  }
+}
+
+// Blocks of `threads` threads of kernel k resident at once on the current
+// device (at least one per SM).
+template <typename K>
+int resident_grid(K k, int threads) {
+  int dev = 0, sms = 152, per = 1;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, 0) != cudaSuccess || per < 1)
+    per = 1;
+  cudaGetLastError();
+  return sms * per;
 }
 
 int bits_for(int32_t n) {
@@ -1014,7 +1094,7 @@ cudaError_t launch_latch(Ctl* ctl, int* sticky, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+cudaError_t build_hints(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
@@ -1025,24 +1105,39 @@ cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_ad
   if (in_off && hint_in) sd[sides++] = HintSide{in_off, in_adj, hint_in};
   if (sides == 0) return cudaSuccess;
   if (sides == 1) sd[1] = sd[0];
-  // scratch: the middle and heavy lists of both sides (2n each), their two
-  // counts, then the degree keys (n bytes)
-  int32_t* mid = nullptr;
-  cudaError_t e = cudaMallocAsync(&mid, ((size_t)n * 4 + 2) * 4 + (size_t)n, s);
+  // Scratch: the heavy slots and the three counts (zeroed together), the
+  // chunks, the middle list (a vertex-side each at most), the heavy tags,
+  // then the degree keys (n bytes).  A side holds m entries, so at most
+  // 2m / (kHintWarp + 1) vertex-sides are heavy and their lists make at most
+  // 2m / kHintChunk + (heavy vertex-sides) chunks.
+  const int64_t mm = m > 0 ? m : 0;
+  HintLists L;
+  L.heavy_cap = std::min<int64_t>(2 * (int64_t)n, 2 * mm / (kHintWarp + 1) + 1);
+  L.chunk_cap = 2 * mm / kHintChunk + L.heavy_cap;
+  const size_t zero_b = ((size_t)L.heavy_cap + 4) * 8;
+  const size_t bytes = zero_b + (size_t)L.chunk_cap * 8 + (size_t)2 * n * 4 +
+                       (size_t)L.heavy_cap * 4 + (size_t)n;
+  char* buf = nullptr;
+  cudaError_t e = cudaMallocAsync(&buf, bytes, s);
   if (e != cudaSuccess) return e;
-  int32_t* heavy = mid + 2 * (size_t)n;
-  int32_t* cnt = heavy + 2 * (size_t)n;  // [0] mid, [1] heavy
-  uint8_t* deg = reinterpret_cast<uint8_t*>(cnt + 2);
-  cudaMemsetAsync(cnt, 0, 8, s);
+  L.slot = reinterpret_cast<unsigned long long*>(buf);
+  L.count = L.slot + L.heavy_cap;
+  L.chunk = reinterpret_cast<int64_t*>(L.count + 4);
+  L.mid = reinterpret_cast<int32_t*>(L.chunk + L.chunk_cap);
+  L.heavy = L.mid + 2 * (size_t)n;
+  uint8_t* deg = reinterpret_cast<uint8_t*>(L.heavy + L.heavy_cap);
+  cudaMemsetAsync(buf, 0, zero_b, s);
   k_degree_key<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
-  const int gw = 152 * 8;  // 8 blocks of 8 warps per SM for the list passes
-  k_hint<<<grid_for((int64_t)sides * n), kHintBlock, 0, s>>>(n, sides, sd[0], sd[1], deg, mid,
-                                                               cnt, heavy, cnt + 1);
+  // the list passes: as many blocks as are resident at once on the SMs
+  static const int gw_mid = resident_grid(k_hint_mid, kHintBlock);
+  static const int gw_heavy = resident_grid(k_hint_heavy, kHintBlock);
   // (a side's entries carry its tag; with one side the in-side copy is the
   // out-side's, never tagged)
-  k_hint_mid<<<gw, kHintBlock, 0, s>>>(sd[0], sd[1], deg, mid, cnt);
-  k_hint_heavy<<<152 * 2, 1024, 0, s>>>(sd[0], sd[1], deg, heavy, cnt + 1);
-  cudaFreeAsync(mid, s);
+  k_hint<<<grid_for((int64_t)sides * n), kHintBlock, 0, s>>>(n, sides, sd[0], sd[1], deg, L);
+  k_hint_mid<<<gw_mid, kHintBlock, 0, s>>>(sd[0], sd[1], deg, L.mid, L.count);
+  k_hint_heavy<<<gw_heavy, kHintBlock, 0, s>>>(sd[0], sd[1], deg, L);
+  k_hint_slots<<<grid_for(L.heavy_cap), 256, 0, s>>>(sd[0], sd[1], L);
+  cudaFreeAsync(buf, s);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return cudaStreamSynchronize(s);

@@ -305,8 +305,9 @@ cudaError_t launch_localize(int32_t* labels, int32_t n, const int32_t* gid, cons
                             cudaStream_t s);
 // Pull hints: for every vertex, its neighbour of largest degree key (the
 // total degree, above 32 rounded down to eight steps per power of two) in
-// each CSR (hint_in may be null when in_off is).  Synchronises the stream.
-cudaError_t build_hints(int32_t n, const int64_t* out_off, const int32_t* out_adj,
+// each CSR of m entries (hint_in may be null when in_off is).  Synchronises
+// the stream.
+cudaError_t build_hints(int32_t n, int64_t m, const int64_t* out_off, const int32_t* out_adj,
                         const int64_t* in_off, const int32_t* in_adj, int32_t* hint_out,
                         int32_t* hint_in, cudaStream_t s);
 // Seeded R-MAT edge list on the device for n vertices: edge_factor * n

@@ -456,9 +456,19 @@ def _hints_want(n, off, adj, deg):
     return want.astype(np.int32)
 
 
-@pytest.mark.parametrize("case", ["rmat16", "rmat20", "hub", "star"])
+@pytest.mark.parametrize("case", ["rmat16", "rmat20", "hub", "hub_big", "star"])
 def test_pull_hints_follow_the_rule(ctx, case):
-    if case == "rmat16":
+    if case == "hub_big":
+        # a list of 300,000 entries (hundreds of 1,024-entry chunks, equal
+        # keys in many of them) and in-lists of every size around it
+        n = 400000
+        r = np.random.default_rng(5)
+        s = np.concatenate([np.zeros(300000, np.int32), r.integers(0, n, 400000).astype(np.int32),
+                            np.full(3000, 11, np.int32)])
+        d = np.concatenate([np.arange(1, 300001, dtype=np.int32),
+                            r.integers(0, n, 400000).astype(np.int32),
+                            r.integers(0, 50, 3000).astype(np.int32)])
+    elif case == "rmat16":
         n, s, d = gb.rmat_edges(16, 16, 1)
     elif case == "rmat20":
         n, s, d = gb.rmat_edges(20, 16, 1)
