@@ -1126,7 +1126,11 @@ cudaError_t build_hints(int32_t n, int64_t m, const int64_t* out_off, const int3
   L.mid = reinterpret_cast<int32_t*>(L.chunk + L.chunk_cap);
   L.heavy = L.mid + 2 * (size_t)n;
   uint8_t* deg = reinterpret_cast<uint8_t*>(L.heavy + L.heavy_cap);
-  cudaMemsetAsync(buf, 0, zero_b, s);
+  e = cudaMemsetAsync(buf, 0, zero_b, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(buf, s);
+    return e;
+  }
   k_degree_key<<<grid_for(n), 256, 0, s>>>(n, out_off, in_off, deg);
   // the list passes: as many blocks as are resident at once on the SMs
   static const int gw_mid = resident_grid(k_hint_mid, kHintBlock);
