@@ -167,6 +167,13 @@ typedef struct gb_stats {
 } gb_stats;
 
 /* ---- contexts --------------------------------------------------------- */
+/* A context owns a stream, its control block and event ring on `device`.
+ * It raises the release threshold of the device's default memory pool
+ * (cudaDeviceGetDefaultMemPool) to at least 4 GB, process-wide, so that
+ * memory freed with cudaFreeAsync stays reserved for the next call instead
+ * of going back to the driver at every synchronise; a larger threshold set
+ * before is left as it is.  A host that wants its own threshold sets it
+ * after creating its contexts. */
 gb_status gb_ctx_create(int device, gb_ctx** ctx);
 gb_status gb_ctx_destroy(gb_ctx* ctx);
 /* Use an existing cudaStream_t (e.g. a framework's current stream) for all
