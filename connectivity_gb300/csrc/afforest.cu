@@ -11,10 +11,9 @@
 // follows the published Afforest scheme (Sutton, Ben-Nun and Barak, IPDPS
 // 2018): every vertex first links to its first kSample neighbours (one:
 // measured faster than the scheme's two on R-MAT, whose first neighbours
-// are hubs); the most
-// frequent root among a sample of vertices is then taken for the largest
-// component, and only the vertices outside it link their remaining
-// neighbours.  A vertex inside it may skip them: a neighbour outside the
+// are hubs); the most frequent root among a sample of vertices is then
+// taken for the largest component, and only the vertices outside it link
+// their remaining neighbours.  A vertex inside it may skip them: a neighbour outside the
 // component holds the same edge in its own list (the CSR is symmetric) and
 // links it from there.
 #include <cstdint>
